@@ -1,0 +1,202 @@
+/*
+ * srs_gb300.h — C ABI of the GB300-native (sm_103a) spark timestep.
+ *
+ * The reference (mwalker174/srs) has no plugin or FFI layer: its seam is the
+ * C++ function set declared in cpu/parameters.h:252-275 (ReadParameters,
+ * ReadGrid, InitializeDomainStruct, ResetDefaultGridStates, RunSimulation,
+ * ExplicitStep, UpdateChannelGating, WriteToStateFiles, ...), plus the
+ * on-disk mesh / XML / states formats.  Each entry point below replaces one
+ * of those functions; the comment names the reference definition.
+ *
+ * Conventions: every call returns an int status (SRS_OK == 0, negative on
+ * failure; srs_last_error() gives the message).  Host buffers are owned by
+ * the caller; device buffers are owned by the library.  Element indices,
+ * state arrays and channel arrays use the reference's numbering (the
+ * breadth-first renumbering of cpu/InitFuncs.cpp:679-793) and absolute
+ * concentrations in uM.  One CUDA stream per simulation; a simulation is not
+ * thread-safe.  No entry point falls back to the CPU: without a usable
+ * sm_103a device, srs_sim_create fails with SRS_ERR_CUDA.
+ */
+#ifndef SRS_GB300_H
+#define SRS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SRS_N_INT_PARAMS 19
+#define SRS_N_REAL_PARAMS 56
+#define SRS_N_CHAR_PARAMS 4
+#define SRS_N_SPECIES 6
+#define SRS_STATES_ROW_BASE 7
+
+enum srs_status {
+  SRS_OK = 0,
+  SRS_ERR_INPUT = -1,       /* bad argument or parameter value */
+  SRS_ERR_IO = -2,          /* file missing or malformed */
+  SRS_ERR_MESH = -3,        /* mesh not connected / inconsistent */
+  SRS_ERR_UNSTABLE = -4,    /* explicit step violates D*dt*max|a0| <= 1 */
+  SRS_ERR_CUDA = -5,        /* no sm_103a device or a CUDA call failed */
+  SRS_ERR_UNSUPPORTED = -6, /* configuration outside what the engine supports */
+  SRS_ERR_NONFINITE = -7,   /* a realization produced NaN/Inf (status word) */
+  SRS_ERR_TIMEOUT = -8,     /* a bounded device wait gave up */
+  SRS_ERR_STATE = -9,       /* call out of order */
+  SRS_ERR_NOMEM = -10
+};
+
+enum srs_precision { SRS_FP64 = 64, SRS_FP32 = 32 };
+enum srs_engine {
+  SRS_ENGINE_PLAIN = 0,   /* one fused step kernel launch per time step */
+  SRS_ENGINE_RESIDENT = 1 /* persistent batched kernel, state held on chip */
+};
+
+/* ParamStruct (cpu/parameters.h:234-246): Integers[19], Reals[56], Chars[4][255]. */
+typedef struct srs_params {
+  int ints[SRS_N_INT_PARAMS];
+  double reals[SRS_N_REAL_PARAMS];
+  char chars[SRS_N_CHAR_PARAMS][255];
+} srs_params;
+
+const char* srs_status_string(int status);
+const char* srs_last_error(void);
+const char* srs_version(void);
+
+/* ---- parameters: ReadParameters (cpu/InitFuncs.cpp:25-381) ------------- */
+void srs_default_parameters(srs_params* ps);                 /* :28-108 */
+int srs_read_parameters(srs_params* ps, const char* param_file); /* :110-364 */
+
+/* ---- mesh: ReadGrid (cpu/InitFuncs.cpp:384-813) + InitializeDomainStruct
+ *      (cpu/InitFuncs.cpp:1005-1039) / InitializeExplicitSparseMatrixFast
+ *      (cpu/InitFuncs.cpp:1058-1418) ------------------------------------ */
+typedef struct srs_grid srs_grid;
+int srs_read_grid(const srs_params* ps, const char* mesh_base, srs_grid** out);
+void srs_free_grid(srs_grid* g); /* FreeGridStruct (cpu/main.cpp:298-338) */
+
+typedef struct srs_grid_info {
+  int n_ele, n_face, n_nodes, n_ryr, n_lcc, n_jsr;
+  double vol_jsr;   /* GridStruct::Vol_JSR (cpu/InitFuncs.cpp:1032-1037) */
+  double max_diag;  /* max |a0| over elements (explicit stability bound) */
+} srs_grid_info;
+int srs_grid_get_info(const srs_grid* g, srs_grid_info* info);
+/* aij[5N], nij[4N], boundary_rates[6N] exactly as GridStruct holds them. */
+int srs_grid_get_operator(const srs_grid* g, double* aij, int* nij, double* boundary_rates);
+/* V0[N], tt_area[N], domain[N], tropc[N], file_index[N] (file order of each element). */
+int srs_grid_get_elements(const srs_grid* g, double* v0, double* tt_area, int* domain,
+                          int* tropc, int* file_index);
+/* RyR_Ele[NR], RyR_JSR_Ele[NR], RyR_Neighb[4 NR], LCC_Ele[NL] (renumbered). */
+int srs_grid_get_channels(const srs_grid* g, int* ryr_ele, int* ryr_jsr_ele, int* ryr_neighb,
+                          int* lcc_ele);
+/* ResetDefaultGridStates (cpu/InitFuncs.cpp:890-955): states[6N], species-major. */
+int srs_initial_states(const srs_grid* g, const srs_params* ps, double* states);
+
+/* ---- simulation ---------------------------------------------------------- */
+typedef struct srs_sim srs_sim;
+typedef struct srs_sim_desc {
+  int n_realizations;   /* independent realizations sharing the grid */
+  int precision;        /* SRS_FP64 or SRS_FP32 */
+  int engine;           /* SRS_ENGINE_PLAIN or SRS_ENGINE_RESIDENT */
+  int threads_per_cta;  /* 0: chosen by the tuner */
+  int cluster_size;     /* resident engine: CTAs sharing one realization, 0: tuner */
+  int steps_per_launch; /* resident engine: time steps per persistent launch, 0: tuner */
+  const uint64_t* seeds;/* n_realizations Philox keys; NULL: 1..n_realizations */
+} srs_sim_desc;
+
+/* InitializeDefaultGrid + InitializeDefaultChannels + ResetGlobals + the
+ * device upload of gpu/InitFuncs.cu:1001-1105, for R realizations. */
+int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* d,
+                   srs_sim** out);
+void srs_sim_destroy(srs_sim* s);
+int srs_sim_get_desc(const srs_sim* s, srs_sim_desc* d);
+
+/* Per-realization reset (cpu/main.cpp:216-257): equilibrium grid state,
+ * default channels, globals, initial channel opening by protocol (LCC
+ * trigger / clamp / fixed RyR / rate-weighted random RyR as OpenRandomRyR,
+ * cpu/InitFuncs.cpp:1420-1475) and initial residuals (Philox). */
+int srs_sim_reset(srs_sim* s);
+
+/* State exchange for realization r, reference numbering, absolute units.
+ * Any pointer may be NULL to skip that array.  states: 6N doubles. */
+int srs_sim_set_state(srs_sim* s, int r, const double* states, const int* ryr_states,
+                      const int* lcc_states, const int* lccv_states, const double* residuals);
+int srs_sim_get_state(srs_sim* s, int r, double* states, int* ryr_states, int* lcc_states,
+                      int* lccv_states, double* residuals);
+/* Global_Vars (V_m, Ca_NSR) for every realization. */
+int srs_sim_set_globals(srs_sim* s, double v_m, double ca_nsr);
+
+/* ExplicitStep (cpu/RunSimulation.cpp:591-654) repeated n_steps times for
+ * every realization: reactions, RyR/LCC flux, fast SL buffer, Euler update,
+ * then UpdateChannelGating (:656-674) unless I_FLAG_NO_GATING.  No protocol
+ * events and no output. */
+int srs_explicit_step(srs_sim* s, int64_t n_steps);
+
+/* RunSimulation (cpu/RunSimulation.cpp:402-589) for every realization:
+ * protocol events, termination predicate and states rows (the float32 row
+ * layout of WriteToStateFiles, cpu/OutputFuncs.cpp:223-350).  rows must hold
+ * n_realizations * row_capacity * row_width floats where row_width is
+ * SRS_STATES_ROW_BASE (+ n_ryr when I_FLAG_RYR_OUT).  n_rows[r] receives the
+ * number of rows written for realization r, t_end[r] its final time. */
+typedef struct srs_run_output {
+  float* rows;
+  int64_t row_capacity;
+  int row_width;
+  int64_t* n_rows;
+  double* t_end;
+  int64_t* n_steps;
+} srs_run_output;
+int srs_run_simulation(srs_sim* s, srs_run_output* out);
+
+/* Time-stepping without protocol, for throughput measurement: advances every
+ * realization by n_steps (gating on), device-resident, stream-ordered; the
+ * call returns after the work is enqueued.  srs_sim_synchronize waits. */
+int srs_sim_advance_async(srs_sim* s, int64_t n_steps);
+int srs_sim_synchronize(srs_sim* s);
+/* srs_sim_advance_async bracketed by CUDA events recorded on the
+ * simulation's stream; *ms receives the device time of the advance. */
+int srs_sim_time_advance(srs_sim* s, int64_t n_steps, float* ms);
+/* Device status word OR-ed over realizations (bit 0: non-finite value,
+ * bit 1: bounded wait timed out). */
+int srs_sim_status(srs_sim* s, int* status_bits);
+/* Kernel configuration actually used (engine, threads, cluster, steps/launch,
+ * dynamic shared memory bytes, kernels launched so far). */
+typedef struct srs_sim_config {
+  int engine, precision, threads_per_cta, cluster_size, steps_per_launch;
+  int smem_bytes;
+  int64_t kernel_launches;
+} srs_sim_config;
+int srs_sim_get_config(const srs_sim* s, srs_sim_config* c);
+
+/* ---- output formats (cpu/OutputFuncs.cpp) -------------------------------- */
+/* WriteToGridFiles (cpu/OutputFuncs.cpp:42-220): legacy ASCII VTK of the
+ * current state of realization r at time t. */
+int srs_write_grid_vtk(srs_sim* s, int r, const char* path, int run, int rank, int n, double t);
+
+/* ---- synthetic meshes (no reference counterpart beyond the file format of
+ * mesh/main.cpp:1305-1364): box dyad, see the generator for the geometry. */
+typedef struct srs_box_mesh_spec {
+  double box_x, box_y, box_z;
+  double foot_half_x, foot_half_y;
+  int n_foot_x, n_foot_y, n_out_x, n_out_y;
+  double cleft_h, jsr_h;
+  int n_cleft_z, n_jsr_z, n_above_z;
+  double r_trpn;
+  int flag_tt;
+  int ryr_mode; /* 0: square lattice, 1: Poisson disk */
+  int ryr_nx, ryr_ny;
+  double ryr_pitch, ryr_depth, ryr_cx, ryr_cy;
+  int ryr_count;
+  double ryr_radius;
+  int n_lcc;
+  double lcc_half;
+  uint64_t lcc_seed, seed;
+} srs_box_mesh_spec;
+void srs_box_mesh_default(srs_box_mesh_spec* spec);
+/* report: n_tets, n_faces, n_nodes, n_ryr, n_lcc, n_jsr (6 ints); max_a0 (1 double) */
+int srs_box_mesh_write(const srs_box_mesh_spec* spec, const char* base, int* report_ints,
+                       double* report_max_a0);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SRS_GB300_H */

@@ -1,0 +1,197 @@
+"""ctypes access to the CPU oracles (test infrastructure only).
+
+    Oracle      oracle/_build/liboracle.so — C restatement (srs_oracle.c)
+    Reference   oracle/_ref/libsrsref.so   — the reference's own
+                cpu/RunSimulation.cpp driven by oracle/ref_harness.cpp
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module, and only as the checker.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libsrsref.so")
+RNG_REFERENCE, RNG_PHILOX = 0, 1
+
+
+def build():
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Oracle:
+    def __init__(self):
+        if not os.path.exists(ORACLE_SO):
+            build()
+        self.lib = C.CDLL(ORACLE_SO)
+        L = self.lib
+        vp = C.c_void_p
+        L.or_mesh_load.argtypes = [C.c_char_p, C.c_int, vp, C.POINTER(vp)]
+        L.or_mesh_load.restype = C.c_int
+        L.or_mesh_free.argtypes = [vp]
+        L.or_mesh_counts.argtypes = [vp, vp]
+        L.or_mesh_operator.argtypes = [vp, vp, vp, vp]
+        L.or_mesh_elements.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.or_mesh_channels.argtypes = [vp, vp, vp, vp, vp]
+        L.or_initial_states.argtypes = [vp, vp, vp]
+        L.or_explicit_step.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.or_gating_philox.argtypes = [vp, vp, C.c_double, vp, C.c_uint64, C.c_int64, vp, vp, vp, vp]
+        L.or_steps_philox.argtypes = [vp, vp, vp, vp, C.c_uint64, C.c_int64, C.c_int64, vp, vp, vp, vp]
+        L.or_reset_philox.argtypes = [vp, vp, vp, C.c_uint64, vp, vp, vp, vp, vp, vp]
+        L.or_run_simulation.argtypes = [vp, vp, vp, C.c_int, C.c_uint64, C.c_int, vp, C.c_int64,
+                                        C.c_int, vp, vp, vp]
+        L.or_run_simulation.restype = C.c_int64
+        L.or_logf.argtypes = [C.c_float]
+        L.or_logf.restype = C.c_float
+        L.or_exp2f.argtypes = [C.c_float]
+        L.or_exp2f.restype = C.c_float
+        L.or_log.argtypes = [C.c_double]
+        L.or_log.restype = C.c_double
+        L.or_philox4x32_10.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
+
+
+class Mesh:
+    """Oracle mesh: ReadGrid + operator assembly restated."""
+
+    def __init__(self, oracle, base, flag_noflux, reals):
+        self.o = oracle
+        self.reals = _f64(reals)
+        h = C.c_void_p()
+        rc = oracle.lib.or_mesh_load(str(base).encode(), int(flag_noflux), _p(self.reals), C.byref(h))
+        if rc != 0:
+            raise RuntimeError("oracle mesh load failed (%d)" % rc)
+        self.h = h
+        c = np.zeros(6, np.int32)
+        oracle.lib.or_mesh_counts(h, _p(c))
+        self.N, self.NF, self.NN, self.NR, self.NL, self.n_jsr = (int(x) for x in c)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.o.lib.or_mesh_free(self.h)
+            self.h = None
+
+    def operator(self):
+        aij = np.zeros(5 * self.N)
+        nij = np.zeros(4 * self.N, np.int32)
+        br = np.zeros(6 * self.N)
+        self.o.lib.or_mesh_operator(self.h, _p(aij), _p(nij), _p(br))
+        return aij, nij, br
+
+    def elements(self):
+        v0, tt = np.zeros(self.N), np.zeros(self.N)
+        dom, trop, order = (np.zeros(self.N, np.int32) for _ in range(3))
+        self.o.lib.or_mesh_elements(self.h, _p(v0), _p(tt), _p(dom), _p(trop), _p(order))
+        return dict(V0=v0, TT=tt, domain=dom, tropc=trop, order=order)
+
+    def channels(self):
+        a, b = np.zeros(self.NR, np.int32), np.zeros(self.NR, np.int32)
+        c, d = np.zeros(4 * self.NR, np.int32), np.zeros(self.NL, np.int32)
+        self.o.lib.or_mesh_channels(self.h, _p(a), _p(b), _p(c), _p(d))
+        return dict(ryr_ele=a, ryr_jsr=b, ryr_nb=c, lcc_ele=d)
+
+    def initial_states(self):
+        S = np.zeros(6 * self.N)
+        self.o.lib.or_initial_states(self.h, _p(self.reals), _p(S))
+        return S
+
+    def explicit_step(self, S, ryr, lcc, lccv, globals_=None):
+        g = _f64(globals_ if globals_ is not None else
+                 [self.reals[15], self.reals[16]])
+        self.o.lib.or_explicit_step(self.h, _p(self.reals), _p(g), _p(S), _p(_i32(ryr)), _p(_i32(lcc)),
+                                    _p(_i32(lccv)))
+        return S
+
+    def steps_philox(self, S, seed, step0, n, ryr, lcc, lccv, res, globals_=None):
+        g = _f64(globals_ if globals_ is not None else [self.reals[15], self.reals[16]])
+        self.o.lib.or_steps_philox(self.h, _p(self.reals), _p(g), _p(S), C.c_uint64(seed), step0, n,
+                                   _p(ryr), _p(lcc), _p(lccv), _p(res))
+
+    def gating_philox(self, V, ca, seed, step, ryr, lcc, lccv, res):
+        self.o.lib.or_gating_philox(self.h, _p(self.reals), float(V), _p(_f64(ca)), C.c_uint64(seed),
+                                    step, _p(ryr), _p(lcc), _p(lccv), _p(res))
+
+    def reset_philox(self, ints, seed):
+        S = np.zeros(6 * self.N)
+        ryr = np.zeros(self.NR, np.int32)
+        lcc = np.zeros(self.NL, np.int32)
+        lccv = np.zeros(self.NL, np.int32)
+        res = np.zeros(self.NR + self.NL)
+        step = np.zeros(1, np.int64)
+        self.o.lib.or_reset_philox(self.h, _p(_i32(ints)), _p(self.reals), C.c_uint64(seed), _p(S),
+                                   _p(ryr), _p(lcc), _p(lccv), _p(res), _p(step))
+        return dict(states=S, ryr=ryr, lcc=lcc, lccv=lccv, residuals=res, lcc_close_step=int(step[0]))
+
+    def run_simulation(self, ints, mode, seed_or_rank, index=0, row_capacity=None, row_w=7):
+        R = self.reals
+        if row_capacity is None:
+            row_capacity = int(R[0] / R[2]) + 8
+        rows = np.zeros((row_capacity, row_w), np.float32)
+        S = np.zeros(6 * self.N)
+        t_end = np.zeros(1)
+        n_steps = np.zeros(1, np.int64)
+        n = self.o.lib.or_run_simulation(self.h, _p(_i32(ints)), _p(R), mode, C.c_uint64(seed_or_rank),
+                                         index, _p(rows), row_capacity, row_w, _p(S), _p(t_end),
+                                         _p(n_steps))
+        return rows[:n].copy(), S, float(t_end[0]), int(n_steps[0])
+
+
+class Reference:
+    """The reference's cpu/RunSimulation.cpp, compiled in oracle/_ref."""
+
+    def __init__(self):
+        if not os.path.exists(REF_SO):
+            build()
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError("reference sources unavailable: %s not built" % REF_SO)
+        self.lib = C.CDLL(REF_SO)
+        vp = C.c_void_p
+        self.lib.ref_explicit_steps.argtypes = [C.c_int] * 3 + [vp] * 18 + [C.c_int64, C.c_uint]
+        self.lib.ref_run_simulation.argtypes = [C.c_int] * 3 + [vp] * 14 + [C.c_int, C.c_int, vp,
+                                                                             C.c_int64, C.c_int, vp]
+        self.lib.ref_run_simulation.restype = C.c_int64
+
+    @staticmethod
+    def _mesh_args(m):
+        aij, nij, br = m.operator()
+        e = m.elements()
+        ch = m.channels()
+        keep = [aij, nij, br, e["V0"], e["TT"], e["domain"], e["tropc"], ch["ryr_ele"], ch["ryr_jsr"],
+                ch["ryr_nb"], ch["lcc_ele"]]
+        return keep, [m.N, m.NR, m.NL] + [_p(a) for a in keep]
+
+    def explicit_steps(self, m, ints, S, ryr, lcc, lccv, res, n, srand_seed=1):
+        keep, args = self._mesh_args(m)
+        ints = _i32(ints)
+        self.lib.ref_explicit_steps(*args, _p(ints), _p(m.reals), _p(S), _p(ryr), _p(lcc), _p(lccv),
+                                    _p(res), n, srand_seed)
+
+    def run_simulation(self, m, ints, rank=0, index=0, row_capacity=None, row_w=7):
+        keep, args = self._mesh_args(m)
+        R = m.reals
+        if row_capacity is None:
+            row_capacity = int(R[0] / R[2]) + 8
+        rows = np.zeros((row_capacity, row_w), np.float32)
+        S0 = m.initial_states()
+        S = np.zeros(6 * m.N)
+        ints = _i32(ints)
+        n = self.lib.ref_run_simulation(*args, _p(ints), _p(R), _p(S0), rank, index, _p(rows),
+                                        row_capacity, row_w, _p(S))
+        if n < 0:
+            raise ValueError("reference harness needs an explicit initial channel")
+        return rows[:n].copy(), S

@@ -1,0 +1,347 @@
+"""srs_gb300 — GB300-native (sm_103a) spark timestep of the SRS Ca2+-spark model.
+
+Python mirror of the reference's C++ function set (cpu/parameters.h:252-275)
+over the C ABI of include/srs_gb300.h, loaded with ctypes from the in-tree
+library srs_gb300/libsrs_gb300.so.  Names follow the reference:
+
+    read_parameters(path)            ReadParameters      cpu/InitFuncs.cpp:25
+    Grid(params, mesh_base)          ReadGrid + InitializeDomainStruct
+    Simulation(grid, params, ...)    per-realization device state
+      .reset()                       cpu/main.cpp:216-257 initial opening
+      .explicit_step(n)              ExplicitStep (+UpdateChannelGating)
+      .run_simulation(row_capacity)  RunSimulation with states rows
+
+There is no CPU fallback: if the library is missing, importing the module
+raises; if no sm_103a GPU is present, creating a Simulation raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsrs_gb300.so")
+HEADER = os.path.join(os.path.dirname(_HERE), "include", "srs_gb300.h")
+
+N_INT, N_REAL, N_CHAR = 19, 56, 4
+FP64, FP32 = 64, 32
+ENGINE_PLAIN, ENGINE_RESIDENT = 0, 1
+STATES_ROW_BASE = 7
+
+# parameter indices (cpu/parameters.h:18-96)
+I = dict(OUTPUT_GRID_FLAG=0, FLAG_FIDELITY_SIM=1, FLAG_CLOCK_SEED=2, RAND_SEED_0=3, RAND_ADD_A=4,
+         RAND_ADD_B=5, INITIALIZE_FROM_FILE=6, CUDA_DEVICE=7, FLAG_SECONDARY_GRADIENT=8,
+         FLAG_NO_FLUX_BOUNDARY=9, N_RYR_FIDELITY=10, FLAG_LCC=11, LCC_INDEX=12, FLAG_V_CLAMP=13,
+         FLAG_NO_GATING=14, GATING_FFWD=15, FLAG_RYR_OUT=16, N_SIMS=17, INIT_RYR=18)
+R = dict(T_FINAL=0, T_STEP=1, OUTPUT_STATES_INTERVAL=2, OUTPUT_GRID_INTERVAL=3, C_MIN=4, D_CA=5,
+         D_CA_JSR=6, D_ATP=7, D_CMDN=8, D_TRPN=9, D_CSQN=10, D_DYE=11, D_EGTA=12, C_0_CA=13,
+         C_0_CA_JSR=14, DEFAULT_VM=15, DEFAULT_CA_NSR=16, CA_0=17, B_TOT_ATP=18, K_OFF_ATP=19,
+         K_ON_ATP=20, B_TOT_CMDN=21, K_OFF_CMDN=22, K_ON_CMDN=23, B_TOT_TRPN=24, K_OFF_TRPN=25,
+         K_ON_TRPN=26, B_TOT_SL_HI=27, K_D_SL_HI=28, B_TOT_SL_LO=29, K_D_SL_LO=30, B_TOT_DYE=31,
+         K_OFF_DYE=32, K_ON_DYE=33, B_T_JSR=34, K_M_JSR=35, V_REFILL=36, V_RYR=37, V_CELL=38,
+         K_ON_CSQN=39, K_OFF_CSQN=40, RYR_ETA=41, RYR_A_STAR=42, RYR_EPS_CC=43, RYR_EPS_OO=44,
+         RYR_K_PLUS=45, RYR_K_MINUS=46, RYR_PHI_M=47, RYR_PHI_B=48, K_D_i=49, K_D_SR=50, A_P=51,
+         LCC_DURATION=52, T_CLAMP=53, V_CLAMP=54, INIT_RYR_HOLD=55)
+SPECIES = ("CA", "ATP", "CMDN", "TRPN", "CSQN", "DYE")
+
+
+class SrsError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (_lib.srs_status_string(status).decode(), status, msg))
+        self.status = status
+
+
+class Params(C.Structure):
+    """ParamStruct (cpu/parameters.h:234-246)."""
+    _fields_ = [("ints", C.c_int * N_INT), ("reals", C.c_double * N_REAL),
+                ("chars", (C.c_char * 255) * N_CHAR)]
+
+    def copy(self):
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+    def set(self, **kw):
+        for k, v in kw.items():
+            if k in I:
+                self.ints[I[k]] = int(v)
+            elif k in R:
+                self.reals[R[k]] = float(v)
+            else:
+                raise KeyError(k)
+        return self
+
+
+class _GridInfo(C.Structure):
+    _fields_ = [("n_ele", C.c_int), ("n_face", C.c_int), ("n_nodes", C.c_int), ("n_ryr", C.c_int),
+                ("n_lcc", C.c_int), ("n_jsr", C.c_int), ("vol_jsr", C.c_double),
+                ("max_diag", C.c_double)]
+
+
+class _SimDesc(C.Structure):
+    _fields_ = [("n_realizations", C.c_int), ("precision", C.c_int), ("engine", C.c_int),
+                ("threads_per_cta", C.c_int), ("cluster_size", C.c_int),
+                ("steps_per_launch", C.c_int), ("seeds", C.POINTER(C.c_uint64))]
+
+
+class _SimConfig(C.Structure):
+    _fields_ = [("engine", C.c_int), ("precision", C.c_int), ("threads_per_cta", C.c_int),
+                ("cluster_size", C.c_int), ("steps_per_launch", C.c_int), ("smem_bytes", C.c_int),
+                ("kernel_launches", C.c_int64)]
+
+
+class _RunOutput(C.Structure):
+    _fields_ = [("rows", C.POINTER(C.c_float)), ("row_capacity", C.c_int64), ("row_width", C.c_int),
+                ("n_rows", C.POINTER(C.c_int64)), ("t_end", C.POINTER(C.c_double)),
+                ("n_steps", C.POINTER(C.c_int64))]
+
+
+class BoxMeshSpec(C.Structure):
+    """Synthetic box-dyad mesh (see csrc/meshgen.cpp)."""
+    _fields_ = [("box_x", C.c_double), ("box_y", C.c_double), ("box_z", C.c_double),
+                ("foot_half_x", C.c_double), ("foot_half_y", C.c_double),
+                ("n_foot_x", C.c_int), ("n_foot_y", C.c_int), ("n_out_x", C.c_int),
+                ("n_out_y", C.c_int), ("cleft_h", C.c_double), ("jsr_h", C.c_double),
+                ("n_cleft_z", C.c_int), ("n_jsr_z", C.c_int), ("n_above_z", C.c_int),
+                ("r_trpn", C.c_double), ("flag_tt", C.c_int), ("ryr_mode", C.c_int),
+                ("ryr_nx", C.c_int), ("ryr_ny", C.c_int), ("ryr_pitch", C.c_double),
+                ("ryr_depth", C.c_double), ("ryr_cx", C.c_double), ("ryr_cy", C.c_double),
+                ("ryr_count", C.c_int), ("ryr_radius", C.c_double), ("n_lcc", C.c_int),
+                ("lcc_half", C.c_double), ("lcc_seed", C.c_uint64), ("seed", C.c_uint64)]
+
+
+# Every symbol declared in include/srs_gb300.h with its ctypes signature.
+_P = C.c_void_p
+_SIGS = {
+    "srs_status_string": (C.c_char_p, [C.c_int]),
+    "srs_last_error": (C.c_char_p, []),
+    "srs_version": (C.c_char_p, []),
+    "srs_default_parameters": (None, [C.POINTER(Params)]),
+    "srs_read_parameters": (C.c_int, [C.POINTER(Params), C.c_char_p]),
+    "srs_read_grid": (C.c_int, [C.POINTER(Params), C.c_char_p, C.POINTER(_P)]),
+    "srs_free_grid": (None, [_P]),
+    "srs_grid_get_info": (C.c_int, [_P, C.POINTER(_GridInfo)]),
+    "srs_grid_get_operator": (C.c_int, [_P, _P, _P, _P]),
+    "srs_grid_get_elements": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+    "srs_grid_get_channels": (C.c_int, [_P, _P, _P, _P, _P]),
+    "srs_initial_states": (C.c_int, [_P, C.POINTER(Params), _P]),
+    "srs_sim_create": (C.c_int, [_P, C.POINTER(Params), C.POINTER(_SimDesc), C.POINTER(_P)]),
+    "srs_sim_destroy": (None, [_P]),
+    "srs_sim_get_desc": (C.c_int, [_P, C.POINTER(_SimDesc)]),
+    "srs_sim_reset": (C.c_int, [_P]),
+    "srs_sim_set_state": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P]),
+    "srs_sim_get_state": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P]),
+    "srs_sim_set_globals": (C.c_int, [_P, C.c_double, C.c_double]),
+    "srs_explicit_step": (C.c_int, [_P, C.c_int64]),
+    "srs_run_simulation": (C.c_int, [_P, C.POINTER(_RunOutput)]),
+    "srs_sim_advance_async": (C.c_int, [_P, C.c_int64]),
+    "srs_sim_synchronize": (C.c_int, [_P]),
+    "srs_sim_time_advance": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
+    "srs_sim_status": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "srs_sim_get_config": (C.c_int, [_P, C.POINTER(_SimConfig)]),
+    "srs_write_grid_vtk": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "srs_box_mesh_default": (None, [C.POINTER(BoxMeshSpec)]),
+    "srs_box_mesh_write": (C.c_int, [C.POINTER(BoxMeshSpec), C.c_char_p, _P, _P]),
+}
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("srs_gb300: native library %s is missing; run "
+                          "`python -c 'import __graft_entry__ as g; g.build()'` first" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_lib = _load()
+
+
+def _check(rc):
+    if rc != 0:
+        raise SrsError(rc, _lib.srs_last_error().decode())
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def library():
+    return _lib
+
+
+def default_parameters():
+    p = Params()
+    _lib.srs_default_parameters(C.byref(p))
+    return p
+
+
+def read_parameters(path, params=None):
+    """ReadParameters (cpu/InitFuncs.cpp:25): defaults overridden by the XML file."""
+    p = params.copy() if params is not None else default_parameters()
+    _check(_lib.srs_read_parameters(C.byref(p), str(path).encode()))
+    return p
+
+
+def box_mesh_spec(**kw):
+    s = BoxMeshSpec()
+    _lib.srs_box_mesh_default(C.byref(s))
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def write_box_mesh(base, spec=None, **kw):
+    """Writes the six reference mesh files for a synthetic box dyad."""
+    s = spec if spec is not None else box_mesh_spec(**kw)
+    rep = np.zeros(6, np.int32)
+    a0 = np.zeros(1, np.float64)
+    _check(_lib.srs_box_mesh_write(C.byref(s), str(base).encode(), _ptr(rep), _ptr(a0)))
+    keys = ("n_tets", "n_faces", "n_nodes", "n_ryr", "n_lcc", "n_jsr_tets")
+    d = {k: int(v) for k, v in zip(keys, rep)}
+    d["max_a0"] = float(a0[0])
+    return d
+
+
+class Grid:
+    """ReadGrid + InitializeDomainStruct (cpu/InitFuncs.cpp:384, 1005)."""
+
+    def __init__(self, params, mesh_base):
+        h = C.c_void_p()
+        _check(_lib.srs_read_grid(C.byref(params), str(mesh_base).encode(), C.byref(h)))
+        self._h = h
+        info = _GridInfo()
+        _check(_lib.srs_grid_get_info(h, C.byref(info)))
+        self.n_ele, self.n_face, self.n_nodes = info.n_ele, info.n_face, info.n_nodes
+        self.n_ryr, self.n_lcc, self.n_jsr = info.n_ryr, info.n_lcc, info.n_jsr
+        self.vol_jsr, self.max_diag = info.vol_jsr, info.max_diag
+
+    def operator(self):
+        N = self.n_ele
+        aij = np.zeros(5 * N, np.float64)
+        nij = np.zeros(4 * N, np.int32)
+        br = np.zeros(6 * N, np.float64)
+        _check(_lib.srs_grid_get_operator(self._h, _ptr(aij), _ptr(nij), _ptr(br)))
+        return aij, nij, br
+
+    def elements(self):
+        N = self.n_ele
+        v0, tt = np.zeros(N), np.zeros(N)
+        dom, trop, order = (np.zeros(N, np.int32) for _ in range(3))
+        _check(_lib.srs_grid_get_elements(self._h, _ptr(v0), _ptr(tt), _ptr(dom), _ptr(trop),
+                                          _ptr(order)))
+        return dict(V0=v0, TT=tt, domain=dom, tropc=trop, order=order)
+
+    def channels(self):
+        a = np.zeros(self.n_ryr, np.int32)
+        b = np.zeros(self.n_ryr, np.int32)
+        c = np.zeros(4 * self.n_ryr, np.int32)
+        d = np.zeros(self.n_lcc, np.int32)
+        _check(_lib.srs_grid_get_channels(self._h, _ptr(a), _ptr(b), _ptr(c), _ptr(d)))
+        return dict(ryr_ele=a, ryr_jsr=b, ryr_nb=c, lcc_ele=d)
+
+    def initial_states(self, params):
+        S = np.zeros(6 * self.n_ele, np.float64)
+        _check(_lib.srs_initial_states(self._h, C.byref(params), _ptr(S)))
+        return S
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.srs_free_grid(self._h)
+            self._h = None
+
+
+class Simulation:
+    """R independent realizations of one grid on the GPU."""
+
+    def __init__(self, grid, params, n_realizations=1, precision=FP64, engine=ENGINE_PLAIN,
+                 seeds=None, threads_per_cta=0, cluster_size=0, steps_per_launch=0):
+        self.grid, self.params = grid, params.copy()
+        self.R = int(n_realizations)
+        d = _SimDesc(self.R, int(precision), int(engine), int(threads_per_cta), int(cluster_size),
+                     int(steps_per_launch), None)
+        if seeds is not None:
+            self._seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
+            d.seeds = self._seeds.ctypes.data_as(C.POINTER(C.c_uint64))
+        h = C.c_void_p()
+        _check(_lib.srs_sim_create(grid._h, C.byref(self.params), C.byref(d), C.byref(h)))
+        self._h = h
+        self.precision, self.engine = precision, engine
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.srs_sim_destroy(self._h)
+            self._h = None
+
+    def config(self):
+        c = _SimConfig()
+        _check(_lib.srs_sim_get_config(self._h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in _SimConfig._fields_}
+
+    def reset(self):
+        _check(_lib.srs_sim_reset(self._h))
+
+    def set_state(self, r, states=None, ryr=None, lcc=None, lccv=None, residuals=None):
+        conv = lambda a, t: None if a is None else np.ascontiguousarray(a, dtype=t)
+        arrs = [conv(states, np.float64), conv(ryr, np.int32), conv(lcc, np.int32),
+                conv(lccv, np.int32), conv(residuals, np.float64)]
+        _check(_lib.srs_sim_set_state(self._h, r, *[_ptr(a) for a in arrs]))
+
+    def get_state(self, r):
+        g = self.grid
+        S = np.zeros(6 * g.n_ele)
+        ryr = np.zeros(g.n_ryr, np.int32)
+        lcc = np.zeros(g.n_lcc, np.int32)
+        lccv = np.zeros(g.n_lcc, np.int32)
+        res = np.zeros(g.n_ryr + g.n_lcc)
+        _check(_lib.srs_sim_get_state(self._h, r, _ptr(S), _ptr(ryr), _ptr(lcc), _ptr(lccv),
+                                      _ptr(res)))
+        return dict(states=S, ryr=ryr, lcc=lcc, lccv=lccv, residuals=res)
+
+    def set_globals(self, v_m, ca_nsr):
+        _check(_lib.srs_sim_set_globals(self._h, float(v_m), float(ca_nsr)))
+
+    def explicit_step(self, n_steps=1):
+        _check(_lib.srs_explicit_step(self._h, int(n_steps)))
+
+    def advance_async(self, n_steps):
+        _check(_lib.srs_sim_advance_async(self._h, int(n_steps)))
+
+    def synchronize(self):
+        _check(_lib.srs_sim_synchronize(self._h))
+
+    def time_advance(self, n_steps):
+        ms = C.c_float()
+        _check(_lib.srs_sim_time_advance(self._h, int(n_steps), C.byref(ms)))
+        return float(ms.value)
+
+    def status(self):
+        b = C.c_int()
+        _check(_lib.srs_sim_status(self._h, C.byref(b)))
+        return int(b.value)
+
+    def row_width(self):
+        return STATES_ROW_BASE + (self.grid.n_ryr if self.params.ints[I["FLAG_RYR_OUT"]] else 0)
+
+    def run_simulation(self, row_capacity=None):
+        """RunSimulation for every realization; returns per-realization rows."""
+        p = self.params
+        if row_capacity is None:
+            row_capacity = int(p.reals[R["T_FINAL"]] / p.reals[R["OUTPUT_STATES_INTERVAL"]]) + 8
+        w = self.row_width()
+        rows = np.zeros((self.R, row_capacity, w), np.float32)
+        n_rows = np.zeros(self.R, np.int64)
+        t_end = np.zeros(self.R)
+        n_steps = np.zeros(self.R, np.int64)
+        out = _RunOutput(rows.ctypes.data_as(C.POINTER(C.c_float)), row_capacity, w,
+                         n_rows.ctypes.data_as(C.POINTER(C.c_int64)),
+                         t_end.ctypes.data_as(C.POINTER(C.c_double)),
+                         n_steps.ctypes.data_as(C.POINTER(C.c_int64)))
+        _check(_lib.srs_run_simulation(self._h, C.byref(out)))
+        return [rows[r, :n_rows[r]].copy() for r in range(self.R)], t_end, n_steps
+
+    def write_grid_vtk(self, r, path, run=0, rank=0, n=0, t=0.0):
+        _check(_lib.srs_write_grid_vtk(self._h, r, str(path).encode(), run, rank, n, float(t)))

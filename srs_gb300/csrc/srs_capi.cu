@@ -1,0 +1,1345 @@
+// srs_capi.cu — the C ABI (include/srs_gb300.h): grids, simulations, engine
+// set-up and launch sequencing.  All numerics run in the sm_103a kernels of
+// k_plain64.cu / k_fp32.cu; this file packs data, moves it and orders work.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "srs_engine.h"
+#include "srs_host.h"
+
+using namespace srs;
+
+namespace {
+thread_local std::string g_err;
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define SRS_CUDA(call)                                                               \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(SRS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+}  // namespace
+
+struct srs_grid {
+  Mesh m;
+  Operator op;
+  srs_params p;
+};
+
+struct srs_sim {
+  Mesh m;
+  Operator op;
+  srs_params p;
+  srs_sim_desc d;
+  std::vector<uint64_t> seeds;
+  int R = 0, N = 0, NR = 0, NL = 0, NCH = 0;
+  cudaStream_t st = nullptr;
+  std::vector<void*> allocs;
+  // element numbering of the engine
+  std::vector<int> eng_of_ref, ref_of_eng;
+  // FP32 rest values per engine element
+  std::vector<double> rest_ca, rest_imm;
+  RestValues rv;
+  double vm = 0, nsr = 0;
+  // channel state (device)
+  int32_t *d_ryr = nullptr, *d_lcc = nullptr, *d_lccv = nullptr;
+  double* d_res = nullptr;
+  RealCtl* d_ctl = nullptr;
+  float* d_rows = nullptr;
+  int64_t rows_cap_alloc = 0;
+  int rows_w_alloc = 0;
+  int64_t* d_ticks = nullptr;
+  double* d_tick_t = nullptr;
+  unsigned int* d_counters = nullptr;
+  Channels ch{};
+  Protocol P{};
+  // engines
+  Plain64Args a64{};
+  Plain32Args a32{};
+  ResidentArgs ar{};
+  double* d_S[2] = {nullptr, nullptr};
+  float4* d_M[2] = {nullptr, nullptr};
+  float* d_I[2] = {nullptr, nullptr};
+  int C = 1, threads = 0, n_clusters = 0, P_stride = 0, off_bits = 0;
+  size_t smem = 0;
+  std::vector<int> part_start, part_len, part_nch;  // resident partitions
+  int64_t launches = 0;
+  cudaGraphExec_t graph_plain = nullptr;
+  int graph_plain_len = 0;
+};
+
+namespace {
+
+template <class T>
+int dev_upload(srs_sim* s, T** dst, const T* src, size_t n) {
+  void* p = nullptr;
+  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  SRS_CUDA(cudaMalloc(&p, bytes));
+  s->allocs.push_back(p);
+  if (n) SRS_CUDA(cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = (T*)p;
+  return SRS_OK;
+}
+template <class T>
+int dev_alloc(srs_sim* s, T** dst, size_t n) {
+  void* p = nullptr;
+  SRS_CUDA(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+  SRS_CUDA(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+  s->allocs.push_back(p);
+  *dst = (T*)p;
+  return SRS_OK;
+}
+#define SRS_TRY(x)          \
+  do {                      \
+    int rc_ = (x);          \
+    if (rc_ != SRS_OK) return rc_; \
+  } while (0)
+
+// Gating and flux constants for membrane potential V (cpu/RunSimulation.cpp:
+// 149-161, 185-197, 239-375), evaluated in double precision on the host.
+void gate_consts(const srs_params& p, double V, srs_gate_consts* g) {
+  const double* R = p.reals;
+  g->ryr_kplus = (float)R[R_RYR_K_PLUS];
+  g->ryr_kminus = (float)R[R_RYR_K_MINUS];
+  g->ryr_eta = (float)R[R_RYR_ETA];
+  g->ryr_phi0 = (float)(1.0 - std::pow(1000.0 / R[R_RYR_PHI_B], R[R_RYR_PHI_M]));
+  g->ryr_inv_kphi = (float)(1.0 / R[R_RYR_PHI_B]);
+  g->ryr_phin = (float)R[R_RYR_PHI_M];
+  g->ryr_astar_half = (float)(0.5 * R[R_RYR_A_STAR]);
+  g->ryr_eps_cc = (float)R[R_RYR_EPS_CC];
+  g->ryr_eps_oo = (float)R[R_RYR_EPS_OO];
+  const double alphacf = 4.0 * 1.2 * 0.416;
+  const double betacf = 4.0 * 0.45 * 0.049;
+  const double gammacf = 0.83 * 1.9 * 1.3 * 0.31 * 7.5 * 0.09233 / 1000.0;
+  g->alpha = (float)(alphacf * std::exp(0.012 * (V - 35.0)));
+  g->beta = (float)(betacf * std::exp(-0.05 * (V - 35.0)));
+  g->gamma_cf = (float)gammacf;
+  const double yCa_frac = 0.4;
+  double yCa_inf = yCa_frac / (1.0 + std::exp((V + 12.5) / 5.0)) + (1.0 - yCa_frac);
+  double tau_yCa = 60.0 + 340.0 / (1.0 + std::exp((V + 30.0) / 12.0));
+  g->lccv_rate_inact_to_act = (float)(yCa_inf / tau_yCa);
+  g->lccv_rate_act_to_inact = (float)((1.0 - yCa_inf) / tau_yCa);
+  g->dt = R[R_T_STEP];
+}
+
+void lcc_flux_consts(const srs_params& p, double V, double* A, double* E, double* Em1, double* B,
+                     double* Vg) {
+  const double P_CaL = (9.13e-13) * (1e12) * (1e-3);
+  const double F = 96.5;
+  const double RT = 310 * 8.314;
+  const double F_over_RT = F / RT;
+  if (std::fabs(V) < 1e-6) V = 1e-6;
+  *Vg = V;
+  *A = -P_CaL * V * (2 * F_over_RT);
+  *E = std::exp(2 * V * F_over_RT);
+  *Em1 = std::exp(2 * V * F_over_RT) - 1;
+  *B = 0.34 * p.reals[R_CA_0];
+}
+
+void fill_protocol_consts(srs_sim* s) {
+  Protocol& P = s->P;
+  const double* R = s->p.reals;
+  const int* I = s->p.ints;
+  double Vs[2] = {s->vm, R[R_V_CLAMP]};
+  for (int v = 0; v < 2; ++v) {
+    gate_consts(s->p, Vs[v], &P.gc[v]);
+    double Vg;
+    lcc_flux_consts(s->p, Vs[v], &P.lccA[v], &P.lccE[v], &P.lccEm1[v], &P.lccB, &Vg);
+    P.Vm[v] = Vg;
+  }
+  P.dt = R[R_T_STEP];
+  P.v_ryr = R[R_V_RYR];
+  P.v_cell = R[R_V_CELL];
+  P.c_min = R[R_C_MIN];
+  P.flag_vclamp = I[I_FLAG_V_CLAMP];
+  P.flag_lcc = I[I_FLAG_LCC];
+  P.lcc_index = I[I_LCC_INDEX];
+  P.init_ryr = I[I_INIT_RYR];
+  P.flag_fidelity = I[I_FLAG_FIDELITY_SIM];
+  P.n_open_max = I[I_N_RYR_FIDELITY];
+  P.nogating = I[I_FLAG_NO_GATING];
+  P.ryr_out = I[I_FLAG_RYR_OUT];
+  P.row_w = SRS_STATES_ROW_BASE + (P.ryr_out ? s->NR : 0);
+}
+
+Consts32 make_consts32(const srs_sim* s) {
+  const double* R = s->p.reals;
+  const RestValues& rv = s->rv;
+  Consts32 k{};
+  k.D[0] = (float)R[R_D_CA];
+  k.D[1] = (float)R[R_D_ATP];
+  k.D[2] = (float)R[R_D_CMDN];
+  k.D[3] = (float)R[R_D_DYE];
+  const int ion[5] = {R_K_ON_DYE, R_K_ON_ATP, R_K_ON_CMDN, R_K_ON_TRPN, R_K_ON_CSQN};
+  const int ioff[5] = {R_K_OFF_DYE, R_K_OFF_ATP, R_K_OFF_CMDN, R_K_OFF_TRPN, R_K_OFF_CSQN};
+  const double btot[5] = {R[R_B_TOT_DYE], R[R_B_TOT_ATP], R[R_B_TOT_CMDN], R[R_B_TOT_TRPN],
+                          R[R_B_T_JSR]};
+  const double brest[5] = {rv.dye, rv.atp, rv.cmdn, rv.trpn, rv.csqn};
+  for (int q = 0; q < 5; ++q) {
+    k.kon[q] = (float)R[ion[q]];
+    k.koff[q] = (float)R[ioff[q]];
+    k.bfree[q] = (float)(btot[q] - brest[q]);
+  }
+  k.c0 = (float)rv.ca0;
+  k.c0j = (float)rv.ca0_jsr;
+  k.inv_kdi = (float)(1.0 / R[R_K_D_i]);
+  double Ksr = s->nsr / R[R_K_D_SR];
+  Ksr = Ksr * Ksr;
+  k.sd0 = (float)(0.104217 + 17.923 * Ksr);
+  k.sd1 = (float)(1.75583e6 + Ksr * 7.61673e6);
+  k.sd2 = (float)(6.08463e11 + Ksr * 4.50544e11);
+  k.sn1 = (float)(9.17846e6 - 11478.2 * Ksr);
+  k.sn0 = (float)(0.329904 * Ksr);
+  k.serca_scale = (float)(2e-3 * R[R_A_P]);
+  k.refill_v = (float)R[R_V_REFILL];
+  k.refill0 = (float)((s->nsr - rv.ca0_jsr) * R[R_V_REFILL]);
+  k.khi = (float)R[R_K_D_SL_HI];
+  k.dt = (float)R[R_T_STEP];
+  k.jr_scale = (float)(R[R_V_RYR] * R[R_V_CELL]);
+  k.dc0 = (float)(rv.ca0_jsr - rv.ca0);
+  for (int v = 0; v < 2; ++v) {
+    k.lccA[v] = (float)(s->P.lccA[v] / s->P.lccEm1[v]);
+    k.lccE[v] = (float)s->P.lccE[v];
+  }
+  k.lccB = (float)s->P.lccB;
+  return k;
+}
+
+// Channel contributions per element in the reference's order, engine numbering.
+void chan_lists(const srs_sim* s, std::vector<int32_t>* ptr, std::vector<ChanEntry>* list) {
+  const Mesh& m = s->m;
+  std::vector<std::vector<ChanEntry>> per(s->N);
+  for (int i = 0; i < m.NR; ++i) {
+    per[s->eng_of_ref[m.ryr_ele[i]]].push_back({0, i});
+    per[s->eng_of_ref[m.ryr_jsr[i]]].push_back({1, i});
+  }
+  for (int i = 0; i < m.NL; ++i) per[s->eng_of_ref[m.lcc_ele[i]]].push_back({2, i});
+  ptr->assign(s->N + 1, 0);
+  list->clear();
+  for (int e = 0; e < s->N; ++e) {
+    (*ptr)[e] = (int32_t)list->size();
+    list->insert(list->end(), per[e].begin(), per[e].end());
+  }
+  (*ptr)[s->N] = (int32_t)list->size();
+}
+
+int alloc_channel_state(srs_sim* s) {
+  SRS_TRY(dev_alloc(s, &s->d_ryr, (size_t)s->R * s->NR));
+  SRS_TRY(dev_alloc(s, &s->d_lcc, (size_t)s->R * s->NL));
+  SRS_TRY(dev_alloc(s, &s->d_lccv, (size_t)s->R * s->NL));
+  SRS_TRY(dev_alloc(s, &s->d_res, (size_t)s->R * s->NCH));
+  SRS_TRY(dev_alloc(s, &s->d_ctl, (size_t)s->R));
+  SRS_TRY(dev_alloc(s, &s->d_counters, (size_t)s->R));
+  SRS_TRY(dev_alloc(s, &s->d_rows, 8));
+  s->rows_cap_alloc = 0;
+  s->rows_w_alloc = 0;
+  return SRS_OK;
+}
+
+ChanState chan_state(const srs_sim* s) {
+  ChanState cs;
+  cs.ryr = s->d_ryr;
+  cs.lcc = s->d_lcc;
+  cs.lccv = s->d_lccv;
+  cs.res = s->d_res;
+  cs.ctl = s->d_ctl;
+  cs.rows = s->d_rows;
+  return cs;
+}
+
+int upload_channels_engine_order(srs_sim* s) {
+  std::vector<int32_t> rc(s->NR), rj(s->NR), lc(s->NL);
+  for (int i = 0; i < s->NR; ++i) {
+    rc[i] = s->eng_of_ref[s->m.ryr_ele[i]];
+    rj[i] = s->eng_of_ref[s->m.ryr_jsr[i]];
+  }
+  for (int i = 0; i < s->NL; ++i) lc[i] = s->eng_of_ref[s->m.lcc_ele[i]];
+  int32_t *a, *b, *c, *d;
+  SRS_TRY(dev_upload(s, &a, rc.data(), rc.size()));
+  SRS_TRY(dev_upload(s, &b, rj.data(), rj.size()));
+  SRS_TRY(dev_upload(s, &c, s->m.ryr_nb.data(), s->m.ryr_nb.size()));
+  SRS_TRY(dev_upload(s, &d, lc.data(), lc.size()));
+  s->ch.NR = s->NR;
+  s->ch.NL = s->NL;
+  s->ch.ryr_cleft = a;
+  s->ch.ryr_jsr = b;
+  s->ch.ryr_nb = c;
+  s->ch.lcc_ele = d;
+  return SRS_OK;
+}
+
+// ---- FP64 plain engine (reference numbering) --------------------------------
+int setup_plain64(srs_sim* s) {
+  const int N = s->N;
+  s->eng_of_ref.resize(N);
+  s->ref_of_eng.resize(N);
+  for (int i = 0; i < N; ++i) s->eng_of_ref[i] = s->ref_of_eng[i] = i;
+  Plain64Args& a = s->a64;
+  a.N = N;
+  a.R = s->R;
+  const double* R = s->p.reals;
+  std::vector<double> br4(4 * (size_t)N), bhi(N), blo(N);
+  for (int j = 0; j < N; ++j) {
+    br4[0 * (size_t)N + j] = s->op.br[SP_CA * (size_t)N + j];
+    br4[1 * (size_t)N + j] = s->op.br[SP_ATP * (size_t)N + j];
+    br4[2 * (size_t)N + j] = s->op.br[SP_CMDN * (size_t)N + j];
+    br4[3 * (size_t)N + j] = s->op.br[SP_DYE * (size_t)N + j];
+    // btothi / btotlo exactly as UpdateFastBuffer forms them (:17-18)
+    bhi[j] = s->m.TT[j] * R[R_B_TOT_SL_HI] / (s->m.V0[j] * (1e-15));
+    blo[j] = s->m.TT[j] * R[R_B_TOT_SL_LO] / (s->m.V0[j] * (1e-15));
+  }
+  std::vector<int32_t> ptr;
+  std::vector<ChanEntry> list;
+  chan_lists(s, &ptr, &list);
+  std::vector<int32_t> flags(N);
+  for (int j = 0; j < N; ++j)
+    flags[j] = (s->m.domain[j] == DOMAIN_JSR ? 1 : 0) | (s->m.tropc[j] ? 2 : 0) |
+               (ptr[j + 1] > ptr[j] ? 4 : 0);
+  SRS_TRY(dev_upload(s, (double**)&a.aij, s->op.aij.data(), s->op.aij.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.nij, s->op.nij.data(), s->op.nij.size()));
+  SRS_TRY(dev_upload(s, (double**)&a.br, br4.data(), br4.size()));
+  SRS_TRY(dev_upload(s, (double**)&a.v0, s->m.V0.data(), s->m.V0.size()));
+  SRS_TRY(dev_upload(s, (double**)&a.bhi, bhi.data(), bhi.size()));
+  SRS_TRY(dev_upload(s, (double**)&a.blo, blo.data(), blo.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.flags, flags.data(), flags.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.chan_ptr, ptr.data(), ptr.size()));
+  SRS_TRY(dev_upload(s, (ChanEntry**)&a.chan_list, list.data(), list.size()));
+  for (int b = 0; b < 2; ++b) SRS_TRY(dev_alloc(s, &s->d_S[b], (size_t)s->R * 6 * N));
+  for (int q = 0; q < 56; ++q) a.p[q] = R[q];
+  SRS_TRY(upload_channels_engine_order(s));
+  return SRS_OK;
+}
+
+// ---- FP32 engines: checks shared by both ------------------------------------
+int check_fp32_supported(const srs_sim* s, bool resident) {
+  const Mesh& m = s->m;
+  const Operator& op = s->op;
+  if (s->p.reals[R_B_TOT_SL_LO] != 0.0)
+    return fail(SRS_ERR_UNSUPPORTED, "FP32 engines model only the high-affinity SL buffer");
+  for (int j = 0; j < m.N; ++j) {
+    for (int k = 0; k < 4; ++k) {
+      int n = op.nij[4 * (size_t)j + k];
+      if (op.aij[5 * (size_t)j + 1 + k] != 0 && m.domain[n] != m.domain[j])
+        return fail(SRS_ERR_UNSUPPORTED,
+                    "FP32 engines need cytosol and JSR uncoupled by diffusion faces");
+    }
+    if (op.kb[j] != 0 && (resident || m.domain[j] == DOMAIN_JSR))
+      return fail(SRS_ERR_UNSUPPORTED,
+                  resident ? "resident engine needs no-flux boundaries (flag_noflux)"
+                           : "FP32 engines need Dirichlet faces on cytosolic elements only");
+  }
+  return SRS_OK;
+}
+
+void fp32_rest(srs_sim* s) {
+  const int N = s->N;
+  s->rest_ca.resize(N);
+  s->rest_imm.resize(N);
+  for (int e = 0; e < N; ++e) {
+    int j = s->ref_of_eng[e];
+    bool jsr = s->m.domain[j] == DOMAIN_JSR;
+    s->rest_ca[e] = jsr ? s->rv.ca0_jsr : s->rv.ca0;
+    s->rest_imm[e] = jsr ? s->rv.csqn : (s->m.tropc[j] ? s->rv.trpn : 0.0);
+  }
+}
+
+float bsl_of(const srs_sim* s, int j) {
+  const double* R = s->p.reals;
+  double bhi = s->m.TT[j] * R[R_B_TOT_SL_HI] / (s->m.V0[j] * (1e-15));
+  return (float)(bhi * R[R_K_D_SL_HI]);
+}
+
+int setup_plain32(srs_sim* s) {
+  SRS_TRY(check_fp32_supported(s, false));
+  const int N = s->N;
+  s->ref_of_eng = rcm_order_by_domain(s->m, s->op);
+  s->eng_of_ref.resize(N);
+  for (int e = 0; e < N; ++e) s->eng_of_ref[s->ref_of_eng[e]] = e;
+  fp32_rest(s);
+  Plain32Args& a = s->a32;
+  a.N = N;
+  a.R = s->R;
+  std::vector<float4> A(N);
+  std::vector<int4> NB(N);
+  std::vector<float> bsl(N), kb(N), rest(N);
+  std::vector<uint32_t> flags(N);
+  std::vector<int32_t> ptr;
+  std::vector<ChanEntry> list;
+  chan_lists(s, &ptr, &list);
+  bool any_kb = false;
+  for (int e = 0; e < N; ++e) {
+    int j = s->ref_of_eng[e];
+    const double* aj = &s->op.aij[5 * (size_t)j];
+    const int* nj = &s->op.nij[4 * (size_t)j];
+    A[e] = make_float4((float)aj[1], (float)aj[2], (float)aj[3], (float)aj[4]);
+    NB[e] = make_int4(s->eng_of_ref[nj[0]], s->eng_of_ref[nj[1]], s->eng_of_ref[nj[2]],
+                      s->eng_of_ref[nj[3]]);
+    bsl[e] = bsl_of(s, j);
+    kb[e] = (float)s->op.kb[j];
+    any_kb |= kb[e] != 0.0f;
+    rest[e] = (float)s->rest_ca[e];
+    flags[e] = (s->m.domain[j] == DOMAIN_JSR ? 1u : 0u) | (s->m.tropc[j] ? 2u : 0u) |
+               (ptr[e + 1] > ptr[e] ? 4u : 0u);
+  }
+  std::vector<ChanEntry32> l32(list.size());
+  for (int e = 0; e < N; ++e) {
+    double iv = 1.0 / s->m.V0[s->ref_of_eng[e]];
+    for (int q = ptr[e]; q < ptr[e + 1]; ++q) {
+      l32[q].kind = list[q].kind;
+      l32[q].ch = list[q].ch;
+      l32[q].s = (float)(list[q].kind == 1 ? -iv : iv);
+      l32[q].pad = 0;
+    }
+  }
+  SRS_TRY(dev_upload(s, (float4**)&a.a, A.data(), A.size()));
+  SRS_TRY(dev_upload(s, (int4**)&a.nb, NB.data(), NB.size()));
+  SRS_TRY(dev_upload(s, (float**)&a.bsl, bsl.data(), bsl.size()));
+  if (any_kb) SRS_TRY(dev_upload(s, (float**)&a.kb, kb.data(), kb.size()));
+  else a.kb = nullptr;
+  SRS_TRY(dev_upload(s, (uint32_t**)&a.flags, flags.data(), flags.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.chan_ptr, ptr.data(), ptr.size()));
+  SRS_TRY(dev_upload(s, (ChanEntry32**)&a.chan_list, l32.data(), l32.size()));
+  SRS_TRY(dev_upload(s, (float**)&a.rest_ca, rest.data(), rest.size()));
+  for (int b = 0; b < 2; ++b) {
+    SRS_TRY(dev_alloc(s, &s->d_M[b], (size_t)s->R * N));
+    SRS_TRY(dev_alloc(s, &s->d_I[b], (size_t)s->R * N));
+  }
+  SRS_TRY(upload_channels_engine_order(s));
+  return SRS_OK;
+}
+
+// ---- FP32 resident engine ----------------------------------------------------
+int resident_partition(srs_sim* s, int C) {
+  // RCM order by domain, cut into C contiguous partitions; inside each, the
+  // elements carrying channels come first (they are updated by warp 0).
+  const int N = s->N;
+  std::vector<int> base = rcm_order_by_domain(s->m, s->op);
+  std::vector<char> has_ch(N, 0);
+  for (int i = 0; i < s->m.NR; ++i) has_ch[s->m.ryr_ele[i]] = has_ch[s->m.ryr_jsr[i]] = 1;
+  for (int i = 0; i < s->m.NL; ++i) has_ch[s->m.lcc_ele[i]] = 1;
+  s->part_start.assign(C, 0);
+  s->part_len.assign(C, 0);
+  s->part_nch.assign(C, 0);
+  int Pmax = 0;
+  for (int q = 0; q < C; ++q) {
+    int b = (int)((int64_t)N * q / C), e = (int)((int64_t)N * (q + 1) / C);
+    s->part_len[q] = e - b;
+    Pmax = std::max(Pmax, e - b);
+  }
+  int bits = 1;
+  while ((1 << bits) < Pmax) ++bits;
+  int rank_bits = 0;
+  while ((1 << rank_bits) < C) ++rank_bits;
+  if (bits + rank_bits > 16) return fail(SRS_ERR_UNSUPPORTED, "partition too large for 16-bit element codes");
+  s->off_bits = bits;
+  s->P_stride = (Pmax + 3) & ~3;
+  // engine index = q * P_stride + local offset
+  s->ref_of_eng.assign((size_t)C * s->P_stride, -1);
+  s->eng_of_ref.assign(N, -1);
+  for (int q = 0; q < C; ++q) {
+    int b = (int)((int64_t)N * q / C), e = (int)((int64_t)N * (q + 1) / C);
+    std::vector<int> first, rest;
+    for (int i = b; i < e; ++i) (has_ch[base[i]] ? first : rest).push_back(base[i]);
+    s->part_nch[q] = (int)first.size();
+    int off = 0;
+    for (int j : first) {
+      s->ref_of_eng[(size_t)q * s->P_stride + off] = j;
+      s->eng_of_ref[j] = q * s->P_stride + off;
+      ++off;
+    }
+    for (int j : rest) {
+      s->ref_of_eng[(size_t)q * s->P_stride + off] = j;
+      s->eng_of_ref[j] = q * s->P_stride + off;
+      ++off;
+    }
+  }
+  return SRS_OK;
+}
+
+uint16_t code_of(const srs_sim* s, int eng) {
+  int q = eng / s->P_stride, off = eng % s->P_stride;
+  return (uint16_t)((q << s->off_bits) | off);
+}
+
+int setup_resident(srs_sim* s, int C, int threads) {
+  SRS_TRY(check_fp32_supported(s, true));
+  SRS_TRY(resident_partition(s, C));
+  const int N = s->N;
+  const int NE = C * s->P_stride;
+  // rest arrays over the padded engine numbering
+  s->rest_ca.assign(NE, 0.0);
+  s->rest_imm.assign(NE, 0.0);
+  for (int e = 0; e < NE; ++e) {
+    int j = s->ref_of_eng[e];
+    if (j < 0) continue;
+    bool jsr = s->m.domain[j] == DOMAIN_JSR;
+    s->rest_ca[e] = jsr ? s->rv.ca0_jsr : s->rv.ca0;
+    s->rest_imm[e] = jsr ? s->rv.csqn : (s->m.tropc[j] ? s->rv.trpn : 0.0);
+  }
+  std::vector<TetRec> geo(NE);
+  std::memset(geo.data(), 0, geo.size() * sizeof(TetRec));
+  std::vector<int32_t> ptr_all;
+  std::vector<ChanEntry> list_all;
+  {
+    // per-element lists in engine numbering (N here is the padded count)
+    std::vector<std::vector<ChanEntry>> per(NE);
+    for (int i = 0; i < s->m.NR; ++i) {
+      per[s->eng_of_ref[s->m.ryr_ele[i]]].push_back({0, i});
+      per[s->eng_of_ref[s->m.ryr_jsr[i]]].push_back({1, i});
+    }
+    for (int i = 0; i < s->m.NL; ++i) per[s->eng_of_ref[s->m.lcc_ele[i]]].push_back({2, i});
+    int maxch = *std::max_element(s->part_nch.begin(), s->part_nch.end());
+    int stride = maxch + 1;
+    std::vector<int32_t> cptr((size_t)C * stride, 0);
+    std::vector<ChanEntry32> clist;
+    for (int q = 0; q < C; ++q) {
+      for (int i = 0; i < s->part_nch[q]; ++i) {
+        int e = q * s->P_stride + i;
+        cptr[(size_t)q * stride + i] = (int32_t)clist.size();
+        double iv = 1.0 / s->m.V0[s->ref_of_eng[e]];
+        for (auto& ce : per[e])
+          clist.push_back({ce.kind, ce.ch, (float)(ce.kind == 1 ? -iv : iv), 0});
+      }
+      for (int i = s->part_nch[q]; i < stride; ++i) cptr[(size_t)q * stride + i] = (int32_t)clist.size();
+    }
+    s->ar.ch_stride = stride;
+    SRS_TRY(dev_upload(s, (int32_t**)&s->ar.ch_ptr, cptr.data(), cptr.size()));
+    SRS_TRY(dev_upload(s, (ChanEntry32**)&s->ar.ch_list, clist.data(), clist.size()));
+    for (int e = 0; e < NE; ++e) {
+      int j = s->ref_of_eng[e];
+      if (j < 0) {
+        // padding slot: isolated element with zero coefficients
+        for (int k = 0; k < 4; ++k) geo[e].nb[k] = code_of(s, e);
+        continue;
+      }
+      const double* aj = &s->op.aij[5 * (size_t)j];
+      const int* nj = &s->op.nij[4 * (size_t)j];
+      for (int k = 0; k < 4; ++k) {
+        geo[e].a[k] = (float)aj[1 + k];
+        geo[e].nb[k] = code_of(s, s->eng_of_ref[nj[k]]);
+      }
+      geo[e].bsl = bsl_of(s, j);
+      geo[e].flags = (s->m.domain[j] == DOMAIN_JSR ? 1u : 0u) | (s->m.tropc[j] ? 2u : 0u) |
+                     (per[e].empty() ? 0u : 4u);
+    }
+  }
+  (void)N;
+  ResidentArgs& a = s->ar;
+  a.R = s->R;
+  a.P = s->P_stride;
+  a.off_bits = s->off_bits;
+  SRS_TRY(dev_upload(s, (TetRec**)&a.geo, geo.data(), geo.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.n_local, s->part_len.data(), s->part_len.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.n_chtet, s->part_nch.data(), s->part_nch.size()));
+  std::vector<uint16_t> rc(s->NR), rj(s->NR), lc(s->NL);
+  std::vector<float> lrest(s->NL);
+  for (int i = 0; i < s->NR; ++i) {
+    rc[i] = code_of(s, s->eng_of_ref[s->m.ryr_ele[i]]);
+    rj[i] = code_of(s, s->eng_of_ref[s->m.ryr_jsr[i]]);
+  }
+  for (int i = 0; i < s->NL; ++i) {
+    lc[i] = code_of(s, s->eng_of_ref[s->m.lcc_ele[i]]);
+    lrest[i] = (float)s->rest_ca[s->eng_of_ref[s->m.lcc_ele[i]]];
+  }
+  SRS_TRY(dev_upload(s, (uint16_t**)&a.ryr_cleft_code, rc.data(), rc.size()));
+  SRS_TRY(dev_upload(s, (uint16_t**)&a.ryr_jsr_code, rj.data(), rj.size()));
+  SRS_TRY(dev_upload(s, (uint16_t**)&a.lcc_code, lc.data(), lc.size()));
+  SRS_TRY(dev_upload(s, (float**)&a.lcc_rest, lrest.data(), lrest.size()));
+  // Channels for the protocol code: codes by kind (see ResidentCa)
+  std::vector<int32_t> kc(s->NR), kj(s->NR), kl(s->NL);
+  for (int i = 0; i < s->NR; ++i) {
+    kc[i] = i;
+    kj[i] = (1 << 28) | i;
+  }
+  for (int i = 0; i < s->NL; ++i) kl[i] = (2 << 28) | i;
+  int32_t *p1, *p2, *p3, *p4;
+  SRS_TRY(dev_upload(s, &p1, kc.data(), kc.size()));
+  SRS_TRY(dev_upload(s, &p2, kj.data(), kj.size()));
+  SRS_TRY(dev_upload(s, &p3, s->m.ryr_nb.data(), s->m.ryr_nb.size()));
+  SRS_TRY(dev_upload(s, &p4, kl.data(), kl.size()));
+  s->ch.NR = s->NR;
+  s->ch.NL = s->NL;
+  s->ch.ryr_cleft = p1;
+  s->ch.ryr_jsr = p2;
+  s->ch.ryr_nb = p3;
+  s->ch.lcc_ele = p4;
+  SRS_TRY(dev_alloc(s, &s->d_M[0], (size_t)s->R * NE));
+  SRS_TRY(dev_alloc(s, &s->d_I[0], (size_t)s->R * NE));
+  s->C = C;
+  s->threads = threads;
+  s->smem = resident_smem_bytes(s->P_stride, s->NR, s->NL);
+  int maxc = resident_max_clusters(C, threads, s->smem);
+  if (maxc <= 0) return fail(SRS_ERR_UNSUPPORTED, "resident configuration does not fit on the device");
+  s->n_clusters = std::min(maxc, s->R);
+  return SRS_OK;
+}
+
+// Engine-layout offsets of realization r.
+size_t eng_count(const srs_sim* s) {
+  return s->d.engine == SRS_ENGINE_RESIDENT ? (size_t)s->C * s->P_stride : (size_t)s->N;
+}
+
+// ---- state conversion ---------------------------------------------------------
+int upload_state(srs_sim* s, int r, const double* S6) {
+  const int N = s->N;
+  if (s->d.precision == SRS_FP64) {
+    SRS_CUDA(cudaMemcpy(s->d_S[0] + (size_t)r * 6 * N, S6, sizeof(double) * 6 * N,
+                        cudaMemcpyHostToDevice));
+    return SRS_OK;
+  }
+  size_t NE = eng_count(s);
+  std::vector<float4> M(NE, make_float4(0, 0, 0, 0));
+  std::vector<float> I(NE, 0.0f);
+  const RestValues& rv = s->rv;
+  for (size_t e = 0; e < NE; ++e) {
+    int j = s->ref_of_eng[e];
+    if (j < 0) continue;
+    M[e] = make_float4((float)(S6[SP_CA * (size_t)N + j] - s->rest_ca[e]),
+                       (float)(S6[SP_ATP * (size_t)N + j] - rv.atp),
+                       (float)(S6[SP_CMDN * (size_t)N + j] - rv.cmdn),
+                       (float)(S6[SP_DYE * (size_t)N + j] - rv.dye));
+    bool jsr = s->m.domain[j] == DOMAIN_JSR;
+    double imm = jsr ? S6[SP_CSQN * (size_t)N + j] : S6[SP_TRPN * (size_t)N + j];
+    I[e] = (float)(imm - s->rest_imm[e]);
+  }
+  SRS_CUDA(cudaMemcpy(s->d_M[0] + r * NE, M.data(), NE * sizeof(float4), cudaMemcpyHostToDevice));
+  SRS_CUDA(cudaMemcpy(s->d_I[0] + r * NE, I.data(), NE * sizeof(float), cudaMemcpyHostToDevice));
+  return SRS_OK;
+}
+
+int download_state(srs_sim* s, int r, double* S6) {
+  const int N = s->N;
+  if (s->d.precision == SRS_FP64) {
+    SRS_CUDA(cudaMemcpy(S6, s->d_S[0] + (size_t)r * 6 * N, sizeof(double) * 6 * N,
+                        cudaMemcpyDeviceToHost));
+    return SRS_OK;
+  }
+  size_t NE = eng_count(s);
+  std::vector<float4> M(NE);
+  std::vector<float> I(NE);
+  SRS_CUDA(cudaMemcpy(M.data(), s->d_M[0] + r * NE, NE * sizeof(float4), cudaMemcpyDeviceToHost));
+  SRS_CUDA(cudaMemcpy(I.data(), s->d_I[0] + r * NE, NE * sizeof(float), cudaMemcpyDeviceToHost));
+  const RestValues& rv = s->rv;
+  for (size_t e = 0; e < NE; ++e) {
+    int j = s->ref_of_eng[e];
+    if (j < 0) continue;
+    bool jsr = s->m.domain[j] == DOMAIN_JSR;
+    S6[SP_CA * (size_t)N + j] = s->rest_ca[e] + (double)M[e].x;
+    S6[SP_ATP * (size_t)N + j] = rv.atp + (double)M[e].y;
+    S6[SP_CMDN * (size_t)N + j] = rv.cmdn + (double)M[e].z;
+    S6[SP_DYE * (size_t)N + j] = rv.dye + (double)M[e].w;
+    double imm = s->rest_imm[e] + (double)I[e];
+    S6[SP_TRPN * (size_t)N + j] = jsr ? 0.0 : imm;
+    S6[SP_CSQN * (size_t)N + j] = jsr ? imm : 0.0;
+  }
+  return SRS_OK;
+}
+
+// After a run of the plain engines realization r's state sits in buffer
+// (steps taken) % 2; move it to buffer 0.
+int normalize_buffers(srs_sim* s, const std::vector<int64_t>& steps_before) {
+  if (s->d.engine == SRS_ENGINE_RESIDENT) return SRS_OK;
+  std::vector<RealCtl> ctl(s->R);
+  SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+  const size_t N = s->N;
+  for (int r = 0; r < s->R; ++r) {
+    if (((ctl[r].step - steps_before[r]) & 1) == 0) continue;
+    if (s->d.precision == SRS_FP64) {
+      SRS_CUDA(cudaMemcpyAsync(s->d_S[0] + r * 6 * N, s->d_S[1] + r * 6 * N, sizeof(double) * 6 * N,
+                               cudaMemcpyDeviceToDevice, s->st));
+    } else {
+      SRS_CUDA(cudaMemcpyAsync(s->d_M[0] + r * N, s->d_M[1] + r * N, sizeof(float4) * N,
+                               cudaMemcpyDeviceToDevice, s->st));
+      SRS_CUDA(cudaMemcpyAsync(s->d_I[0] + r * N, s->d_I[1] + r * N, sizeof(float) * N,
+                               cudaMemcpyDeviceToDevice, s->st));
+    }
+  }
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  return SRS_OK;
+}
+
+std::vector<int64_t> ctl_steps(srs_sim* s) {
+  std::vector<RealCtl> ctl(s->R);
+  cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost);
+  std::vector<int64_t> v(s->R);
+  for (int r = 0; r < s->R; ++r) v[r] = ctl[r].step;
+  return v;
+}
+
+// ---- launches -----------------------------------------------------------------
+void refresh_args(srs_sim* s) {
+  ChanState cs = chan_state(s);
+  if (s->d.precision == SRS_FP64) {
+    s->a64.P = s->P;
+    s->a64.C = s->ch;
+    s->a64.CS = cs;
+    s->a64.counters = s->d_counters;
+    s->a64.nsr = s->nsr;
+  } else if (s->d.engine == SRS_ENGINE_PLAIN) {
+    s->a32.P = s->P;
+    s->a32.C = s->ch;
+    s->a32.CS = cs;
+    s->a32.counters = s->d_counters;
+    s->a32.k = make_consts32(s);
+  } else {
+    s->ar.P_ = s->P;
+    s->ar.C = s->ch;
+    s->ar.CS = cs;
+    s->ar.k = make_consts32(s);
+    s->ar.M = s->d_M[0];
+    s->ar.I = s->d_I[0];
+  }
+  if (s->graph_plain) {
+    cudaGraphExecDestroy(s->graph_plain);
+    s->graph_plain = nullptr;
+  }
+}
+
+int plain_launch(srs_sim* s, int parity) {
+  int rc;
+  if (s->d.precision == SRS_FP64) {
+    Plain64Args a = s->a64;
+    a.S_in = s->d_S[parity];
+    a.S_out = s->d_S[parity ^ 1];
+    rc = launch_plain64_step(a, s->st);
+  } else {
+    Plain32Args a = s->a32;
+    a.M_in = s->d_M[parity];
+    a.I_in = s->d_I[parity];
+    a.M_out = s->d_M[parity ^ 1];
+    a.I_out = s->d_I[parity ^ 1];
+    rc = launch_plain32_step(a, s->st);
+  }
+  s->launches++;
+  if (rc) return fail(SRS_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(cudaGetLastError()));
+  return SRS_OK;
+}
+
+int plain_prestep(srs_sim* s, int write_initial_row) {
+  int rc;
+  if (s->d.precision == SRS_FP64) {
+    Plain64Args a = s->a64;
+    a.S_in = s->d_S[0];
+    rc = launch_plain64_prestep(a, write_initial_row, s->st);
+  } else {
+    Plain32Args a = s->a32;
+    a.M_in = s->d_M[0];
+    rc = launch_plain32_prestep(a, write_initial_row, s->st);
+  }
+  s->launches++;
+  if (rc) return fail(SRS_ERR_CUDA, "prestep launch failed");
+  return SRS_OK;
+}
+
+// n plain steps starting from buffer 0 (graph-replayed in pairs).
+int plain_steps(srs_sim* s, int64_t n) {
+  const int G = 32;  // launches per graph replay (even)
+  int64_t done = 0;
+  if (n >= G) {
+    if (!s->graph_plain) {
+      cudaGraph_t g;
+      SRS_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+      int64_t l0 = s->launches;
+      for (int i = 0; i < G; ++i) {
+        int rc = plain_launch(s, i & 1);
+        if (rc) {
+          cudaStreamEndCapture(s->st, &g);
+          return rc;
+        }
+      }
+      s->launches = l0;
+      SRS_CUDA(cudaStreamEndCapture(s->st, &g));
+      SRS_CUDA(cudaGraphInstantiate(&s->graph_plain, g, 0));
+      cudaGraphDestroy(g);
+      s->graph_plain_len = G;
+    }
+    while (n - done >= G) {
+      SRS_CUDA(cudaGraphLaunch(s->graph_plain, s->st));
+      s->launches += G;
+      done += G;
+    }
+  }
+  for (; done < n; ++done) SRS_TRY(plain_launch(s, (int)(done & 1)));
+  return SRS_OK;
+}
+
+int resident_launch(srs_sim* s, int steps) {
+  ResidentArgs a = s->ar;
+  a.steps = steps;
+  int rc = launch_resident(a, s->C, s->n_clusters, s->threads, s->smem, s->st);
+  s->launches++;
+  if (rc) return fail(SRS_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(cudaGetLastError()));
+  return SRS_OK;
+}
+
+int advance(srs_sim* s, int64_t n) {
+  if (s->d.engine == SRS_ENGINE_RESIDENT) {
+    const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
+    for (int64_t done = 0; done < n;) {
+      int k = (int)std::min<int64_t>(S, n - done);
+      SRS_TRY(resident_launch(s, k));
+      done += k;
+    }
+    return SRS_OK;
+  }
+  return plain_steps(s, n);
+}
+
+int ensure_rows(srs_sim* s, int64_t cap, int w) {
+  if (cap <= s->rows_cap_alloc && w == s->rows_w_alloc) return SRS_OK;
+  void* p = nullptr;
+  SRS_CUDA(cudaMalloc(&p, std::max<size_t>(1, (size_t)s->R * cap * w) * sizeof(float)));
+  s->allocs.push_back(p);
+  s->d_rows = (float*)p;
+  s->rows_cap_alloc = cap;
+  s->rows_w_alloc = w;
+  return SRS_OK;
+}
+
+int set_schedule(srs_sim* s, const Schedule& sc) {
+  std::vector<int64_t> ticks = sc.tick_steps;
+  std::vector<double> tt = sc.tick_times;
+  if (ticks.empty()) {
+    ticks.push_back(-1);
+    tt.push_back(0.0);
+  }
+  SRS_TRY(dev_upload(s, &s->d_ticks, ticks.data(), ticks.size()));
+  SRS_TRY(dev_upload(s, &s->d_tick_t, tt.data(), tt.size()));
+  s->P.ticks = s->d_ticks;
+  s->P.tick_t = s->d_tick_t;
+  s->P.n_ticks = (int32_t)sc.tick_steps.size();
+  s->P.n_steps = sc.n_steps;
+  s->P.clamp_end = sc.clamp_end_step;
+  s->P.hold_end = sc.hold_end_step;
+  return SRS_OK;
+}
+
+int check_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(SRS_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  SRS_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(SRS_ERR_CUDA, "this build targets sm_103a (GB300); device is sm_" +
+                                  std::to_string(prop.major) + std::to_string(prop.minor));
+  return SRS_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+const char* srs_status_string(int status) {
+  switch (status) {
+    case SRS_OK: return "ok";
+    case SRS_ERR_INPUT: return "invalid input";
+    case SRS_ERR_IO: return "i/o error";
+    case SRS_ERR_MESH: return "invalid mesh";
+    case SRS_ERR_UNSTABLE: return "unstable time step";
+    case SRS_ERR_CUDA: return "cuda error";
+    case SRS_ERR_UNSUPPORTED: return "unsupported configuration";
+    case SRS_ERR_NONFINITE: return "non-finite state";
+    case SRS_ERR_TIMEOUT: return "device wait timed out";
+    case SRS_ERR_STATE: return "call out of order";
+    case SRS_ERR_NOMEM: return "out of memory";
+    default: return "unknown status";
+  }
+}
+const char* srs_last_error(void) { return g_err.c_str(); }
+const char* srs_version(void) { return "srs_gb300 0.1 (sm_103a)"; }
+
+void srs_default_parameters(srs_params* ps) { params_default(ps); }
+
+int srs_read_parameters(srs_params* ps, const char* param_file) {
+  if (!ps || !param_file) return fail(SRS_ERR_INPUT, "null argument");
+  std::string err;
+  int rc = params_read_xml(param_file, ps, &err);
+  if (rc) return fail(rc, err);
+  return SRS_OK;
+}
+
+int srs_read_grid(const srs_params* ps, const char* mesh_base, srs_grid** out) {
+  if (!ps || !mesh_base || !out) return fail(SRS_ERR_INPUT, "null argument");
+  srs_grid* g = new srs_grid();
+  g->p = *ps;
+  std::string err;
+  int rc = mesh_read(mesh_base, ps->ints[I_FLAG_NO_FLUX_BOUNDARY], &g->m, &err);
+  if (!rc) rc = assemble_operator(g->m, g->p, &g->op, &err);
+  if (rc) {
+    delete g;
+    return fail(rc, err);
+  }
+  *out = g;
+  return SRS_OK;
+}
+
+void srs_free_grid(srs_grid* g) { delete g; }
+
+int srs_grid_get_info(const srs_grid* g, srs_grid_info* info) {
+  if (!g || !info) return fail(SRS_ERR_INPUT, "null argument");
+  info->n_ele = g->m.N;
+  info->n_face = g->m.NF;
+  info->n_nodes = g->m.NN;
+  info->n_ryr = g->m.NR;
+  info->n_lcc = g->m.NL;
+  int nj = 0;
+  double vj = 0;
+  for (int i = 0; i < g->m.N; ++i)
+    if (g->m.domain[i] == DOMAIN_JSR) {
+      ++nj;
+      vj += g->m.V0[i];
+    }
+  info->n_jsr = nj;
+  info->vol_jsr = vj;
+  info->max_diag = g->op.max_diag;
+  return SRS_OK;
+}
+
+int srs_grid_get_operator(const srs_grid* g, double* aij, int* nij, double* br) {
+  if (!g) return fail(SRS_ERR_INPUT, "null argument");
+  if (aij) std::memcpy(aij, g->op.aij.data(), g->op.aij.size() * sizeof(double));
+  if (nij) std::memcpy(nij, g->op.nij.data(), g->op.nij.size() * sizeof(int));
+  if (br) std::memcpy(br, g->op.br.data(), g->op.br.size() * sizeof(double));
+  return SRS_OK;
+}
+
+int srs_grid_get_elements(const srs_grid* g, double* v0, double* tt, int* domain, int* tropc,
+                          int* file_index) {
+  if (!g) return fail(SRS_ERR_INPUT, "null argument");
+  const int N = g->m.N;
+  if (v0) std::memcpy(v0, g->m.V0.data(), N * sizeof(double));
+  if (tt) std::memcpy(tt, g->m.TT.data(), N * sizeof(double));
+  if (domain) std::memcpy(domain, g->m.domain.data(), N * sizeof(int));
+  if (tropc) std::memcpy(tropc, g->m.tropc.data(), N * sizeof(int));
+  if (file_index) std::memcpy(file_index, g->m.order.data(), N * sizeof(int));
+  return SRS_OK;
+}
+
+int srs_grid_get_channels(const srs_grid* g, int* ryr_ele, int* ryr_jsr, int* ryr_nb, int* lcc) {
+  if (!g) return fail(SRS_ERR_INPUT, "null argument");
+  if (ryr_ele) std::memcpy(ryr_ele, g->m.ryr_ele.data(), g->m.NR * sizeof(int));
+  if (ryr_jsr) std::memcpy(ryr_jsr, g->m.ryr_jsr.data(), g->m.NR * sizeof(int));
+  if (ryr_nb) std::memcpy(ryr_nb, g->m.ryr_nb.data(), 4 * g->m.NR * sizeof(int));
+  if (lcc) std::memcpy(lcc, g->m.lcc_ele.data(), g->m.NL * sizeof(int));
+  return SRS_OK;
+}
+
+int srs_initial_states(const srs_grid* g, const srs_params* ps, double* states) {
+  if (!g || !ps || !states) return fail(SRS_ERR_INPUT, "null argument");
+  std::vector<double> S;
+  initial_states(g->m, *ps, &S);
+  std::memcpy(states, S.data(), S.size() * sizeof(double));
+  return SRS_OK;
+}
+
+int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* d, srs_sim** out) {
+  if (!g || !ps || !d || !out) return fail(SRS_ERR_INPUT, "null argument");
+  if (d->n_realizations <= 0) return fail(SRS_ERR_INPUT, "n_realizations must be positive");
+  if (d->precision != SRS_FP64 && d->precision != SRS_FP32)
+    return fail(SRS_ERR_INPUT, "precision must be 64 or 32");
+  if (d->engine != SRS_ENGINE_PLAIN && d->engine != SRS_ENGINE_RESIDENT)
+    return fail(SRS_ERR_INPUT, "unknown engine");
+  if (d->engine == SRS_ENGINE_RESIDENT && d->precision != SRS_FP32)
+    return fail(SRS_ERR_UNSUPPORTED, "the resident engine runs in FP32");
+  if (ps->ints[I_GATING_FFWD])
+    return fail(SRS_ERR_UNSUPPORTED, "flag_ffwd (steady-state gating fast-forward) is not supported");
+  if (g->m.NR <= 0) return fail(SRS_ERR_MESH, "mesh has no RyRs");
+  if (g->m.NR > 1024 && ps->reals[R_RYR_A_STAR] != 0)
+    return fail(SRS_ERR_UNSUPPORTED, "coupled gating supports at most 1024 RyRs");
+  // explicit stability: D_max * dt * max|a0| <= 1
+  double Dmax = std::max(std::max(ps->reals[R_D_CA], ps->reals[R_D_ATP]),
+                         std::max(ps->reals[R_D_CMDN], ps->reals[R_D_DYE]));
+  double cfl = Dmax * ps->reals[R_T_STEP] * g->op.max_diag;
+  if (!(cfl <= 1.0))
+    return fail(SRS_ERR_UNSTABLE, "explicit step unstable: D*dt*max|a0| = " + std::to_string(cfl));
+  SRS_TRY(check_device());
+  srs_sim* s = new srs_sim();
+  s->m = g->m;
+  s->op = g->op;
+  s->p = *ps;
+  s->d = *d;
+  s->R = d->n_realizations;
+  s->N = g->m.N;
+  s->NR = g->m.NR;
+  s->NL = g->m.NL;
+  s->NCH = s->NR + s->NL;
+  s->rv = rest_values(*ps);
+  s->vm = ps->reals[R_DEFAULT_VM];
+  s->nsr = ps->reals[R_DEFAULT_CA_NSR];
+  s->seeds.resize(s->R);
+  for (int r = 0; r < s->R; ++r) s->seeds[r] = d->seeds ? d->seeds[r] : (uint64_t)(r + 1);
+  s->d.seeds = nullptr;
+  int rc = SRS_OK;
+  if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(SRS_ERR_CUDA, "stream creation failed");
+  if (!rc) rc = alloc_channel_state(s);
+  if (!rc) fill_protocol_consts(s);
+  if (!rc) {
+    if (d->precision == SRS_FP64) rc = setup_plain64(s);
+    else if (d->engine == SRS_ENGINE_PLAIN) rc = setup_plain32(s);
+    else {
+      // resident: smallest cluster whose partition fits in shared memory
+      int threads = d->threads_per_cta > 0 ? d->threads_per_cta : 1024;
+      int C = d->cluster_size;
+      if (C <= 0) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        for (int c : {1, 2, 4, 8, 16}) {
+          int Pm = (s->N + c - 1) / c;
+          Pm = (Pm + 3) & ~3;
+          if (resident_smem_bytes(Pm, s->NR, s->NL) <= (size_t)optin) {
+            C = c;
+            break;
+          }
+        }
+        if (C <= 0) rc = fail(SRS_ERR_UNSUPPORTED, "mesh too large for the resident engine");
+      }
+      if (!rc) rc = setup_resident(s, C, threads);
+    }
+  }
+  if (rc) {
+    srs_sim_destroy(s);
+    return rc;
+  }
+  s->d.cluster_size = s->C;
+  s->d.threads_per_cta = s->threads;
+  s->P.run_protocol = 0;
+  s->P.row_cap = 0;
+  refresh_args(s);
+  rc = srs_sim_reset(s);
+  if (rc) {
+    srs_sim_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return SRS_OK;
+}
+
+void srs_sim_destroy(srs_sim* s) {
+  if (!s) return;
+  if (s->graph_plain) cudaGraphExecDestroy(s->graph_plain);
+  if (s->st) cudaStreamSynchronize(s->st);
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+}
+
+int srs_sim_get_desc(const srs_sim* s, srs_sim_desc* d) {
+  if (!s || !d) return fail(SRS_ERR_INPUT, "null argument");
+  *d = s->d;
+  return SRS_OK;
+}
+
+int srs_sim_get_config(const srs_sim* s, srs_sim_config* c) {
+  if (!s || !c) return fail(SRS_ERR_INPUT, "null argument");
+  c->engine = s->d.engine;
+  c->precision = s->d.precision;
+  c->threads_per_cta = s->d.engine == SRS_ENGINE_RESIDENT ? s->threads : 256;
+  c->cluster_size = s->d.engine == SRS_ENGINE_RESIDENT ? s->C : 1;
+  c->steps_per_launch =
+      s->d.engine == SRS_ENGINE_RESIDENT ? (s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000) : 1;
+  c->smem_bytes = (int)s->smem;
+  c->kernel_launches = s->launches;
+  return SRS_OK;
+}
+
+int srs_sim_reset(srs_sim* s) {
+  if (!s) return fail(SRS_ERR_INPUT, "null argument");
+  const Mesh& m = s->m;
+  const srs_params& p = s->p;
+  const int* I = p.ints;
+  const double* Rr = p.reals;
+  std::vector<double> S6;
+  initial_states(m, p, &S6);
+  const int NR = s->NR, NL = s->NL, NCH = s->NCH;
+  std::vector<int32_t> ryr((size_t)s->R * NR, 0), lcc((size_t)s->R * NL, 1), lccv((size_t)s->R * NL, 2);
+  std::vector<double> res((size_t)s->R * NCH);
+  std::vector<RealCtl> ctl(s->R);
+  if (I[I_INIT_RYR] != -1 && !I[I_FLAG_LCC] && !I[I_FLAG_V_CLAMP] &&
+      (I[I_INIT_RYR] < 0 || I[I_INIT_RYR] >= NR))
+    return fail(SRS_ERR_INPUT, "Invalid initial RyR index (" + std::to_string(I[I_INIT_RYR]) +
+                                   "), must be -1 to ignore, or between 0 and the number of RyRs");
+  if (I[I_FLAG_LCC] && (I[I_LCC_INDEX] < 0 || I[I_LCC_INDEX] >= NL))
+    return fail(SRS_ERR_INPUT, "LCC trigger index out of range");
+  for (int r = 0; r < s->R; ++r) {
+    const uint64_t seed = s->seeds[r];
+    int32_t* ry = &ryr[(size_t)r * NR];
+    int32_t* lc = &lcc[(size_t)r * NL];
+    // initial channel opening (cpu/main.cpp:217-250)
+    if (I[I_FLAG_LCC]) {
+      lc[I[I_LCC_INDEX]] = 6;
+    } else if (I[I_FLAG_V_CLAMP]) {
+    } else if (I[I_INIT_RYR] != -1) {
+      ry[I[I_INIT_RYR]] = 1;
+    } else {
+      // OpenRandomRyR (cpu/InitFuncs.cpp:1420-1475): rate-weighted choice with
+      // the linear luminal factor it uses, drawn from protocol stream 1.
+      std::vector<double> rate(NR);
+      double tot = 0;
+      for (int i = 0; i < NR; ++i) {
+        int no = 0, nc = 0;
+        for (int k = 0; k < 4; ++k) {
+          int j = m.ryr_nb[4 * i + k];
+          if (j >= 0) (ry[j] ? no : nc)++;
+        }
+        double ca_ss = S6[SP_CA * (size_t)m.N + m.ryr_ele[i]];
+        double phi = Rr[R_RYR_PHI_M] * S6[SP_CA * (size_t)m.N + m.ryr_jsr[i]] + Rr[R_RYR_PHI_B];
+        double X = std::exp(0.5 * Rr[R_RYR_A_STAR] * (nc * Rr[R_RYR_EPS_CC] - no * Rr[R_RYR_EPS_OO]));
+        rate[i] = X * phi * Rr[R_RYR_K_PLUS] * std::pow(ca_ss, Rr[R_RYR_ETA]);
+        tot += rate[i];
+      }
+      double u = tot * srs_protocol_uniform(seed, 1);
+      int pick = 0;
+      double sum = 0;
+      for (int i = 0; i < NR; ++i) {
+        sum += rate[i];
+        if (sum >= u) {
+          pick = i;
+          break;
+        }
+      }
+      ry[pick] = 1;
+    }
+    for (int i = 0; i < NCH; ++i) res[(size_t)r * NCH + i] = srs_initial_residual(seed, (uint32_t)i);
+    RealCtl& c = ctl[r];
+    std::memset(&c, 0, sizeof(c));
+    c.seed = seed;
+    c.lcc_open = I[I_FLAG_LCC];
+    c.lcc_close_step = -1;
+    if (I[I_FLAG_LCC]) {
+      double T = -Rr[R_LCC_DURATION] * srs_log(srs_protocol_uniform(seed, 0));
+      c.lcc_close_step = first_step_at_or_after(p, T);
+    }
+    int n_open = 0;
+    for (int i = 0; i < NR; ++i) n_open += ry[i];
+    c.n_open_tick = n_open;
+  }
+  for (int r = 0; r < s->R; ++r) SRS_TRY(upload_state(s, r, S6.data()));
+  SRS_CUDA(cudaMemcpy(s->d_ryr, ryr.data(), ryr.size() * 4, cudaMemcpyHostToDevice));
+  SRS_CUDA(cudaMemcpy(s->d_lcc, lcc.data(), lcc.size() * 4, cudaMemcpyHostToDevice));
+  SRS_CUDA(cudaMemcpy(s->d_lccv, lccv.data(), lccv.size() * 4, cudaMemcpyHostToDevice));
+  SRS_CUDA(cudaMemcpy(s->d_res, res.data(), res.size() * 8, cudaMemcpyHostToDevice));
+  SRS_CUDA(cudaMemcpy(s->d_ctl, ctl.data(), ctl.size() * sizeof(RealCtl), cudaMemcpyHostToDevice));
+  SRS_CUDA(cudaMemset(s->d_counters, 0, sizeof(unsigned) * s->R));
+  return SRS_OK;
+}
+
+int srs_sim_set_state(srs_sim* s, int r, const double* states, const int* ryr, const int* lcc,
+                      const int* lccv, const double* res) {
+  if (!s || r < 0 || r >= s->R) return fail(SRS_ERR_INPUT, "bad realization index");
+  if (states) SRS_TRY(upload_state(s, r, states));
+  if (ryr) SRS_CUDA(cudaMemcpy(s->d_ryr + (size_t)r * s->NR, ryr, s->NR * 4, cudaMemcpyHostToDevice));
+  if (lcc) SRS_CUDA(cudaMemcpy(s->d_lcc + (size_t)r * s->NL, lcc, s->NL * 4, cudaMemcpyHostToDevice));
+  if (lccv) SRS_CUDA(cudaMemcpy(s->d_lccv + (size_t)r * s->NL, lccv, s->NL * 4, cudaMemcpyHostToDevice));
+  if (res) SRS_CUDA(cudaMemcpy(s->d_res + (size_t)r * s->NCH, res, s->NCH * 8, cudaMemcpyHostToDevice));
+  return SRS_OK;
+}
+
+int srs_sim_get_state(srs_sim* s, int r, double* states, int* ryr, int* lcc, int* lccv, double* res) {
+  if (!s || r < 0 || r >= s->R) return fail(SRS_ERR_INPUT, "bad realization index");
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  if (states) SRS_TRY(download_state(s, r, states));
+  if (ryr) SRS_CUDA(cudaMemcpy(ryr, s->d_ryr + (size_t)r * s->NR, s->NR * 4, cudaMemcpyDeviceToHost));
+  if (lcc) SRS_CUDA(cudaMemcpy(lcc, s->d_lcc + (size_t)r * s->NL, s->NL * 4, cudaMemcpyDeviceToHost));
+  if (lccv) SRS_CUDA(cudaMemcpy(lccv, s->d_lccv + (size_t)r * s->NL, s->NL * 4, cudaMemcpyDeviceToHost));
+  if (res) SRS_CUDA(cudaMemcpy(res, s->d_res + (size_t)r * s->NCH, s->NCH * 8, cudaMemcpyDeviceToHost));
+  return SRS_OK;
+}
+
+int srs_sim_set_globals(srs_sim* s, double v_m, double ca_nsr) {
+  if (!s) return fail(SRS_ERR_INPUT, "null argument");
+  s->vm = v_m;
+  s->nsr = ca_nsr;
+  fill_protocol_consts(s);
+  refresh_args(s);
+  return SRS_OK;
+}
+
+int srs_explicit_step(srs_sim* s, int64_t n_steps) {
+  if (!s || n_steps < 0) return fail(SRS_ERR_INPUT, "bad argument");
+  std::vector<int64_t> before = ctl_steps(s);
+  s->P.run_protocol = 0;
+  refresh_args(s);
+  SRS_TRY(advance(s, n_steps));
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  SRS_TRY(normalize_buffers(s, before));
+  return SRS_OK;
+}
+
+int srs_sim_advance_async(srs_sim* s, int64_t n_steps) {
+  if (!s || n_steps < 0) return fail(SRS_ERR_INPUT, "bad argument");
+  if (s->d.engine != SRS_ENGINE_RESIDENT && (n_steps & 1))
+    return fail(SRS_ERR_INPUT, "plain engines advance asynchronously by an even number of steps");
+  if (s->P.run_protocol) {
+    s->P.run_protocol = 0;
+    refresh_args(s);
+  }
+  return advance(s, n_steps);
+}
+
+int srs_sim_synchronize(srs_sim* s) {
+  if (!s) return fail(SRS_ERR_INPUT, "null argument");
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  return SRS_OK;
+}
+
+int srs_sim_time_advance(srs_sim* s, int64_t n_steps, float* ms) {
+  if (!s || !ms) return fail(SRS_ERR_INPUT, "null argument");
+  cudaEvent_t e0, e1;
+  SRS_CUDA(cudaEventCreate(&e0));
+  SRS_CUDA(cudaEventCreate(&e1));
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  SRS_CUDA(cudaEventRecord(e0, s->st));
+  int rc = srs_sim_advance_async(s, n_steps);
+  SRS_CUDA(cudaEventRecord(e1, s->st));
+  SRS_CUDA(cudaEventSynchronize(e1));
+  SRS_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int srs_sim_status(srs_sim* s, int* bits) {
+  if (!s || !bits) return fail(SRS_ERR_INPUT, "null argument");
+  std::vector<RealCtl> ctl(s->R);
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+  int b = 0;
+  for (auto& c : ctl) b |= (int)c.status;
+  *bits = b;
+  return SRS_OK;
+}
+
+int srs_run_simulation(srs_sim* s, srs_run_output* out) {
+  if (!s || !out || !out->rows || out->row_capacity <= 0) return fail(SRS_ERR_INPUT, "bad output");
+  Schedule sc = make_schedule(s->p);
+  fill_protocol_consts(s);
+  if (out->row_width != s->P.row_w)
+    return fail(SRS_ERR_INPUT, "row_width must be " + std::to_string(s->P.row_w));
+  SRS_TRY(set_schedule(s, sc));
+  SRS_TRY(ensure_rows(s, out->row_capacity, s->P.row_w));
+  s->P.row_cap = out->row_capacity;
+  s->P.run_protocol = 1;
+  refresh_args(s);
+  std::vector<int64_t> before = ctl_steps(s);
+  std::vector<RealCtl> ctl(s->R);
+  if (s->d.engine != SRS_ENGINE_RESIDENT) {
+    SRS_TRY(plain_prestep(s, 1));
+    int64_t total = 0;
+    const int64_t chunk = 4096;
+    while (true) {
+      int64_t n = std::min<int64_t>(chunk, sc.n_steps + 1 - total);
+      if (n <= 0) break;
+      // plain_steps assumes buffer 0 at the start: alternate by the global count
+      if (total & 1) return fail(SRS_ERR_STATE, "internal: odd chunk");
+      SRS_TRY(plain_steps(s, n + (n & 1)));
+      total += n + (n & 1);
+      SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+      bool all = true;
+      for (auto& c : ctl) all &= c.done != 0;
+      if (all) break;
+    }
+  } else {
+    // t = 0 row for every realization, written on the host from the initial
+    // state (identical to the device row code's inputs)
+    std::vector<float> row0((size_t)s->R * s->P.row_w);
+    std::vector<int32_t> ryr((size_t)s->R * s->NR), lcc((size_t)s->R * s->NL), lccv((size_t)s->R * s->NL);
+    SRS_CUDA(cudaMemcpy(ryr.data(), s->d_ryr, ryr.size() * 4, cudaMemcpyDeviceToHost));
+    SRS_CUDA(cudaMemcpy(lcc.data(), s->d_lcc, lcc.size() * 4, cudaMemcpyDeviceToHost));
+    SRS_CUDA(cudaMemcpy(lccv.data(), s->d_lccv, lccv.size() * 4, cudaMemcpyDeviceToHost));
+    SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+    std::vector<double> S6((size_t)6 * s->N);
+    for (int r = 0; r < s->R; ++r) {
+      SRS_TRY(download_state(s, r, S6.data()));
+      states_row(s->m, s->p, S6.data(), &ryr[(size_t)r * s->NR], &lcc[(size_t)r * s->NL],
+                 &lccv[(size_t)r * s->NL], s->P.Vm[ctl[r].vsel], ctl[r].t,
+                 &row0[(size_t)r * s->P.row_w], s->P.row_w);
+      SRS_CUDA(cudaMemcpy(s->d_rows + (size_t)r * s->P.row_cap * s->P.row_w, &row0[(size_t)r * s->P.row_w],
+                          s->P.row_w * sizeof(float), cudaMemcpyHostToDevice));
+      ctl[r].n_rows = 1;
+    }
+    SRS_CUDA(cudaMemcpy(s->d_ctl, ctl.data(), sizeof(RealCtl) * s->R, cudaMemcpyHostToDevice));
+    const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
+    while (true) {
+      SRS_TRY(resident_launch(s, S));
+      SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+      bool all = true;
+      for (auto& c : ctl) all &= c.done != 0;
+      if (all) break;
+    }
+  }
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  SRS_TRY(normalize_buffers(s, before));
+  SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+  const size_t rw = (size_t)s->P.row_w;
+  SRS_CUDA(cudaMemcpy(out->rows, s->d_rows, (size_t)s->R * out->row_capacity * rw * sizeof(float),
+                      cudaMemcpyDeviceToHost));
+  int st_bits = 0;
+  for (int r = 0; r < s->R; ++r) {
+    if (out->n_rows) out->n_rows[r] = ctl[r].n_rows;
+    if (out->t_end) out->t_end[r] = ctl[r].t;
+    if (out->n_steps) out->n_steps[r] = ctl[r].step;
+    st_bits |= (int)ctl[r].status;
+  }
+  s->P.run_protocol = 0;
+  s->P.row_cap = 0;
+  refresh_args(s);
+  if (st_bits & 1) return fail(SRS_ERR_NONFINITE, "a realization produced a non-finite Ca value");
+  if (st_bits & 4) return fail(SRS_ERR_INPUT, "row_capacity too small for the run");
+  return SRS_OK;
+}
+
+int srs_write_grid_vtk(srs_sim* s, int r, const char* path, int run, int rank, int n, double t) {
+  if (!s || !path || r < 0 || r >= s->R) return fail(SRS_ERR_INPUT, "bad argument");
+  std::vector<double> S6((size_t)6 * s->N);
+  SRS_TRY(download_state(s, r, S6.data()));
+  std::vector<int32_t> ryr(s->NR);
+  SRS_CUDA(cudaMemcpy(ryr.data(), s->d_ryr + (size_t)r * s->NR, s->NR * 4, cudaMemcpyDeviceToHost));
+  return write_grid_vtk(path, s->m, run, rank, n, t, &S6[0], &S6[(size_t)SP_DYE * s->N], ryr.data());
+}
+
+void srs_box_mesh_default(srs_box_mesh_spec* spec) {
+  MeshGenSpec s;
+  meshgen_default_spec(&s);
+  static_assert(sizeof(MeshGenSpec) == sizeof(srs_box_mesh_spec), "spec layouts differ");
+  std::memcpy(spec, &s, sizeof(s));
+}
+
+int srs_box_mesh_write(const srs_box_mesh_spec* spec, const char* base, int* rep_i, double* rep_a0) {
+  if (!spec || !base) return fail(SRS_ERR_INPUT, "null argument");
+  MeshGenSpec s;
+  std::memcpy(&s, spec, sizeof(s));
+  MeshGenReport rep;
+  int rc = meshgen_box(s, base, &rep);
+  if (rc) return fail(rc, "mesh generation failed");
+  if (rep_i) {
+    rep_i[0] = rep.n_tets;
+    rep_i[1] = rep.n_faces;
+    rep_i[2] = rep.n_nodes;
+    rep_i[3] = rep.n_ryr;
+    rep_i[4] = rep.n_lcc;
+    rep_i[5] = rep.n_jsr_tets;
+  }
+  if (rep_a0) *rep_a0 = rep.max_a0;
+  return SRS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// srs_engine.h — host-side declarations of the kernel launchers and the
+// argument blocks they take (definitions in k_plain64.cu and k_fp32.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "srs_sim.cuh"
+
+namespace srs {
+
+struct Plain64Args {
+  int32_t N, R;
+  const double* aij;
+  const int32_t* nij;
+  const double* br;
+  const double* v0;
+  const double* bhi;
+  const double* blo;
+  const int32_t* flags;
+  const int32_t* chan_ptr;
+  const ChanEntry* chan_list;
+  const double* S_in;
+  double* S_out;
+  double p[56];
+  double nsr;
+  Protocol P;
+  Channels C;
+  ChanState CS;
+  unsigned int* counters;
+};
+int launch_plain64_step(const Plain64Args& a, cudaStream_t st);
+int launch_plain64_prestep(const Plain64Args& a, int write_initial_row, cudaStream_t st);
+
+struct Consts32 {
+  float D[4];
+  float kon[5], koff[5], bfree[5];
+  float c0, c0j;
+  float inv_kdi;
+  float sd0, sd1, sd2;
+  float sn1, sn0;
+  float serca_scale;
+  float refill_v, refill0;
+  float khi;
+  float dt;
+  float jr_scale;
+  float dc0;
+  float lccA[2], lccE[2], lccB;
+};
+
+struct ChanEntry32 {
+  int32_t kind;
+  int32_t ch;
+  float s;
+  int32_t pad;
+};
+
+struct Plain32Args {
+  int32_t N, R;
+  const float4* a;
+  const int4* nb;
+  const float* bsl;
+  const float* kb;
+  const uint32_t* flags;
+  const int32_t* chan_ptr;
+  const ChanEntry32* chan_list;
+  const float* rest_ca;
+  const float4* M_in;
+  const float* I_in;
+  float4* M_out;
+  float* I_out;
+  Consts32 k;
+  Protocol P;
+  Channels C;
+  ChanState CS;
+  unsigned int* counters;
+};
+int launch_plain32_step(const Plain32Args& a, cudaStream_t st);
+int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStream_t st);
+
+struct __align__(16) TetRec {
+  float a[4];
+  uint16_t nb[4];
+  float bsl;
+  uint32_t flags;
+};
+
+struct ResidentArgs {
+  int32_t R;
+  int32_t P;
+  int32_t off_bits;
+  int32_t steps;
+  const TetRec* geo;
+  const int32_t* n_local;
+  const int32_t* n_chtet;
+  const int32_t* ch_ptr;
+  const ChanEntry32* ch_list;
+  int32_t ch_stride;
+  const uint16_t* ryr_cleft_code;
+  const uint16_t* ryr_jsr_code;
+  const uint16_t* lcc_code;
+  const float* lcc_rest;
+  float4* M;
+  float* I;
+  Consts32 k;
+  Protocol P_;
+  Channels C;
+  ChanState CS;
+};
+size_t resident_smem_bytes(int P, int NR, int NL);
+int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
+                    cudaStream_t st);
+int resident_max_clusters(int C, int threads, size_t smem);
+
+}  // namespace srs
