@@ -263,6 +263,10 @@ struct ResidentSmemTail {
   RealCtl ctl;
   uint32_t base[2][16];  // cluster addresses of buf[b] in CTA rank q
   int32_t bad;
+  // Termination flag published by warp 0 in iteration s into slot s & 1 and
+  // read by every thread after that iteration's barrier.  Two slots, so a
+  // slow warp still reading slot s & 1 never sees warp 0's write for s + 1.
+  int32_t done_flag[2];
 };
 
 // Deviation u of the element with code `code` in the current buffer.
@@ -414,7 +418,10 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
       buf0[i] = Mg[i];
       imm0[i] = Ig[i];
     }
-    if (tid == 0) tail->ctl = a.CS.ctl[r];
+    if (tid == 0) {
+      tail->ctl = a.CS.ctl[r];
+      tail->done_flag[1] = tail->ctl.done;
+    }
     for (int i = tid; i < NR; i += nthr) s_ryr[i] = a.CS.ryr[(size_t)r * NR + i];
     for (int i = tid; i < NL; i += nthr) {
       s_lcc[i] = a.CS.lcc[(size_t)r * NL + i];
@@ -422,7 +429,7 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
     }
     for (int i = tid; i < NCH; i += nthr) s_res[i] = a.CS.res[(size_t)r * NCH + i];
     step_barrier<C>();
-    const bool skip = tail->ctl.done != 0;
+    const bool skip = tail->done_flag[1] != 0;
     int cur = 0;
     if (!skip) {
       for (int s = 0; s < a.steps; ++s) {
@@ -458,6 +465,7 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
               ctl.n_rows = nr;
               ctl.status = st;
             }
+            tail->done_flag[s & 1] = ctl.done;
           }
           __syncwarp();
           if (!ctl.done) {
@@ -535,7 +543,7 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
           }
         }
         step_barrier<C>();
-        if (tail->ctl.done) break;
+        if (tail->done_flag[s & 1]) break;
         cur ^= 1;
       }
       if (!tail->ctl.done && warp == 0) {

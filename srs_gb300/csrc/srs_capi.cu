@@ -1073,8 +1073,9 @@ int srs_sim_reset(srs_sim* s) {
   std::vector<int32_t> ryr((size_t)s->R * NR, 0), lcc((size_t)s->R * NL, 1), lccv((size_t)s->R * NL, 2);
   std::vector<double> res((size_t)s->R * NCH);
   std::vector<RealCtl> ctl(s->R);
-  if (I[I_INIT_RYR] != -1 && !I[I_FLAG_LCC] && !I[I_FLAG_V_CLAMP] &&
-      (I[I_INIT_RYR] < 0 || I[I_INIT_RYR] >= NR))
+  // The RyR hold of RunSimulation indexes RyR_States[INIT_RYR] under every
+  // protocol (cpu/RunSimulation.cpp:540), so the index is checked always.
+  if (I[I_INIT_RYR] != -1 && (I[I_INIT_RYR] < 0 || I[I_INIT_RYR] >= NR))
     return fail(SRS_ERR_INPUT, "Invalid initial RyR index (" + std::to_string(I[I_INIT_RYR]) +
                                    "), must be -1 to ignore, or between 0 and the number of RyRs");
   if (I[I_FLAG_LCC] && (I[I_LCC_INDEX] < 0 || I[I_LCC_INDEX] >= NL))

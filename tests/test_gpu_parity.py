@@ -1,0 +1,194 @@
+"""GPU parity: every engine against the oracle, through the C ABI.
+
+Bars:
+  * FP64 plain engine: bit-exact with the oracle (PHILOX gating), and with the
+    reference's own golden rows where no random numbers are involved;
+  * FP32 resident engine: bit-exact with the FP32 plain engine (same per-element
+    arithmetic), for every cluster size;
+  * FP32 engines vs FP64: relative error <= 1e-5 on concentrations
+    (|c32 - c64| / max(|c64|, 1e-3 uM)) over the deterministic part.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GOLDEN_MESH, params_from_golden
+
+pytestmark = pytest.mark.gpu
+TOL32 = 1e-5
+
+
+def rel_err(a, b, floor=1e-3):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+def golden_params(srs, name="spark"):
+    p, _ = params_from_golden(srs, name)
+    return p
+
+
+def oracle_mesh(oracle, p, base=GOLDEN_MESH):
+    from oracle import Mesh
+    return Mesh(oracle, base, p.ints[9], np.array(p.reals[:]))
+
+
+def test_fp64_steps_bit_exact_with_oracle(srs, oracle):
+    p = golden_params(srs)
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [11, 12, 13]
+    sim = srs.Simulation(g, p, len(seeds), srs.FP64, srs.ENGINE_PLAIN, seeds=seeds)
+    st0 = [sim.get_state(r) for r in range(len(seeds))]
+    n = 600
+    sim.explicit_step(n)
+    m = oracle_mesh(oracle, p)
+    for r, sd in enumerate(seeds):
+        s0 = st0[r]
+        S, ryr, lcc, lccv, res = (s0["states"].copy(), s0["ryr"].copy(), s0["lcc"].copy(),
+                                  s0["lccv"].copy(), s0["residuals"].copy())
+        m.steps_philox(S, sd, 0, n, ryr, lcc, lccv, res)
+        got = sim.get_state(r)
+        assert np.array_equal(got["states"], S)
+        assert np.array_equal(got["ryr"], ryr)
+        assert np.array_equal(got["lcc"], lcc) and np.array_equal(got["lccv"], lccv)
+        assert np.array_equal(got["residuals"], res)
+
+
+def test_fp64_reset_matches_oracle(srs, oracle):
+    for name in ["spark", "lcc_trigger", "gain_clamp"]:
+        p = golden_params(srs, name)
+        g = srs.Grid(p, GOLDEN_MESH)
+        sim = srs.Simulation(g, p, 2, srs.FP64, srs.ENGINE_PLAIN, seeds=[5, 6])
+        m = oracle_mesh(oracle, p)
+        for r, sd in enumerate([5, 6]):
+            want = m.reset_philox(np.array(p.ints[:]), sd)
+            got = sim.get_state(r)
+            for k in ("states", "ryr", "lcc", "lccv", "residuals"):
+                assert np.array_equal(got[k], want[k]), (name, k)
+
+
+def test_fp64_random_initial_ryr_matches_oracle(srs, oracle):
+    p = golden_params(srs).set(INIT_RYR=-1)
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = list(range(1, 9))
+    sim = srs.Simulation(g, p, len(seeds), srs.FP64, srs.ENGINE_PLAIN, seeds=seeds)
+    m = oracle_mesh(oracle, p)
+    for r, sd in enumerate(seeds):
+        want = m.reset_philox(np.array(p.ints[:]), sd)
+        assert np.array_equal(sim.get_state(r)["ryr"], want["ryr"])
+
+
+@pytest.mark.parametrize("name", ["spark", "spark_nogating", "lcc_trigger", "gain_clamp",
+                                  "fidelity"])
+def test_fp64_run_simulation_bit_exact_with_oracle(srs, oracle, name):
+    from oracle import RNG_PHILOX
+    p = golden_params(srs, name)
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [21, 22]
+    sim = srs.Simulation(g, p, len(seeds), srs.FP64, srs.ENGINE_PLAIN, seeds=seeds)
+    rows, t_end, n_steps = sim.run_simulation()
+    m = oracle_mesh(oracle, p)
+    for r, sd in enumerate(seeds):
+        want_rows, want_S, want_t, want_n = m.run_simulation(np.array(p.ints[:]), RNG_PHILOX, sd)
+        assert rows[r].shape == want_rows.shape, name
+        assert np.array_equal(rows[r], want_rows), name
+        assert np.array_equal(sim.get_state(r)["states"], want_S), name
+        assert t_end[r] == want_t and n_steps[r] == want_n
+
+
+def test_fp64_deterministic_run_equals_reference_golden(srs):
+    """No random numbers enter a run without gating and with a named initial
+    RyR, so the GPU FP64 rows equal the reference's own rows bit for bit."""
+    p, d = params_from_golden(srs, "spark_nogating")
+    g = srs.Grid(p, GOLDEN_MESH)
+    sim = srs.Simulation(g, p, 1, srs.FP64, srs.ENGINE_PLAIN, seeds=[3])
+    rows, _, _ = sim.run_simulation()
+    assert np.array_equal(rows[0], d["rows"])
+    assert np.array_equal(sim.get_state(0)["states"], d["states"])
+
+
+def test_fp32_plain_within_tolerance_of_fp64(srs):
+    p = golden_params(srs, "spark_nogating")
+    g = srs.Grid(p, GOLDEN_MESH)
+    s64 = srs.Simulation(g, p, 1, srs.FP64, srs.ENGINE_PLAIN)
+    s32 = srs.Simulation(g, p, 1, srs.FP32, srs.ENGINE_PLAIN)
+    for s in (s64, s32):
+        s.explicit_step(4000)
+    e = rel_err(s32.get_state(0)["states"], s64.get_state(0)["states"])
+    assert e <= TOL32, e
+
+
+@pytest.mark.parametrize("cluster", [1, 2, 4])
+def test_fp32_resident_bit_exact_with_plain(srs, cluster):
+    p = golden_params(srs)
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [31, 32, 33, 34, 35]
+    pl = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    rs = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                        cluster_size=cluster, steps_per_launch=97)
+    assert rs.config()["cluster_size"] == cluster
+    pl.explicit_step(1000)
+    rs.explicit_step(1000)
+    for r in range(len(seeds)):
+        a, b = pl.get_state(r), rs.get_state(r)
+        for k in ("states", "ryr", "lcc", "lccv", "residuals"):
+            assert np.array_equal(a[k], b[k]), (cluster, r, k)
+
+
+def test_fp32_resident_run_simulation_matches_plain(srs):
+    p = golden_params(srs, "fidelity")
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [41, 42, 43]
+    pl = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    rs = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                        cluster_size=2, steps_per_launch=500)
+    ra, ta, na = pl.run_simulation()
+    rb, tb, nb = rs.run_simulation()
+    for r in range(len(seeds)):
+        assert ra[r].shape == rb[r].shape
+        assert np.array_equal(ra[r], rb[r])
+        assert ta[r] == tb[r] and na[r] == nb[r]
+        assert np.array_equal(pl.get_state(r)["states"], rs.get_state(r)["states"])
+
+
+def test_resident_on_config_mesh_matches_plain(srs, box_mesh):
+    base, _ = box_mesh
+    p = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24,
+                                     INIT_RYR_HOLD=10.0)
+    g = srs.Grid(p, base)
+    seeds = list(range(1, 5))
+    pl = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    rs = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds)
+    cfg = rs.config()
+    assert cfg["cluster_size"] >= 2  # 10,368 elements do not fit one CTA's shared memory
+    pl.explicit_step(600)
+    rs.explicit_step(600)
+    for r in range(len(seeds)):
+        assert np.array_equal(pl.get_state(r)["states"], rs.get_state(r)["states"])
+
+
+def test_fp32_resident_error_vs_fp64_on_config_mesh(srs, box_mesh):
+    base, _ = box_mesh
+    p = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24,
+                                     FLAG_NO_GATING=1)
+    g = srs.Grid(p, base)
+    s64 = srs.Simulation(g, p, 1, srs.FP64, srs.ENGINE_PLAIN)
+    s32 = srs.Simulation(g, p, 2, srs.FP32, srs.ENGINE_RESIDENT)
+    s64.explicit_step(3000)
+    s32.explicit_step(3000)
+    e = rel_err(s32.get_state(0)["states"], s64.get_state(0)["states"])
+    assert e <= TOL32, e
+
+
+def test_nonfinite_state_is_reported(srs):
+    p = golden_params(srs, "spark_nogating")
+    g = srs.Grid(p, GOLDEN_MESH)
+    for eng, prec in ((srs.ENGINE_PLAIN, srs.FP64), (srs.ENGINE_PLAIN, srs.FP32),
+                      (srs.ENGINE_RESIDENT, srs.FP32)):
+        sim = srs.Simulation(g, p, 1, prec, eng)
+        st = sim.get_state(0)
+        S = st["states"].copy()
+        S[7] = np.nan  # a planted bad value (host side): arithmetic only, no fault
+        sim.set_state(0, S)
+        sim.explicit_step(4)
+        assert sim.status() & 1, (eng, prec)
