@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Throughput of the batched spark timestep on GB300.
+
+Workload (config 1): the 10,368-element box dyad (12^3 hexahedra, 49 RyRs,
+7 LCCs), DefaultSpark parameters at dt = 9 ns, 1024 independent
+realizations (Philox seeds 1..1024) with FP32 state, run by the resident
+persistent engine.  One bench step = one persistent launch that advances all
+realizations by --launch-steps time steps.
+
+Metric: simulated spark-ms per wall second (sum over realizations).
+  value      device-resident: CUDA events on the engine's stream around K
+             launches, state already in HBM (1024 x 10,368 x 20 B = 212 MB,
+             larger than the 129 MB L2, so no flush is needed).
+  e2e        through the public API with host buffers: srs_sim_reset
+             (initial state uploaded from pinned host memory) +
+             srs_run_simulation (RunSimulation protocol, states rows read
+             back) for --launch-steps steps, per bench step.
+  roofline   algorithmic bytes of the dominant kernel per launch =
+             elements x realizations x steps x (48 + 44/R) B (FP32 state
+             read+write of 6 species-slots and shared geometry), divided by
+             the measured launch time, against the measured HBM copy peak.
+             Values above 1 are "effective": the engine keeps each
+             realization on chip for a whole launch.
+  cpu_baseline  the oracle port (RunSimulation of the reference, restated in
+             C) on the host cores, one realization per process.
+
+--impl reference times the reference's CPU implementation (oracle/_ref when
+it was built from the reference sources, else the oracle port) on the host
+cores for the same metric.
+
+Multi-GPU (torchrun, N > 1): replicas only — each rank runs its own 1024
+realizations (seeds offset by rank); no collective on the data path; timing
+is max over ranks.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DT_MS = 9e-6
+METRIC = "simulated spark-ms/s (batched 1024-realization dyad, config 1)"
+UNIT = "spark-ms/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--realizations", type=int, default=1024)
+    ap.add_argument("--launch-steps", type=int, default=2000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(prefix="srs_clocks_", suffix=".csv")
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1].split()[0]))
+                smax.append(float(t[2].split()[0]))
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch of the resident kernel from the committed ncu
+    summary (profiles/k_resident32_config1.md, line 'dram_bytes_per_launch:')."""
+    p = os.path.join(ROOT, "profiles", "k_resident32_config1.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    """One realization of RunSimulation (oracle port, reference gating) for
+    n steps on the config mesh; returns the wall seconds of the time loop."""
+    base, ints, reals, n_steps, rank = args
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    from oracle import Oracle, Mesh, RNG_REFERENCE, Reference
+    reals = np.array(reals)
+    reals[0] = (n_steps - 0.5) * reals[1]  # t_final: n_steps steps
+    m = Mesh(Oracle(), base, 1, reals)
+    t0 = time.perf_counter()
+    m.run_simulation(np.array(ints), RNG_REFERENCE, rank, 0)
+    return time.perf_counter() - t0
+
+
+def _ref_worker(args):
+    """Same sample through the reference's own RunSimulation (oracle/_ref)."""
+    base, ints, reals, n_steps, rank = args
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    from oracle import Oracle, Mesh, Reference
+    reals = np.array(reals)
+    reals[0] = (n_steps - 0.5) * reals[1]
+    m = Mesh(Oracle(), base, 1, reals)
+    ref = Reference()
+    t0 = time.perf_counter()
+    ref.run_simulation(m, np.array(ints), rank=rank)
+    return time.perf_counter() - t0
+
+
+def reference_available():
+    return os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libsrsref.so"))
+
+
+def cpu_sample(base, params, seconds, cores=None, prefer_reference=False):
+    """Times RunSimulation on `cores` processes; returns (spark-ms/s, cores, kind, sample)."""
+    import numpy as np
+    cores = cores or os.cpu_count() or 1
+    ints = list(params.ints)
+    reals = list(params.reals)
+    # calibrate: ~31M element-steps/s per core -> steps for the requested seconds
+    kind = "reference" if (prefer_reference and reference_available()) else "port"
+    worker = _ref_worker if kind == "reference" else _cpu_worker
+    probe = worker((base, ints, reals, 200, 0))
+    n_steps = max(200, int(200 * seconds / max(probe, 1e-3)))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        loops = pool.map(worker, [(base, ints, reals, n_steps, r) for r in range(cores)])
+        wall = time.perf_counter() - t0
+    # metric over the time loops (setup excluded like the reference's clock())
+    span = max(loops)
+    value = cores * n_steps * DT_MS / span
+    sample = ("%d processes x 1 realization x %d steps (%.3g ms simulated each) of the config-1 "
+              "mesh, RunSimulation with reference gating; loop time %.1f s, wall %.1f s"
+              % (cores, n_steps, n_steps * DT_MS, span, wall))
+    return value, cores, kind, sample
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as g
+    g.build()
+    import srs_gb300 as srs
+    from srs_gb300 import workloads as wl
+    tmp = tempfile.mkdtemp(prefix="srs_bench_")
+    base, rep = wl.config_mesh(tmp)
+    p = wl.default_spark_params()
+    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, cores, kind, sample = cpu_sample(base, p, per_step, prefer_reference=True)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "config1 box dyad 10,368 elements, DefaultSpark dt=9ns, "
+                               "one realization per host core", "realizations_per_step": cores},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    dist = dist_init(ws)
+    import torch
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    if rank == 0:
+        g.build()
+    barrier(dist)
+    import srs_gb300 as srs
+    from srs_gb300 import workloads as wl
+    tmp = tempfile.mkdtemp(prefix="srs_bench_%d_" % rank)
+    base, rep = wl.config_mesh(tmp)
+    p = wl.default_spark_params()
+    grid = srs.Grid(p, base)
+    R, S = args.realizations, args.launch_steps
+    seeds = [1 + rank * R + i for i in range(R)]
+    sim = srs.Simulation(grid, p, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                         steps_per_launch=S)
+    cfg = sim.config()
+    # warm-up launches
+    for _ in range(args.warmup):
+        sim.advance_async(S)
+    sim.synchronize()
+    clocks = Clocks(local)
+    launches0 = sim.config()["kernel_launches"]
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    ms = sim.time_advance(args.steps * S)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    launches = sim.config()["kernel_launches"] - launches0
+    if sim.status() & 1:
+        raise SystemExit("non-finite state during the timed region")
+    ms_max = max_over_ranks(dist, ms)
+    sec = ms_max / 1e3
+    value = ws * R * args.steps * S * DT_MS / sec
+    ms_per_step = ms_max / args.steps
+
+    # roofline of the resident kernel (the only kernel in the timed region)
+    n_el = rep["n_tets"]
+    alg_bytes = n_el * R * S * (48.0 + 44.0 / R)
+    achieved = alg_bytes / (ms / args.steps / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "note": "effective fraction (state resident on chip within a launch); peak %s"
+                    % peak_kind}
+
+    # end to end through the public API with host buffers
+    pe = wl.default_spark_params(T_FINAL=(S - 0.5) * DT_MS, OUTPUT_STATES_INTERVAL=S * DT_MS / 4)
+    sim_e = srs.Simulation(grid, pe, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                           steps_per_launch=S)
+    cfg_e = sim_e.config()
+    sim_e.run_simulation()  # warm
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rows_bytes = 0
+    for _ in range(args.e2e_steps):
+        sim_e.reset()
+        rows, t_end, n_steps = sim_e.run_simulation()
+        rows_bytes = sum(r.nbytes for r in rows)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.e2e_steps)
+    e2e_val = ws * R * S * DT_MS / e2e_s
+    row_cap = int(pe.reals[0] / pe.reals[2]) + 8
+    d2h = R * row_cap * sim_e.row_width() * 4 + 2 * cfg_e["ctl_bytes"]
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        v, cores, kind, sample = cpu_sample(base, p, args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {
+                "workload": "config1: batched box dyad, %d realizations x %d elements "
+                            "(12^3 hexahedra, 49 RyR, 7 LCC), DefaultSpark dt=9ns, FP32 state"
+                            % (R, n_el),
+                "realizations_per_gpu": R, "elements": n_el, "steps_per_launch": S,
+                "engine": "resident", "cluster_size": cfg["cluster_size"],
+                "threads_per_cta": cfg["threads_per_cta"], "smem_bytes": cfg["smem_bytes"],
+                "l2": "inputs larger than L2 (212 MB state), no flush",
+                "parallelism": "replicas x%d" % ws},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": cfg_e["reset_h2d_bytes"],
+                    "d2h_bytes_per_step": d2h,
+                    "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)"
+                            % (S, rows_bytes)},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

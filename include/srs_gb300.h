@@ -164,6 +164,9 @@ typedef struct srs_sim_config {
   int engine, precision, threads_per_cta, cluster_size, steps_per_launch;
   int smem_bytes;
   int64_t kernel_launches;
+  int64_t reset_h2d_bytes;  /* host->device bytes of one srs_sim_reset */
+  int64_t ctl_bytes;        /* bytes of the per-realization control blocks */
+  int64_t engine_elements;  /* element slots per realization in the engine layout */
 } srs_sim_config;
 int srs_sim_get_config(const srs_sim* s, srs_sim_config* c);
 

@@ -57,6 +57,10 @@ class Oracle:
         L.or_run_simulation.argtypes = [vp, vp, vp, C.c_int, C.c_uint64, C.c_int, vp, C.c_int64,
                                         C.c_int, vp, vp, vp]
         L.or_run_simulation.restype = C.c_int64
+        L.or_fp32_to_dev.argtypes = [vp, vp, vp, vp, vp]
+        L.or_fp32_from_dev.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.or_steps_fp32.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_int64, C.c_int64, vp,
+                                    vp, vp, vp, C.c_int]
         L.or_logf.argtypes = [C.c_float]
         L.or_logf.restype = C.c_float
         L.or_exp2f.argtypes = [C.c_float]
@@ -121,6 +125,26 @@ class Mesh:
         g = _f64(globals_ if globals_ is not None else [self.reals[15], self.reals[16]])
         self.o.lib.or_steps_philox(self.h, _p(self.reals), _p(g), _p(S), C.c_uint64(seed), step0, n,
                                    _p(ryr), _p(lcc), _p(lccv), _p(res))
+
+    def to_fp32(self, S):
+        """Deviation-form FP32 state (U: 4N mobile, Im: N immobile) and zero
+        compensation terms (CM, CI)."""
+        U = np.zeros(4 * self.N, np.float32)
+        Im = np.zeros(self.N, np.float32)
+        self.o.lib.or_fp32_to_dev(self.h, _p(self.reals), _p(_f64(S)), _p(U), _p(Im))
+        return dict(U=U, Im=Im, CM=np.zeros(4 * self.N, np.float32), CI=np.zeros(self.N, np.float32))
+
+    def from_fp32(self, st):
+        S = np.zeros(6 * self.N)
+        self.o.lib.or_fp32_from_dev(self.h, _p(self.reals), _p(st["U"]), _p(st["Im"]), _p(st["CM"]),
+                                    _p(st["CI"]), _p(S))
+        return S
+
+    def steps_fp32(self, st, seed, step0, n, ryr, lcc, lccv, res, gating=True, globals_=None):
+        g = _f64(globals_ if globals_ is not None else [self.reals[15], self.reals[16]])
+        self.o.lib.or_steps_fp32(self.h, _p(self.reals), _p(g), _p(st["U"]), _p(st["Im"]), _p(st["CM"]),
+                                 _p(st["CI"]), C.c_uint64(seed), step0, n, _p(ryr), _p(lcc), _p(lccv),
+                                 _p(res), int(gating))
 
     def gating_philox(self, V, ca, seed, step, ryr, lcc, lccv, res):
         self.o.lib.or_gating_philox(self.h, _p(self.reals), float(V), _p(_f64(ca)), C.c_uint64(seed),

@@ -49,6 +49,7 @@ struct or_mesh {
   double* aij;
   int* nij;
   double* br;
+  double* scratch; /* States_Buffer of cpu/parameters.h:165 (6N) */
 };
 
 static void skipline(FILE* f) {
@@ -337,6 +338,7 @@ void or_mesh_free(or_mesh* m) {
   free(m->aij);
   free(m->nij);
   free(m->br);
+  free(m->scratch);
   free(m);
 }
 
@@ -407,8 +409,10 @@ void or_initial_states(const or_mesh* m, const double* R, double* S) {
 void or_explicit_step(const or_mesh* m, const double* R, const double* G, double* S, const int* ryr,
                       const int* lcc, const int* lccv) {
   int N = m->N, j, i;
-  double* buf = malloc(sizeof(double) * 6 * N);
+  double* buf;
   const double* gca = S + S_CA * N;
+  if (!m->scratch) ((or_mesh*)m)->scratch = malloc(sizeof(double) * 6 * N);
+  buf = m->scratch;
   /* UpdateReactionTerms (:25-125) */
   for (j = 0; j < N; ++j) {
     double c_ca = S[S_CA * N + j], r_net, c_b;
@@ -504,7 +508,6 @@ void or_explicit_step(const or_mesh* m, const double* R, const double* G, double
     for (i = 0; i < 6; ++i)
       for (j = 0; j < N; ++j) S[i * N + j] += buf[i * N + j] * dt;
   }
-  free(buf);
 }
 
 /* ---- reference-mode gating (cpu/RunSimulation.cpp:166-400) -------------- */
@@ -1022,4 +1025,248 @@ int64_t or_run_simulation(const or_mesh* m, const int* I, const double* R, int m
   free(lccv);
   free(res);
   return nrows;
+}
+
+
+/* ---- FP32 engine restated (deviation form, see k_fp32.cu's tet_update) ----
+ * The GPU's FP32 engines store u = c - c_rest and evaluate each element's
+ * update with the operation order below (every fused multiply-add explicit).
+ * This restatement is the bit-exact CPU model of those engines. */
+typedef struct {
+  float D[4], kon[5], koff[5], bfree[5], c0, c0j, inv_kdi, sd0, sd1, sd2, sn1, sn0, serca_scale,
+      refill_v, refill0, khi, dt, jr_scale, dc0, lccA, lccE, lccB;
+  double rest_atp, rest_cmdn, rest_dye, rest_trpn, rest_csqn, rest_ca, rest_caj;
+} or_k32;
+
+static void make_k32(const double* R, double V, double nsr, or_k32* k) {
+  double ca0 = R[OR_C_0_CA], ca0j = R[OR_C_0_CA_JSR], Kd, Ksr;
+  double P_CaL = (9.13e-13) * (1e12) * (1e-3), F_over_RT = 96.5 / (310 * 8.314), A, E, Em1;
+  const int ion[5] = {OR_K_ON_DYE, OR_K_ON_ATP, OR_K_ON_CMDN, OR_K_ON_TRPN, OR_K_ON_CSQN};
+  const int ioff[5] = {OR_K_OFF_DYE, OR_K_OFF_ATP, OR_K_OFF_CMDN, OR_K_OFF_TRPN, OR_K_OFF_CSQN};
+  double btot[5], brest[5];
+  int q;
+  Kd = R[OR_K_OFF_TRPN] / R[OR_K_ON_TRPN];
+  k->rest_trpn = ca0 * R[OR_B_TOT_TRPN] / (Kd + ca0);
+  Kd = R[OR_K_OFF_CSQN] / R[OR_K_ON_CSQN];
+  k->rest_csqn = ca0j * R[OR_B_T_JSR] / (Kd + ca0j);
+  Kd = R[OR_K_OFF_ATP] / R[OR_K_ON_ATP];
+  k->rest_atp = ca0 * R[OR_B_TOT_ATP] / (Kd + ca0);
+  Kd = R[OR_K_OFF_CMDN] / R[OR_K_ON_CMDN];
+  k->rest_cmdn = ca0 * R[OR_B_TOT_CMDN] / (Kd + ca0);
+  Kd = R[OR_K_OFF_DYE] / R[OR_K_ON_DYE];
+  k->rest_dye = ca0 * R[OR_B_TOT_DYE] / (Kd + ca0);
+  k->rest_ca = ca0;
+  k->rest_caj = ca0j;
+  btot[0] = R[OR_B_TOT_DYE];
+  btot[1] = R[OR_B_TOT_ATP];
+  btot[2] = R[OR_B_TOT_CMDN];
+  btot[3] = R[OR_B_TOT_TRPN];
+  btot[4] = R[OR_B_T_JSR];
+  brest[0] = k->rest_dye;
+  brest[1] = k->rest_atp;
+  brest[2] = k->rest_cmdn;
+  brest[3] = k->rest_trpn;
+  brest[4] = k->rest_csqn;
+  k->D[0] = (float)R[OR_D_CA];
+  k->D[1] = (float)R[OR_D_ATP];
+  k->D[2] = (float)R[OR_D_CMDN];
+  k->D[3] = (float)R[OR_D_DYE];
+  for (q = 0; q < 5; ++q) {
+    k->kon[q] = (float)R[ion[q]];
+    k->koff[q] = (float)R[ioff[q]];
+    k->bfree[q] = (float)(btot[q] - brest[q]);
+  }
+  k->c0 = (float)ca0;
+  k->c0j = (float)ca0j;
+  k->inv_kdi = (float)(1.0 / R[OR_K_D_i]);
+  Ksr = nsr / R[OR_K_D_SR];
+  Ksr = Ksr * Ksr;
+  k->sd0 = (float)(0.104217 + 17.923 * Ksr);
+  k->sd1 = (float)(1.75583e6 + Ksr * 7.61673e6);
+  k->sd2 = (float)(6.08463e11 + Ksr * 4.50544e11);
+  k->sn1 = (float)(9.17846e6 - 11478.2 * Ksr);
+  k->sn0 = (float)(0.329904 * Ksr);
+  k->serca_scale = (float)(2e-3 * R[OR_A_P]);
+  k->refill_v = (float)R[OR_V_REFILL];
+  k->refill0 = (float)((nsr - ca0j) * R[OR_V_REFILL]);
+  k->khi = (float)R[OR_K_D_SL_HI];
+  k->dt = (float)R[OR_T_STEP];
+  k->jr_scale = (float)(R[OR_V_RYR] * R[OR_V_CELL]);
+  k->dc0 = (float)(ca0j - ca0);
+  if (fabs(V) < 1e-6) V = 1e-6;
+  A = -P_CaL * V * (2 * F_over_RT);
+  E = exp(2 * V * F_over_RT);
+  Em1 = exp(2 * V * F_over_RT) - 1;
+  k->lccA = (float)(A / Em1);
+  k->lccE = (float)E;
+  k->lccB = (float)(0.34 * R[OR_CA_0]);
+}
+
+/* absolute (6N doubles, reference numbering) <-> deviation (4N + N floats) */
+void or_fp32_to_dev(const or_mesh* m, const double* R, const double* S, float* U, float* Im) {
+  or_k32 k;
+  int N = m->N, j;
+  make_k32(R, R[OR_DEFAULT_VM], R[OR_DEFAULT_CA_NSR], &k);
+  for (j = 0; j < N; ++j) {
+    int jsr = m->domain[j] == 1;
+    U[4 * j + 0] = (float)(S[S_CA * N + j] - (jsr ? k.rest_caj : k.rest_ca));
+    U[4 * j + 1] = (float)(S[S_ATP * N + j] - (jsr ? 0.0 : k.rest_atp));
+    U[4 * j + 2] = (float)(S[S_CMDN * N + j] - (jsr ? 0.0 : k.rest_cmdn));
+    U[4 * j + 3] = (float)(S[S_DYE * N + j] - (jsr ? 0.0 : k.rest_dye));
+    Im[j] = jsr ? (float)(S[S_CSQN * N + j] - k.rest_csqn)
+                : (float)(S[S_TRPN * N + j] - (m->tropc[j] ? k.rest_trpn : 0.0));
+  }
+}
+void or_fp32_from_dev(const or_mesh* m, const double* R, const float* U, const float* Im, const float* CM,
+                      const float* CI, double* S) {
+  or_k32 k;
+  int N = m->N, j;
+  make_k32(R, R[OR_DEFAULT_VM], R[OR_DEFAULT_CA_NSR], &k);
+  for (j = 0; j < N; ++j) {
+    int jsr = m->domain[j] == 1;
+    S[S_CA * N + j] = (jsr ? k.rest_caj : k.rest_ca) + ((double)U[4 * j] - (double)CM[4 * j]);
+    S[S_ATP * N + j] = (jsr ? 0.0 : k.rest_atp) + ((double)U[4 * j + 1] - (double)CM[4 * j + 1]);
+    S[S_CMDN * N + j] = (jsr ? 0.0 : k.rest_cmdn) + ((double)U[4 * j + 2] - (double)CM[4 * j + 2]);
+    S[S_DYE * N + j] = (jsr ? 0.0 : k.rest_dye) + ((double)U[4 * j + 3] - (double)CM[4 * j + 3]);
+    if (jsr) {
+      S[S_CSQN * N + j] = k.rest_csqn + ((double)Im[j] - (double)CI[j]);
+      S[S_TRPN * N + j] = 0.0;
+    } else {
+      S[S_TRPN * N + j] = (m->tropc[j] ? k.rest_trpn : 0.0) + ((double)Im[j] - (double)CI[j]);
+      S[S_CSQN * N + j] = 0.0;
+    }
+  }
+}
+
+static void fp32_element(const or_k32* k, const float* o, float im, const float* s1, const float* s2,
+                         const float* s3, const float* s4, const float* a, int jsr, int tropc, float bsl,
+                         float flux, float* cm, float* ci, float* out, float* im_out) {
+  float dx = a[0] * (s1[0] - o[0]), dy = a[0] * (s1[1] - o[1]), dz = a[0] * (s1[2] - o[2]),
+        dw = a[0] * (s1[3] - o[3]);
+  float rca, ratp, rcmdn, rdye, rim = 0.0f, u = o[0], c, rb;
+  dx = fmaf(a[1], s2[0] - o[0], dx);
+  dx = fmaf(a[2], s3[0] - o[0], dx);
+  dx = fmaf(a[3], s4[0] - o[0], dx);
+  dy = fmaf(a[1], s2[1] - o[1], dy);
+  dy = fmaf(a[2], s3[1] - o[1], dy);
+  dy = fmaf(a[3], s4[1] - o[1], dy);
+  dz = fmaf(a[1], s2[2] - o[2], dz);
+  dz = fmaf(a[2], s3[2] - o[2], dz);
+  dz = fmaf(a[3], s4[2] - o[2], dz);
+  dw = fmaf(a[1], s2[3] - o[3], dw);
+  dw = fmaf(a[2], s3[3] - o[3], dw);
+  dw = fmaf(a[3], s4[3] - o[3], dw);
+  rca = k->D[0] * dx;
+  ratp = k->D[1] * dy;
+  rcmdn = k->D[2] * dz;
+  rdye = k->D[3] * dw;
+  if (!jsr) {
+    c = k->c0 + u;
+    if (tropc) {
+      float Ki, Ki2, den, num;
+      rb = fmaf(k->kon[3], fmaf(k->bfree[3], u, -im * c), -k->koff[3] * im);
+      rca -= rb;
+      rim = rb;
+      Ki = c * k->inv_kdi;
+      Ki = Ki * Ki;
+      Ki2 = Ki * Ki;
+      den = fmaf(Ki2, k->sd2, fmaf(Ki, k->sd1, k->sd0));
+      num = fmaf(Ki2, 3.24873e12f, fmaf(Ki, k->sn1, -k->sn0));
+      rca = fmaf(-k->serca_scale, num / den, rca);
+    }
+    rb = fmaf(k->kon[0], fmaf(k->bfree[0], u, -o[3] * c), -k->koff[0] * o[3]);
+    rca -= rb;
+    rdye += rb;
+    rb = fmaf(k->kon[1], fmaf(k->bfree[1], u, -o[1] * c), -k->koff[1] * o[1]);
+    rca -= rb;
+    ratp += rb;
+    rb = fmaf(k->kon[2], fmaf(k->bfree[2], u, -o[2] * c), -k->koff[2] * o[2]);
+    rca -= rb;
+    rcmdn += rb;
+  } else {
+    c = k->c0j + u;
+    rb = fmaf(k->kon[4], fmaf(k->bfree[4], u, -im * c), -k->koff[4] * im);
+    rca -= rb;
+    rim = rb;
+    rca += fmaf(-u, k->refill_v, k->refill0);
+  }
+  rca += flux;
+  if (bsl != 0.0f) {
+    float kc = k->khi + c;
+    rca = rca / fmaf(bsl, 1.0f / (kc * kc), 1.0f);
+  }
+  /* compensated (Kahan) Euler update: y = dt*r - comp; t = u + y;
+   * comp = (t - u) - y */
+  {
+    float r4[4] = {rca, ratp, rcmdn, rdye}, y, t;
+    int q;
+    for (q = 0; q < 4; ++q) {
+      y = fmaf(k->dt, r4[q], -cm[q]);
+      t = o[q] + y;
+      cm[q] = (t - o[q]) - y;
+      out[q] = t;
+    }
+    y = fmaf(k->dt, rim, -*ci);
+    t = im + y;
+    *ci = (t - im) - y;
+    *im_out = t;
+  }
+}
+
+/* n FP32 steps (+ PHILOX gating on float Ca when `gating`), reference numbering. */
+void or_steps_fp32(const or_mesh* m, const double* R, const double* G, float* U, float* Im, float* CM,
+                   float* CI, uint64_t seed, int64_t step0, int64_t n, int* ryr, int* lcc, int* lccv,
+                   double* res, int gating) {
+  int N = m->N, j, q, i;
+  or_k32 k;
+  float* U2 = malloc(sizeof(float) * 4 * N);
+  float* I2 = malloc(sizeof(float) * N);
+  float* a = malloc(sizeof(float) * 4 * N);
+  float* bsl = malloc(sizeof(float) * N);
+  float* rest = malloc(sizeof(float) * N);
+  double* ca = malloc(sizeof(double) * N);
+  int64_t s;
+  make_k32(R, G[0], G[1], &k);
+  for (j = 0; j < N; ++j) {
+    double bhi = m->TT[j] * R[OR_B_TOT_SL_HI] / (m->V0[j] * (1e-15));
+    for (q = 0; q < 4; ++q) a[4 * j + q] = (float)m->aij[5 * j + 1 + q];
+    bsl[j] = (float)(bhi * R[OR_K_D_SL_HI]);
+    rest[j] = m->domain[j] == 1 ? k.c0j : k.c0;
+  }
+  for (s = 0; s < n; ++s) {
+    for (j = 0; j < N; ++j) {
+      float flux = 0.0f;
+      const int* nb = &m->nij[4 * j];
+      for (i = 0; i < m->NR; ++i) {
+        if (m->ryr_ele[i] == j && ryr[i]) {
+          float dc = (k.dc0 + U[4 * m->ryr_jsr[i]]) - U[4 * m->ryr_ele[i]];
+          flux = fmaf(k.jr_scale * dc, (float)(1.0 / m->V0[j]), flux);
+        }
+        if (m->ryr_jsr[i] == j && ryr[i]) {
+          float dc = (k.dc0 + U[4 * m->ryr_jsr[i]]) - U[4 * m->ryr_ele[i]];
+          flux = fmaf(k.jr_scale * dc, (float)(-(1.0 / m->V0[j])), flux);
+        }
+      }
+      for (i = 0; i < m->NL; ++i)
+        if (m->lcc_ele[i] == j && (lcc[i] == 6 || lcc[i] == 12) && lccv[i] == 2) {
+          float c = rest[j] + U[4 * j];
+          flux = fmaf(k.lccA * fmaf(c, k.lccE, -k.lccB), (float)(1.0 / m->V0[j]), flux);
+        }
+      fp32_element(&k, &U[4 * j], Im[j], &U[4 * nb[0]], &U[4 * nb[1]], &U[4 * nb[2]], &U[4 * nb[3]],
+                   &a[4 * j], m->domain[j] == 1, m->tropc[j], bsl[j], flux, &CM[4 * j], &CI[j],
+                   &U2[4 * j], &I2[j]);
+    }
+    memcpy(U, U2, sizeof(float) * 4 * N);
+    memcpy(Im, I2, sizeof(float) * N);
+    if (gating) {
+      for (j = 0; j < N; ++j) ca[j] = (double)(rest[j] + U[4 * j]);
+      or_gating_philox(m, R, G[0], ca, seed, step0 + s, ryr, lcc, lccv, res);
+    }
+  }
+  free(U2);
+  free(I2);
+  free(a);
+  free(bsl);
+  free(rest);
+  free(ca);
 }

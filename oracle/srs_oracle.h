@@ -68,6 +68,17 @@ int64_t or_run_simulation(const or_mesh* m, const int* ints, const double* reals
                           uint64_t seed_or_rank, int index, float* rows, int64_t row_cap,
                           int row_w, double* states_out, double* t_end, int64_t* n_steps);
 
+/* The FP32 engines restated: deviation-form state u = c - c_rest (4 mobile
+ * species per element, AoS, plus the immobile buffer), each element updated
+ * with the same operation order as the GPU.  Reference numbering. */
+void or_fp32_to_dev(const or_mesh* m, const double* reals, const double* states, float* U, float* Im);
+void or_fp32_from_dev(const or_mesh* m, const double* reals, const float* U, const float* Im,
+                      const float* CM, const float* CI, double* states);
+/* CM (4N) and CI (N) hold the compensation terms of the Euler update. */
+void or_steps_fp32(const or_mesh* m, const double* reals, const double* globals, float* U, float* Im,
+                   float* CM, float* CI, uint64_t seed, int64_t step0, int64_t n, int* ryr, int* lcc,
+                   int* lccv, double* res, int gating);
+
 /* Bit-reproducible arithmetic restated (for direct tests). */
 float or_logf(float x);
 float or_exp2f(float y);

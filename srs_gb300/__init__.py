@@ -87,7 +87,8 @@ class _SimDesc(C.Structure):
 class _SimConfig(C.Structure):
     _fields_ = [("engine", C.c_int), ("precision", C.c_int), ("threads_per_cta", C.c_int),
                 ("cluster_size", C.c_int), ("steps_per_launch", C.c_int), ("smem_bytes", C.c_int),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("reset_h2d_bytes", C.c_int64),
+                ("ctl_bytes", C.c_int64), ("engine_elements", C.c_int64)]
 
 
 class _RunOutput(C.Structure):

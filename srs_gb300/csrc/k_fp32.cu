@@ -5,35 +5,37 @@
 // buffer reactions are written in the cancellation-free deviation form
 //   r = kon*((B - b_rest)*u - c*u_b) - koff*u_b,
 // which is the reference's kon*(B - b)*c - koff*b (cpu/RunSimulation.cpp:
-// 78, 95, 101, 107, 115) minus its value at rest (zero at equilibrium).  At
-// rest all deviations are zero, so single precision keeps full relative
-// precision in the small perturbations that make up most of the domain.
+// 78, 95, 101, 107, 115) minus its value at rest (zero at equilibrium).  The
+// explicit Euler update u += dt*r is compensated (Kahan summation): each
+// element keeps the rounding error of its last update and feeds it back, so
+// the tiny per-step increments (dt = 9 ns) do not accumulate a rounding bias
+// over millions of steps.  Compensation terms are private to the element's
+// owner thread and never travel to neighbours.
 //
 // Two engines share the per-element update `tet_update`:
 //   * k_plain32_step: one launch per time step, state in HBM, grid.y over
 //     realizations, last block per realization runs gating + protocol;
 //   * k_resident32<C>: persistent batched kernel.  One realization at a time
 //     per thread-block cluster of C CTAs; the mobile species (Ca, ATP, CMDN,
-//     dye) live in shared memory as float4, double buffered, partitioned
-//     over the cluster; neighbours in another CTA's partition are read
-//     through distributed shared memory.  Warp 0 of every CTA runs the
-//     channel work (gating, protocol, release flux and the elements that
-//     carry channels) while the other warps update all other elements, so a
-//     time step costs one cluster barrier.
-#include <cooperative_groups.h>
-
+//     dye) live in shared memory as float4, double buffered, partitioned over
+//     the cluster; neighbours in another CTA's partition are read through
+//     distributed shared memory.  Every element that carries a channel sits in
+//     partition 0, where warp 0 computes the release flux, updates those
+//     elements, gates the channels and runs the protocol of the next step
+//     while the other warps update everything else — one cluster barrier per
+//     time step, and the termination decision is known at that barrier.
 #include "srs_engine.h"
 #include "srs_protocol.cuh"
 
 namespace srs {
 
-
-
+// One element, one step.  o/im: state, cm/ci: compensation (updated in place),
+// s1..s4: neighbour states, a: off-diagonal coefficients.
 // flags: bit0 JSR, bit1 TropC, bit2 carries channel entries.
 __device__ __forceinline__ void tet_update(const Consts32& k, float4 o, float im, float4 s1,
                                            float4 s2, float4 s3, float4 s4, float4 a,
                                            uint32_t fl, float bsl, float kb, float flux,
-                                           float4* out, float* im_out) {
+                                           float4& cm, float& ci, float4* out, float* im_out) {
   float dx = a.x * (s1.x - o.x);
   dx = fmaf(a.y, s2.x - o.x, dx);
   dx = fmaf(a.z, s3.x - o.x, dx);
@@ -68,6 +70,7 @@ __device__ __forceinline__ void tet_update(const Consts32& k, float4 o, float im
       rca -= rb;
       rim = rb;
       float Ki = c * k.inv_kdi;
+      Ki = Ki * Ki;  // K_i = (c / K_D_i)^2 (cpu/RunSimulation.cpp:83-84)
       float Ki2 = Ki * Ki;
       float den = fmaf(Ki2, k.sd2, fmaf(Ki, k.sd1, k.sd0));
       float num = fmaf(Ki2, 3.24873e12f, fmaf(Ki, k.sn1, -k.sn0));
@@ -94,20 +97,33 @@ __device__ __forceinline__ void tet_update(const Consts32& k, float4 o, float im
     float kc = k.khi + c;
     rca = rca / fmaf(bsl, 1.0f / (kc * kc), 1.0f);
   }
-  out->x = fmaf(k.dt, rca, o.x);
-  out->y = fmaf(k.dt, ratp, o.y);
-  out->z = fmaf(k.dt, rcmdn, o.z);
-  out->w = fmaf(k.dt, rdye, o.w);
-  *im_out = fmaf(k.dt, rim, im);
+  // compensated Euler: y = dt*r - comp; t = u + y; comp = (t - u) - y
+  float y, t;
+  y = fmaf(k.dt, rca, -cm.x);
+  t = o.x + y;
+  cm.x = (t - o.x) - y;
+  out->x = t;
+  y = fmaf(k.dt, ratp, -cm.y);
+  t = o.y + y;
+  cm.y = (t - o.y) - y;
+  out->y = t;
+  y = fmaf(k.dt, rcmdn, -cm.z);
+  t = o.z + y;
+  cm.z = (t - o.z) - y;
+  out->z = t;
+  y = fmaf(k.dt, rdye, -cm.w);
+  t = o.w + y;
+  cm.w = (t - o.w) - y;
+  out->w = t;
+  y = fmaf(k.dt, rim, -ci);
+  t = im + y;
+  ci = (t - im) - y;
+  *im_out = t;
 }
-
-
 
 // ===========================================================================
 // Plain FP32 engine
 // ===========================================================================
-
-
 __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
   const int r = blockIdx.y;
   RealCtl* ctlp = a.CS.ctl + r;
@@ -128,24 +144,30 @@ __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
       const int v = ctlp->vsel;
       for (int q = a.chan_ptr[j]; q < a.chan_ptr[j + 1]; ++q) {
         ChanEntry32 e = a.chan_list[q];
+        float J = 0.0f;
         if (e.kind < 2) {
           if (ryr[e.ch]) {
             float dc = (a.k.dc0 + M[a.C.ryr_jsr[e.ch]].x) - M[a.C.ryr_cleft[e.ch]].x;
-            flux = fmaf(a.k.jr_scale * dc, e.s, flux);
+            J = a.k.jr_scale * dc;
           }
         } else if ((lcc[e.ch] == 6 || lcc[e.ch] == 12) && lccv[e.ch] == 2) {
           float c = a.rest_ca[j] + M[j].x;
-          flux = fmaf(a.k.lccA[v] * fmaf(c, a.k.lccE[v], -a.k.lccB), e.s, flux);
+          J = a.k.lccA[v] * fmaf(c, a.k.lccE[v], -a.k.lccB);
         }
+        flux = fmaf(J, e.s, flux);
       }
     }
     const int4 nb = a.nb[j];
+    float4 cm = a.CM[(size_t)r * N + j];
+    float ci = a.CI[(size_t)r * N + j];
     float4 out;
     float imo;
     tet_update(a.k, M[j], I[j], M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
-               a.kb ? a.kb[j] : 0.0f, flux, &out, &imo);
+               a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo);
     Mo[j] = out;
     Io[j] = imo;
+    a.CM[(size_t)r * N + j] = cm;
+    a.CI[(size_t)r * N + j] = ci;
     if (!isfinite(out.x)) atomicOr(&ctlp->status, 1u);
   }
   __shared__ int s_last;
@@ -210,12 +232,6 @@ int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStre
 // ===========================================================================
 // Resident FP32 engine
 // ===========================================================================
-// Packed element record (32 bytes): neighbour slot k holds
-// (cluster rank << off_bits) | local offset.
-
-
-
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -231,9 +247,9 @@ __device__ __forceinline__ float4 ld_dsmem_f4(uint32_t addr) {
                : "r"(addr));
   return v;
 }
-__device__ __forceinline__ float ld_dsmem_f32(uint32_t addr) {
-  float v;
-  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+__device__ __forceinline__ int32_t ld_dsmem_s32(uint32_t addr) {
+  int32_t v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr));
   return v;
 }
 __device__ __forceinline__ float4 ld_smem_f4(uint32_t addr) {
@@ -258,27 +274,19 @@ __device__ __forceinline__ void step_barrier() {
 }
 
 // Shared-memory layout of one CTA (dynamic):
-//   float4 buf[2][P]; float imm[2][P];  then the channel block below.
+//   float4 buf[2][P]; float4 cm[P]; float imm[P]; float ci[P]; then this
+//   tail, then the channel block (used by rank 0).
 struct ResidentSmemTail {
   RealCtl ctl;
   uint32_t base[2][16];  // cluster addresses of buf[b] in CTA rank q
   int32_t bad;
-  // Termination flag published by warp 0 in iteration s into slot s & 1 and
-  // read by every thread after that iteration's barrier.  Two slots, so a
-  // slow warp still reading slot s & 1 never sees warp 0's write for s + 1.
+  // Termination flag published by rank 0's warp 0 in iteration s into slot
+  // s & 1 and read by every thread of the cluster after that iteration's
+  // barrier.  Two slots, so a thread still reading slot s & 1 never sees the
+  // write for s + 1.
   int32_t done_flag[2];
 };
 
-// Deviation u of the element with code `code` in the current buffer.
-template <int C>
-__device__ __forceinline__ float resident_u(const ResidentArgs& a, const uint32_t* bs,
-                                            const float4* src, uint32_t code, uint32_t mask) {
-  if constexpr (C == 1) {
-    return src[code & mask].x;
-  } else {
-    return ld_dsmem_f32(bs[code >> a.off_bits] + (code & mask) * 16u);
-  }
-}
 template <int C>
 __device__ __forceinline__ float4 resident_nb(const uint32_t* bs, const float4* src,
                                               uint32_t code, int off_bits, uint32_t mask) {
@@ -289,13 +297,12 @@ __device__ __forceinline__ float4 resident_nb(const uint32_t* bs, const float4* 
   }
 }
 
-// Absolute Ca by channel code for the protocol code: the resident engine's
-// Channels arrays hold (kind << 28 | channel) instead of element indices,
-// kind 0 = RyR cleft element, 1 = RyR JSR element, 2 = LCC element.
-template <int C>
+// Absolute Ca by channel code for the protocol code.  The resident engine's
+// Channels arrays hold (kind << 28 | channel) instead of element indices:
+// kind 0 = RyR cleft element, 1 = RyR JSR element, 2 = LCC element.  All of
+// them live in partition 0 (local shared memory of rank 0).
 struct ResidentCa {
   const ResidentArgs* a;
-  const uint32_t* bs;
   const float4* src;
   uint32_t mask;
   __device__ double operator()(int e) const {
@@ -312,16 +319,16 @@ struct ResidentCa {
       code = a->lcc_code[idx];
       rest = a->lcc_rest[idx];
     }
-    return (double)(resident_u<C>(*a, bs, src, code, mask) + rest);
+    return (double)(src[code & mask].x + rest);
   }
 };
 
 // Gating of every channel after time step ctl.step by one warp
-// (UpdateChannelGating, cpu/RunSimulation.cpp:656-674).
-template <int C>
-__device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const uint32_t* bs,
-                              const float4* src, int32_t* s_ryr, int32_t* s_lcc, int32_t* s_lccv,
-                              double* s_res, int32_t* s_nb, int lane) {
+// (UpdateChannelGating, cpu/RunSimulation.cpp:656-674).  `src` holds the
+// state after that step; every channel element is local (partition 0).
+__device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const float4* src,
+                              int32_t* s_ryr, int32_t* s_lcc, int32_t* s_lccv, double* s_res,
+                              int32_t* s_nb, int lane) {
   const int NR = a.C.NR, NL = a.C.NL;
   const uint32_t mask = (1u << a.off_bits) - 1u;
   const srs_gate_consts* g = &a.P_.gc[ctl.vsel];
@@ -346,15 +353,15 @@ __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const uint32_
       no = s_nb[i] & 0xffff;
       nc = s_nb[i] >> 16;
     }
-    float cs = resident_u<C>(a, bs, src, a.ryr_cleft_code[i], mask) + a.k.c0;
-    float cj = resident_u<C>(a, bs, src, a.ryr_jsr_code[i], mask) + a.k.c0j;
+    float cs = src[a.ryr_cleft_code[i] & mask].x + a.k.c0;
+    float cj = src[a.ryr_jsr_code[i] & mask].x + a.k.c0j;
     double rr = s_res[i];
     s_ryr[i] = srs_gate_ryr(g, s_ryr[i], cs, cj, no, nc, &rr, ctl.seed, (uint32_t)i,
                             (uint64_t)ctl.step);
     s_res[i] = rr;
   }
   for (int i = lane; i < NL; i += 32) {
-    float cs = resident_u<C>(a, bs, src, a.lcc_code[i], mask) + a.lcc_rest[i];
+    float cs = src[a.lcc_code[i] & mask].x + a.lcc_rest[i];
     double rr = s_res[NR + i];
     int st = s_lcc[i], vs = s_lccv[i];
     srs_gate_lcc(g, &st, &vs, cs, &rr, ctl.seed, (uint32_t)(NR + i), (uint64_t)ctl.step);
@@ -365,16 +372,31 @@ __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const uint32_
   __syncwarp();
 }
 
+// Protocol of step ctl.step (rank 0, warp 0; lane 0 does the work).
+__device__ void resident_prestep(const ResidentArgs& a, RealCtl& ctl, const float4* src,
+                                 int32_t* s_ryr, int32_t* s_lcc, int32_t* s_lccv, int r,
+                                 int write_row_now, int lane) {
+  if (lane == 0) {
+    ResidentCa cab{&a, src, (1u << a.off_bits) - 1u};
+    float* rows = a.CS.rows + (size_t)r * a.P_.row_cap * a.P_.row_w;
+    if (write_row_now && a.P_.run_protocol)
+      write_row(a.P_, a.C, ctl, s_ryr, s_lcc, s_lccv, rows, ctl.t, cab);
+    prestep(a.P_, a.C, ctl, s_ryr, s_lcc, s_lccv, rows, cab);
+  }
+  __syncwarp();
+}
+
 template <int C>
 __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int P = a.P;
   float4* buf0 = reinterpret_cast<float4*>(smem);
   float4* buf1 = buf0 + P;
-  float* imm0 = reinterpret_cast<float*>(buf1 + P);
-  float* imm1 = imm0 + P;
+  float4* cmb = buf1 + P;
+  float* immb = reinterpret_cast<float*>(cmb + P);
+  float* cib = immb + P;
   const int NR = a.C.NR, NL = a.C.NL, NCH = NR + NL;
-  ResidentSmemTail* tail = reinterpret_cast<ResidentSmemTail*>(imm1 + P);
+  ResidentSmemTail* tail = reinterpret_cast<ResidentSmemTail*>(cib + P);
   int32_t* s_ryr = reinterpret_cast<int32_t*>(tail + 1);
   int32_t* s_lcc = s_ryr + NR;
   int32_t* s_lccv = s_lcc + NL;
@@ -394,11 +416,15 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
   const int warp = tid >> 5, lane = tid & 31;
   const int nthr = blockDim.x;
   const int n_loc = a.n_local[rank];
-  const int n_ch = a.n_chtet[rank];
+  const int n_ch = (rank == 0) ? a.n_chtet[0] : 0;  // channel elements: rank 0 only
+  const bool chan_warp = (rank == 0) && (warp == 0);
   const TetRec* geo = a.geo + (size_t)rank * P;
   const uint32_t off_mask = (1u << a.off_bits) - 1u;
   const Consts32& k = a.k;
   const Protocol& P_ = a.P_;
+  // regular elements: rank 0 leaves warp 0 to the channel work
+  const int t0 = (rank == 0) ? tid - 32 : tid;
+  const int tstride = (rank == 0) ? nthr - 32 : nthr;
 
   if (tid < 32) {
     for (int q = lane; q < C; q += 32) {
@@ -407,114 +433,101 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
     }
   }
   if (tid == 0) tail->bad = 0;
+  // address of rank 0's termination flags, as seen from this CTA
+  uint32_t done_addr0 = smem_addr(&tail->done_flag[0]);
+  if constexpr (C > 1) done_addr0 = map_rank(done_addr0, 0);
   step_barrier<C>();  // all CTAs of the cluster are running before DSMEM use
   int bad = 0;
 
   for (int r = cid; r < a.R; r += ncl) {
     // ---- load the realization ----------------------------------------------
-    const float4* Mg = a.M + ((size_t)r * C + rank) * P;
-    const float* Ig = a.I + ((size_t)r * C + rank) * P;
+    const size_t roff = ((size_t)r * C + rank) * P;
     for (int i = tid; i < n_loc; i += nthr) {
-      buf0[i] = Mg[i];
-      imm0[i] = Ig[i];
+      buf0[i] = a.M[roff + i];
+      immb[i] = a.I[roff + i];
+      cmb[i] = a.CM[roff + i];
+      cib[i] = a.CI[roff + i];
     }
-    if (tid == 0) {
-      tail->ctl = a.CS.ctl[r];
-      tail->done_flag[1] = tail->ctl.done;
+    if (rank == 0) {
+      if (tid == 0) tail->ctl = a.CS.ctl[r];
+      for (int i = tid; i < NR; i += nthr) s_ryr[i] = a.CS.ryr[(size_t)r * NR + i];
+      for (int i = tid; i < NL; i += nthr) {
+        s_lcc[i] = a.CS.lcc[(size_t)r * NL + i];
+        s_lccv[i] = a.CS.lccv[(size_t)r * NL + i];
+      }
+      for (int i = tid; i < NCH; i += nthr) s_res[i] = a.CS.res[(size_t)r * NCH + i];
     }
-    for (int i = tid; i < NR; i += nthr) s_ryr[i] = a.CS.ryr[(size_t)r * NR + i];
-    for (int i = tid; i < NL; i += nthr) {
-      s_lcc[i] = a.CS.lcc[(size_t)r * NL + i];
-      s_lccv[i] = a.CS.lccv[(size_t)r * NL + i];
+    __syncthreads();
+    if (chan_warp) {
+      // protocol work that precedes the first step of a run
+      if (a.prestep_first && !tail->ctl.done)
+        resident_prestep(a, tail->ctl, buf0, s_ryr, s_lcc, s_lccv, r, a.initial_row, lane);
+      if (lane == 0) tail->done_flag[1] = tail->ctl.done;
     }
-    for (int i = tid; i < NCH; i += nthr) s_res[i] = a.CS.res[(size_t)r * NCH + i];
     step_barrier<C>();
-    const bool skip = tail->done_flag[1] != 0;
+    const bool skip = ((C > 1) ? ld_dsmem_s32(done_addr0 + 4u) : tail->done_flag[1]) != 0;
     int cur = 0;
     if (!skip) {
       for (int s = 0; s < a.steps; ++s) {
         const float4* src = cur ? buf1 : buf0;
         float4* dst = cur ? buf0 : buf1;
-        const float* isrc = cur ? imm1 : imm0;
-        float* idst = cur ? imm0 : imm1;
         const uint32_t* bs = tail->base[cur];
-        if (warp == 0) {
-          // ---- channel work ------------------------------------------------
+        if (chan_warp) {
+          // ---- channel work: flux, channel elements, gating, next protocol --
           RealCtl& ctl = tail->ctl;
-          if (s > 0) {
-            if (!P_.nogating) resident_gate<C>(a, ctl, bs, src, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
-            if (lane == 0) {
-              ctl.step += 1;
-              ctl.t += P_.dt;
+          const int v = ctl.vsel;
+          for (int i = lane; i < NR; i += 32) {
+            float J = 0.0f;
+            if (s_ryr[i]) {
+              float us = src[a.ryr_cleft_code[i] & off_mask].x;
+              float uj = src[a.ryr_jsr_code[i] & off_mask].x;
+              J = k.jr_scale * ((k.dc0 + uj) - us);
             }
-            __syncwarp();
+            s_jr[i] = J;
           }
-          if (lane == 0) {
-            ResidentCa<C> cab{&a, bs, src, off_mask};
-            if (rank == 0) {
-              prestep(P_, a.C, ctl, s_ryr, s_lcc, s_lccv,
-                      a.CS.rows + (size_t)r * P_.row_cap * P_.row_w, cab);
-            } else {
-              // the other CTAs of the cluster track the same protocol state
-              // without writing rows
-              Protocol Pq = P_;
-              Pq.row_cap = 0;
-              const int64_t nr = ctl.n_rows;
-              const uint32_t st = ctl.status;
-              prestep(Pq, a.C, ctl, s_ryr, s_lcc, s_lccv, a.CS.rows, cab);
-              ctl.n_rows = nr;
-              ctl.status = st;
+          for (int i = lane; i < NL; i += 32) {
+            float J = 0.0f;
+            if ((s_lcc[i] == 6 || s_lcc[i] == 12) && s_lccv[i] == 2) {
+              float c = a.lcc_rest[i] + src[a.lcc_code[i] & off_mask].x;
+              J = k.lccA[v] * fmaf(c, k.lccE[v], -k.lccB);
             }
-            tail->done_flag[s & 1] = ctl.done;
+            s_jl[i] = J;
           }
           __syncwarp();
-          if (!ctl.done) {
-            // release flux of every channel for this step
-            const int v = ctl.vsel;
-            for (int i = lane; i < NR; i += 32) {
-              float J = 0.0f;
-              if (s_ryr[i]) {
-                float us = resident_u<C>(a, bs, src, a.ryr_cleft_code[i], off_mask);
-                float uj = resident_u<C>(a, bs, src, a.ryr_jsr_code[i], off_mask);
-                J = k.jr_scale * ((k.dc0 + uj) - us);
-              }
-              s_jr[i] = J;
+          for (int i = lane; i < n_ch; i += 32) {
+            const TetRec g = geo[i];
+            float flux = 0.0f;
+            for (int q = a.ch_ptr[i]; q < a.ch_ptr[i + 1]; ++q) {
+              ChanEntry32 e = a.ch_list[q];
+              float J = (e.kind < 2) ? s_jr[e.ch] : s_jl[e.ch];
+              flux = fmaf(J, e.s, flux);
             }
-            for (int i = lane; i < NL; i += 32) {
-              float J = 0.0f;
-              if ((s_lcc[i] == 6 || s_lcc[i] == 12) && s_lccv[i] == 2) {
-                float c = a.lcc_rest[i] + resident_u<C>(a, bs, src, a.lcc_code[i], off_mask);
-                J = k.lccA[v] * fmaf(c, k.lccE[v], -k.lccB);
-              }
-              s_jl[i] = J;
-            }
-            __syncwarp();
-            // channel elements of this partition
-            const int32_t* cp = a.ch_ptr + (size_t)rank * a.ch_stride;
-            for (int i = lane; i < n_ch; i += 32) {
-              const TetRec g = geo[i];
-              float flux = 0.0f;
-              for (int q = cp[i]; q < cp[i + 1]; ++q) {
-                ChanEntry32 e = a.ch_list[q];
-                float J = (e.kind < 2) ? s_jr[e.ch] : s_jl[e.ch];
-                flux = fmaf(J, e.s, flux);
-              }
-              float4 nv[4];
+            float4 nv[4];
 #pragma unroll
-              for (int q = 0; q < 4; ++q) nv[q] = resident_nb<C>(bs, src, g.nb[q], a.off_bits, off_mask);
-              float4 out;
-              float imo;
-              tet_update(k, src[i], isrc[i], nv[0], nv[1], nv[2], nv[3],
-                         make_float4(g.a[0], g.a[1], g.a[2], g.a[3]), g.flags, g.bsl, 0.0f, flux,
-                         &out, &imo);
-              dst[i] = out;
-              idst[i] = imo;
-              bad |= !isfinite(out.x);
-            }
+            for (int q = 0; q < 4; ++q) nv[q] = resident_nb<C>(bs, src, g.nb[q], a.off_bits, off_mask);
+            float4 out, cm = cmb[i];
+            float imo, ci = cib[i];
+            tet_update(k, src[i], immb[i], nv[0], nv[1], nv[2], nv[3],
+                       make_float4(g.a[0], g.a[1], g.a[2], g.a[3]), g.flags, g.bsl, 0.0f, flux,
+                       cm, ci, &out, &imo);
+            dst[i] = out;
+            immb[i] = imo;
+            cmb[i] = cm;
+            cib[i] = ci;
+            bad |= !isfinite(out.x);
           }
+          __syncwarp();
+          // gating after this step reads the channel elements just written
+          if (!P_.nogating) resident_gate(a, ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
+          if (lane == 0) {
+            ctl.step += 1;
+            ctl.t += P_.dt;
+          }
+          __syncwarp();
+          resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane);
+          if (lane == 0) tail->done_flag[s & 1] = ctl.done;
         } else {
           // ---- all other elements ------------------------------------------
-          const int t0 = tid - 32, tstride = nthr - 32;
           for (int i = n_ch + t0; i < n_loc; i += tstride) {
             const float4* gp = reinterpret_cast<const float4*>(geo + i);
             float4 ga = __ldg(gp);
@@ -533,47 +546,35 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
               n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & off_mask) * 16u);
               n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & off_mask) * 16u);
             }
-            float4 out;
-            float imo;
-            tet_update(k, src[i], isrc[i], n0, n1, n2, n3, ga, __float_as_uint(gb.w), gb.z, 0.0f,
-                       0.0f, &out, &imo);
+            float4 out, cm = cmb[i];
+            float imo, ci = cib[i];
+            tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, __float_as_uint(gb.w), gb.z, 0.0f,
+                       0.0f, cm, ci, &out, &imo);
             dst[i] = out;
-            idst[i] = imo;
+            immb[i] = imo;
+            cmb[i] = cm;
+            cib[i] = ci;
             bad |= !isfinite(out.x);
           }
         }
         step_barrier<C>();
-        if (tail->done_flag[s & 1]) break;
         cur ^= 1;
-      }
-      if (!tail->ctl.done && warp == 0) {
-        // gating after the last step of this launch (the next launch starts
-        // with the protocol work of the following step)
-        RealCtl& ctl = tail->ctl;
-        const float4* src = cur ? buf1 : buf0;
-        const uint32_t* bs = tail->base[cur];
-        if (!P_.nogating) resident_gate<C>(a, ctl, bs, src, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
-        if (lane == 0) {
-          ctl.step += 1;
-          ctl.t += P_.dt;
-        }
-        __syncwarp();
+        const int done =
+            (C > 1) ? ld_dsmem_s32(done_addr0 + 4u * (uint32_t)(s & 1)) : tail->done_flag[s & 1];
+        if (done) break;
       }
     }
     step_barrier<C>();
     // ---- store the realization ----------------------------------------------
-    {
+    if (!skip) {
       const float4* fin = cur ? buf1 : buf0;
-      const float* ifin = cur ? imm1 : imm0;
-      float4* Mw = a.M + ((size_t)r * C + rank) * P;
-      float* Iw = a.I + ((size_t)r * C + rank) * P;
-      if (!skip) {
-        for (int i = tid; i < n_loc; i += nthr) {
-          Mw[i] = fin[i];
-          Iw[i] = ifin[i];
-        }
+      for (int i = tid; i < n_loc; i += nthr) {
+        a.M[roff + i] = fin[i];
+        a.I[roff + i] = immb[i];
+        a.CM[roff + i] = cmb[i];
+        a.CI[roff + i] = cib[i];
       }
-      if (rank == 0 && !skip) {
+      if (rank == 0) {
         for (int i = tid; i < NR; i += nthr) a.CS.ryr[(size_t)r * NR + i] = s_ryr[i];
         for (int i = tid; i < NL; i += nthr) {
           a.CS.lcc[(size_t)r * NL + i] = s_lcc[i];
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
         if (tid == 0) a.CS.ctl[r] = tail->ctl;
       }
     }
-    step_barrier<C>();  // smem reused by the next realization
+    step_barrier<C>();  // shared memory is reused by the next realization
   }
   if (bad) atomicOr(&tail->bad, 1);
   __syncthreads();
@@ -592,7 +593,7 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
 }
 
 size_t resident_smem_bytes(int P, int NR, int NL) {
-  size_t b = (size_t)P * (2 * sizeof(float4) + 2 * sizeof(float));
+  size_t b = (size_t)P * (3 * sizeof(float4) + 2 * sizeof(float));
   b += sizeof(ResidentSmemTail);
   b += (size_t)(NR + 2 * NL + NR) * sizeof(int32_t);
   b += (size_t)(NR + NL) * sizeof(float);
@@ -602,15 +603,18 @@ size_t resident_smem_bytes(int P, int NR, int NL) {
 }
 
 template <int C>
+static cudaError_t set_attrs(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_resident32<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  if (C > 8) e = cudaFuncSetAttribute(k_resident32<C>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+template <int C>
 static int launch_resident_t(const ResidentArgs& a, int n_clusters, int threads, size_t smem,
                              cudaStream_t st) {
-  auto fn = k_resident32<C>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return -1;
-  if (C > 8) {
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return -1;
-  }
+  if (set_attrs<C>(smem) != cudaSuccess) return -1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n_clusters * C);
   cfg.blockDim = dim3(threads);
@@ -623,24 +627,16 @@ static int launch_resident_t(const ResidentArgs& a, int n_clusters, int threads,
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelEx(&cfg, fn, a);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_resident32<C>, a);
   return e == cudaSuccess ? 0 : -1;
 }
 
-int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
-                    cudaStream_t st) {
-  switch (C) {
-    case 1: return launch_resident_t<1>(a, n_clusters, threads, smem, st);
-    case 2: return launch_resident_t<2>(a, n_clusters, threads, smem, st);
-    case 4: return launch_resident_t<4>(a, n_clusters, threads, smem, st);
-    case 8: return launch_resident_t<8>(a, n_clusters, threads, smem, st);
-    case 16: return launch_resident_t<16>(a, n_clusters, threads, smem, st);
-    default: return -1;
+template <int C>
+static int max_clusters_t(int threads, size_t smem) {
+  if (set_attrs<C>(smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
   }
-}
-
-// Largest number of co-resident clusters for a configuration (0: does not fit).
-int resident_max_clusters(int C, int threads, size_t smem) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(C);
   cfg.blockDim = dim3(threads);
@@ -653,25 +649,48 @@ int resident_max_clusters(int C, int threads, size_t smem) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  cudaError_t e;
-  switch (C) {
-#define SRS_MC(CC)                                                                        \
-  case CC:                                                                                \
-    cudaFuncSetAttribute(k_resident32<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                         (int)smem);                                                      \
-    if (CC > 8)                                                                           \
-      cudaFuncSetAttribute(k_resident32<CC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1); \
-    e = cudaOccupancyMaxActiveClusters(&n, k_resident32<CC>, &cfg);                       \
-    break;
-    SRS_MC(1) SRS_MC(2) SRS_MC(4) SRS_MC(8) SRS_MC(16)
-#undef SRS_MC
-    default: return 0;
-  }
-  if (e != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, k_resident32<C>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return n;
+}
+
+#define SRS_RESIDENT_SIZES(X) X(1) X(2) X(3) X(4) X(5) X(6) X(8) X(16)
+
+int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
+                    cudaStream_t st) {
+  switch (C) {
+#define SRS_L(CC) \
+  case CC:        \
+    return launch_resident_t<CC>(a, n_clusters, threads, smem, st);
+    SRS_RESIDENT_SIZES(SRS_L)
+#undef SRS_L
+    default: return -1;
+  }
+}
+
+// Largest number of co-resident clusters for a configuration (0: does not fit).
+int resident_max_clusters(int C, int threads, size_t smem) {
+  switch (C) {
+#define SRS_M(CC) \
+  case CC:        \
+    return max_clusters_t<CC>(threads, smem);
+    SRS_RESIDENT_SIZES(SRS_M)
+#undef SRS_M
+    default: return 0;
+  }
+}
+
+bool resident_cluster_supported(int C) {
+  switch (C) {
+#define SRS_S(CC) \
+  case CC:        \
+    return true;
+    SRS_RESIDENT_SIZES(SRS_S)
+#undef SRS_S
+    default: return false;
+  }
 }
 
 }  // namespace srs

@@ -70,12 +70,16 @@ struct srs_sim {
   double* d_S[2] = {nullptr, nullptr};
   float4* d_M[2] = {nullptr, nullptr};
   float* d_I[2] = {nullptr, nullptr};
+  float4* d_CM = nullptr;  // FP32 engines: Euler compensation terms
+  float* d_CI = nullptr;
   int C = 1, threads = 0, n_clusters = 0, P_stride = 0, off_bits = 0;
   size_t smem = 0;
   std::vector<int> part_start, part_len, part_nch;  // resident partitions
   int64_t launches = 0;
   cudaGraphExec_t graph_plain = nullptr;
   int graph_plain_len = 0;
+  void* h_stage = nullptr;  // pinned host staging for state uploads
+  size_t h_stage_bytes = 0;
 };
 
 namespace {
@@ -414,28 +418,42 @@ int setup_plain32(srs_sim* s) {
     SRS_TRY(dev_alloc(s, &s->d_M[b], (size_t)s->R * N));
     SRS_TRY(dev_alloc(s, &s->d_I[b], (size_t)s->R * N));
   }
+  SRS_TRY(dev_alloc(s, &s->d_CM, (size_t)s->R * N));
+  SRS_TRY(dev_alloc(s, &s->d_CI, (size_t)s->R * N));
   SRS_TRY(upload_channels_engine_order(s));
   return SRS_OK;
 }
 
 // ---- FP32 resident engine ----------------------------------------------------
 int resident_partition(srs_sim* s, int C) {
-  // RCM order by domain, cut into C contiguous partitions; inside each, the
-  // elements carrying channels come first (they are updated by warp 0).
+  // Elements carrying channels first (they form the head of partition 0 and
+  // are updated by its warp 0), then the RCM order of all other elements;
+  // the sequence is cut into C contiguous partitions of equal size.
   const int N = s->N;
   std::vector<int> base = rcm_order_by_domain(s->m, s->op);
   std::vector<char> has_ch(N, 0);
   for (int i = 0; i < s->m.NR; ++i) has_ch[s->m.ryr_ele[i]] = has_ch[s->m.ryr_jsr[i]] = 1;
   for (int i = 0; i < s->m.NL; ++i) has_ch[s->m.lcc_ele[i]] = 1;
+  std::vector<int> seq;
+  seq.reserve(N);
+  for (int j : base)
+    if (has_ch[j]) seq.push_back(j);
+  const int n_ch = (int)seq.size();
+  for (int j : base)
+    if (!has_ch[j]) seq.push_back(j);
   s->part_start.assign(C, 0);
   s->part_len.assign(C, 0);
   s->part_nch.assign(C, 0);
   int Pmax = 0;
   for (int q = 0; q < C; ++q) {
-    int b = (int)((int64_t)N * q / C), e = (int)((int64_t)N * (q + 1) / C);
-    s->part_len[q] = e - b;
-    Pmax = std::max(Pmax, e - b);
+    int b0 = (int)((int64_t)N * q / C), e0 = (int)((int64_t)N * (q + 1) / C);
+    s->part_start[q] = b0;
+    s->part_len[q] = e0 - b0;
+    Pmax = std::max(Pmax, e0 - b0);
   }
+  if (n_ch > s->part_len[0])
+    return fail(SRS_ERR_UNSUPPORTED, "channel elements do not fit in one partition");
+  s->part_nch[0] = n_ch;
   int bits = 1;
   while ((1 << bits) < Pmax) ++bits;
   int rank_bits = 0;
@@ -443,26 +461,14 @@ int resident_partition(srs_sim* s, int C) {
   if (bits + rank_bits > 16) return fail(SRS_ERR_UNSUPPORTED, "partition too large for 16-bit element codes");
   s->off_bits = bits;
   s->P_stride = (Pmax + 3) & ~3;
-  // engine index = q * P_stride + local offset
   s->ref_of_eng.assign((size_t)C * s->P_stride, -1);
   s->eng_of_ref.assign(N, -1);
-  for (int q = 0; q < C; ++q) {
-    int b = (int)((int64_t)N * q / C), e = (int)((int64_t)N * (q + 1) / C);
-    std::vector<int> first, rest;
-    for (int i = b; i < e; ++i) (has_ch[base[i]] ? first : rest).push_back(base[i]);
-    s->part_nch[q] = (int)first.size();
-    int off = 0;
-    for (int j : first) {
-      s->ref_of_eng[(size_t)q * s->P_stride + off] = j;
-      s->eng_of_ref[j] = q * s->P_stride + off;
-      ++off;
+  for (int q = 0; q < C; ++q)
+    for (int i = 0; i < s->part_len[q]; ++i) {
+      int j = seq[s->part_start[q] + i];
+      s->ref_of_eng[(size_t)q * s->P_stride + i] = j;
+      s->eng_of_ref[j] = q * s->P_stride + i;
     }
-    for (int j : rest) {
-      s->ref_of_eng[(size_t)q * s->P_stride + off] = j;
-      s->eng_of_ref[j] = q * s->P_stride + off;
-      ++off;
-    }
-  }
   return SRS_OK;
 }
 
@@ -498,21 +504,15 @@ int setup_resident(srs_sim* s, int C, int threads) {
       per[s->eng_of_ref[s->m.ryr_jsr[i]]].push_back({1, i});
     }
     for (int i = 0; i < s->m.NL; ++i) per[s->eng_of_ref[s->m.lcc_ele[i]]].push_back({2, i});
-    int maxch = *std::max_element(s->part_nch.begin(), s->part_nch.end());
-    int stride = maxch + 1;
-    std::vector<int32_t> cptr((size_t)C * stride, 0);
+    const int n_ch = s->part_nch[0];
+    std::vector<int32_t> cptr(n_ch + 1, 0);
     std::vector<ChanEntry32> clist;
-    for (int q = 0; q < C; ++q) {
-      for (int i = 0; i < s->part_nch[q]; ++i) {
-        int e = q * s->P_stride + i;
-        cptr[(size_t)q * stride + i] = (int32_t)clist.size();
-        double iv = 1.0 / s->m.V0[s->ref_of_eng[e]];
-        for (auto& ce : per[e])
-          clist.push_back({ce.kind, ce.ch, (float)(ce.kind == 1 ? -iv : iv), 0});
-      }
-      for (int i = s->part_nch[q]; i < stride; ++i) cptr[(size_t)q * stride + i] = (int32_t)clist.size();
+    for (int i = 0; i < n_ch; ++i) {
+      cptr[i] = (int32_t)clist.size();
+      double iv = 1.0 / s->m.V0[s->ref_of_eng[i]];
+      for (auto& ce : per[i]) clist.push_back({ce.kind, ce.ch, (float)(ce.kind == 1 ? -iv : iv), 0});
     }
-    s->ar.ch_stride = stride;
+    cptr[n_ch] = (int32_t)clist.size();
     SRS_TRY(dev_upload(s, (int32_t**)&s->ar.ch_ptr, cptr.data(), cptr.size()));
     SRS_TRY(dev_upload(s, (ChanEntry32**)&s->ar.ch_list, clist.data(), clist.size()));
     for (int e = 0; e < NE; ++e) {
@@ -575,6 +575,9 @@ int setup_resident(srs_sim* s, int C, int threads) {
   s->ch.lcc_ele = p4;
   SRS_TRY(dev_alloc(s, &s->d_M[0], (size_t)s->R * NE));
   SRS_TRY(dev_alloc(s, &s->d_I[0], (size_t)s->R * NE));
+  SRS_TRY(dev_alloc(s, &s->d_CM, (size_t)s->R * NE));
+  SRS_TRY(dev_alloc(s, &s->d_CI, (size_t)s->R * NE));
+  if (!resident_cluster_supported(C)) return fail(SRS_ERR_UNSUPPORTED, "unsupported cluster size");
   s->C = C;
   s->threads = threads;
   s->smem = resident_smem_bytes(s->P_stride, s->NR, s->NL);
@@ -590,32 +593,76 @@ size_t eng_count(const srs_sim* s) {
 }
 
 // ---- state conversion ---------------------------------------------------------
-int upload_state(srs_sim* s, int r, const double* S6) {
-  const int N = s->N;
-  if (s->d.precision == SRS_FP64) {
-    SRS_CUDA(cudaMemcpy(s->d_S[0] + (size_t)r * 6 * N, S6, sizeof(double) * 6 * N,
-                        cudaMemcpyHostToDevice));
-    return SRS_OK;
+void* stage(srs_sim* s, size_t bytes) {
+  if (bytes > s->h_stage_bytes) {
+    if (s->h_stage) cudaFreeHost(s->h_stage);
+    s->h_stage = nullptr;
+    s->h_stage_bytes = 0;
+    if (cudaMallocHost(&s->h_stage, bytes) != cudaSuccess) return nullptr;
+    s->h_stage_bytes = bytes;
   }
-  size_t NE = eng_count(s);
-  std::vector<float4> M(NE, make_float4(0, 0, 0, 0));
-  std::vector<float> I(NE, 0.0f);
+  return s->h_stage;
+}
+
+// Reference-numbered absolute state -> engine layout of one realization.
+void to_engine_fp32(const srs_sim* s, const double* S6, float4* M, float* I) {
+  const int N = s->N;
+  const size_t NE = eng_count(s);
   const RestValues& rv = s->rv;
   for (size_t e = 0; e < NE; ++e) {
     int j = s->ref_of_eng[e];
-    if (j < 0) continue;
-    M[e] = make_float4((float)(S6[SP_CA * (size_t)N + j] - s->rest_ca[e]),
-                       (float)(S6[SP_ATP * (size_t)N + j] - rv.atp),
-                       (float)(S6[SP_CMDN * (size_t)N + j] - rv.cmdn),
-                       (float)(S6[SP_DYE * (size_t)N + j] - rv.dye));
+    if (j < 0) {
+      M[e] = make_float4(0, 0, 0, 0);
+      I[e] = 0.0f;
+      continue;
+    }
+    // mobile buffers rest at their cytosolic equilibrium; JSR elements carry
+    // none (they are never coupled to the cytosol by diffusion)
     bool jsr = s->m.domain[j] == DOMAIN_JSR;
+    double f = jsr ? 0.0 : 1.0;
+    M[e] = make_float4((float)(S6[SP_CA * (size_t)N + j] - s->rest_ca[e]),
+                       (float)(S6[SP_ATP * (size_t)N + j] - f * rv.atp),
+                       (float)(S6[SP_CMDN * (size_t)N + j] - f * rv.cmdn),
+                       (float)(S6[SP_DYE * (size_t)N + j] - f * rv.dye));
     double imm = jsr ? S6[SP_CSQN * (size_t)N + j] : S6[SP_TRPN * (size_t)N + j];
     I[e] = (float)(imm - s->rest_imm[e]);
   }
-  SRS_CUDA(cudaMemcpy(s->d_M[0] + r * NE, M.data(), NE * sizeof(float4), cudaMemcpyHostToDevice));
-  SRS_CUDA(cudaMemcpy(s->d_I[0] + r * NE, I.data(), NE * sizeof(float), cudaMemcpyHostToDevice));
+}
+
+// Uploads one state to realizations [r0, r1) through pinned staging.
+int upload_state_range(srs_sim* s, int r0, int r1, const double* S6) {
+  const int N = s->N;
+  const int nr = r1 - r0;
+  if (s->d.precision == SRS_FP64) {
+    const size_t per = (size_t)6 * N;
+    double* h = (double*)stage(s, per * nr * sizeof(double));
+    if (!h) return fail(SRS_ERR_NOMEM, "pinned staging allocation failed");
+    for (int r = 0; r < nr; ++r) std::memcpy(h + r * per, S6, per * sizeof(double));
+    SRS_CUDA(cudaMemcpyAsync(s->d_S[0] + (size_t)r0 * per, h, per * nr * sizeof(double),
+                             cudaMemcpyHostToDevice, s->st));
+    SRS_CUDA(cudaStreamSynchronize(s->st));
+    return SRS_OK;
+  }
+  const size_t NE = eng_count(s);
+  float4* hM = (float4*)stage(s, NE * nr * (sizeof(float4) + sizeof(float)));
+  if (!hM) return fail(SRS_ERR_NOMEM, "pinned staging allocation failed");
+  float* hI = (float*)(hM + NE * nr);
+  to_engine_fp32(s, S6, hM, hI);
+  for (int r = 1; r < nr; ++r) {
+    std::memcpy(hM + r * NE, hM, NE * sizeof(float4));
+    std::memcpy(hI + r * NE, hI, NE * sizeof(float));
+  }
+  SRS_CUDA(cudaMemcpyAsync(s->d_M[0] + (size_t)r0 * NE, hM, NE * nr * sizeof(float4),
+                           cudaMemcpyHostToDevice, s->st));
+  SRS_CUDA(cudaMemcpyAsync(s->d_I[0] + (size_t)r0 * NE, hI, NE * nr * sizeof(float),
+                           cudaMemcpyHostToDevice, s->st));
+  SRS_CUDA(cudaMemsetAsync(s->d_CM + (size_t)r0 * NE, 0, NE * nr * sizeof(float4), s->st));
+  SRS_CUDA(cudaMemsetAsync(s->d_CI + (size_t)r0 * NE, 0, NE * nr * sizeof(float), s->st));
+  SRS_CUDA(cudaStreamSynchronize(s->st));
   return SRS_OK;
 }
+
+int upload_state(srs_sim* s, int r, const double* S6) { return upload_state_range(s, r, r + 1, S6); }
 
 int download_state(srs_sim* s, int r, double* S6) {
   const int N = s->N;
@@ -625,20 +672,25 @@ int download_state(srs_sim* s, int r, double* S6) {
     return SRS_OK;
   }
   size_t NE = eng_count(s);
-  std::vector<float4> M(NE);
-  std::vector<float> I(NE);
+  std::vector<float4> M(NE), CMh(NE);
+  std::vector<float> I(NE), CIh(NE);
   SRS_CUDA(cudaMemcpy(M.data(), s->d_M[0] + r * NE, NE * sizeof(float4), cudaMemcpyDeviceToHost));
   SRS_CUDA(cudaMemcpy(I.data(), s->d_I[0] + r * NE, NE * sizeof(float), cudaMemcpyDeviceToHost));
+  SRS_CUDA(cudaMemcpy(CMh.data(), s->d_CM + r * NE, NE * sizeof(float4), cudaMemcpyDeviceToHost));
+  SRS_CUDA(cudaMemcpy(CIh.data(), s->d_CI + r * NE, NE * sizeof(float), cudaMemcpyDeviceToHost));
   const RestValues& rv = s->rv;
   for (size_t e = 0; e < NE; ++e) {
     int j = s->ref_of_eng[e];
     if (j < 0) continue;
     bool jsr = s->m.domain[j] == DOMAIN_JSR;
-    S6[SP_CA * (size_t)N + j] = s->rest_ca[e] + (double)M[e].x;
-    S6[SP_ATP * (size_t)N + j] = rv.atp + (double)M[e].y;
-    S6[SP_CMDN * (size_t)N + j] = rv.cmdn + (double)M[e].z;
-    S6[SP_DYE * (size_t)N + j] = rv.dye + (double)M[e].w;
-    double imm = s->rest_imm[e] + (double)I[e];
+    double f = jsr ? 0.0 : 1.0;
+    // compensated sum: the state is u - comp (the comp term holds the
+    // rounding error of the last update)
+    S6[SP_CA * (size_t)N + j] = s->rest_ca[e] + ((double)M[e].x - (double)CMh[e].x);
+    S6[SP_ATP * (size_t)N + j] = f * rv.atp + ((double)M[e].y - (double)CMh[e].y);
+    S6[SP_CMDN * (size_t)N + j] = f * rv.cmdn + ((double)M[e].z - (double)CMh[e].z);
+    S6[SP_DYE * (size_t)N + j] = f * rv.dye + ((double)M[e].w - (double)CMh[e].w);
+    double imm = s->rest_imm[e] + ((double)I[e] - (double)CIh[e]);
     S6[SP_TRPN * (size_t)N + j] = jsr ? 0.0 : imm;
     S6[SP_CSQN * (size_t)N + j] = jsr ? imm : 0.0;
   }
@@ -691,6 +743,8 @@ void refresh_args(srs_sim* s) {
     s->a32.CS = cs;
     s->a32.counters = s->d_counters;
     s->a32.k = make_consts32(s);
+    s->a32.CM = s->d_CM;
+    s->a32.CI = s->d_CI;
   } else {
     s->ar.P_ = s->P;
     s->ar.C = s->ch;
@@ -698,6 +752,8 @@ void refresh_args(srs_sim* s) {
     s->ar.k = make_consts32(s);
     s->ar.M = s->d_M[0];
     s->ar.I = s->d_I[0];
+    s->ar.CM = s->d_CM;
+    s->ar.CI = s->d_CI;
   }
   if (s->graph_plain) {
     cudaGraphExecDestroy(s->graph_plain);
@@ -773,9 +829,11 @@ int plain_steps(srs_sim* s, int64_t n) {
   return SRS_OK;
 }
 
-int resident_launch(srs_sim* s, int steps) {
+int resident_launch(srs_sim* s, int steps, int prestep_first = 0) {
   ResidentArgs a = s->ar;
   a.steps = steps;
+  a.prestep_first = prestep_first;
+  a.initial_row = prestep_first;
   int rc = launch_resident(a, s->C, s->n_clusters, s->threads, s->smem, s->st);
   s->launches++;
   if (rc) return fail(SRS_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -1038,6 +1096,7 @@ void srs_sim_destroy(srs_sim* s) {
   if (s->graph_plain) cudaGraphExecDestroy(s->graph_plain);
   if (s->st) cudaStreamSynchronize(s->st);
   for (void* p : s->allocs) cudaFree(p);
+  if (s->h_stage) cudaFreeHost(s->h_stage);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
 }
@@ -1058,6 +1117,12 @@ int srs_sim_get_config(const srs_sim* s, srs_sim_config* c) {
       s->d.engine == SRS_ENGINE_RESIDENT ? (s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000) : 1;
   c->smem_bytes = (int)s->smem;
   c->kernel_launches = s->launches;
+  const int64_t NE = (int64_t)eng_count(s);
+  const int64_t per_state = s->d.precision == SRS_FP64 ? (int64_t)6 * s->N * 8 : NE * 20;
+  c->ctl_bytes = (int64_t)s->R * (int64_t)sizeof(RealCtl);
+  c->reset_h2d_bytes = (int64_t)s->R * (per_state + (int64_t)(s->NR + 2 * s->NL) * 4 +
+                                         (int64_t)s->NCH * 8) + c->ctl_bytes;
+  c->engine_elements = NE;
   return SRS_OK;
 }
 
@@ -1133,7 +1198,7 @@ int srs_sim_reset(srs_sim* s) {
     for (int i = 0; i < NR; ++i) n_open += ry[i];
     c.n_open_tick = n_open;
   }
-  for (int r = 0; r < s->R; ++r) SRS_TRY(upload_state(s, r, S6.data()));
+  SRS_TRY(upload_state_range(s, 0, s->R, S6.data()));
   SRS_CUDA(cudaMemcpy(s->d_ryr, ryr.data(), ryr.size() * 4, cudaMemcpyHostToDevice));
   SRS_CUDA(cudaMemcpy(s->d_lcc, lcc.data(), lcc.size() * 4, cudaMemcpyHostToDevice));
   SRS_CUDA(cudaMemcpy(s->d_lccv, lccv.data(), lccv.size() * 4, cudaMemcpyHostToDevice));
@@ -1259,28 +1324,12 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
       if (all) break;
     }
   } else {
-    // t = 0 row for every realization, written on the host from the initial
-    // state (identical to the device row code's inputs)
-    std::vector<float> row0((size_t)s->R * s->P.row_w);
-    std::vector<int32_t> ryr((size_t)s->R * s->NR), lcc((size_t)s->R * s->NL), lccv((size_t)s->R * s->NL);
-    SRS_CUDA(cudaMemcpy(ryr.data(), s->d_ryr, ryr.size() * 4, cudaMemcpyDeviceToHost));
-    SRS_CUDA(cudaMemcpy(lcc.data(), s->d_lcc, lcc.size() * 4, cudaMemcpyDeviceToHost));
-    SRS_CUDA(cudaMemcpy(lccv.data(), s->d_lccv, lccv.size() * 4, cudaMemcpyDeviceToHost));
-    SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
-    std::vector<double> S6((size_t)6 * s->N);
-    for (int r = 0; r < s->R; ++r) {
-      SRS_TRY(download_state(s, r, S6.data()));
-      states_row(s->m, s->p, S6.data(), &ryr[(size_t)r * s->NR], &lcc[(size_t)r * s->NL],
-                 &lccv[(size_t)r * s->NL], s->P.Vm[ctl[r].vsel], ctl[r].t,
-                 &row0[(size_t)r * s->P.row_w], s->P.row_w);
-      SRS_CUDA(cudaMemcpy(s->d_rows + (size_t)r * s->P.row_cap * s->P.row_w, &row0[(size_t)r * s->P.row_w],
-                          s->P.row_w * sizeof(float), cudaMemcpyHostToDevice));
-      ctl[r].n_rows = 1;
-    }
-    SRS_CUDA(cudaMemcpy(s->d_ctl, ctl.data(), sizeof(RealCtl) * s->R, cudaMemcpyHostToDevice));
+    // the first launch writes the t = 0 row and runs the protocol of step 0
     const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
+    int first = 1;
     while (true) {
-      SRS_TRY(resident_launch(s, S));
+      SRS_TRY(resident_launch(s, S, first));
+      first = 0;
       SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
       bool all = true;
       for (auto& c : ctl) all &= c.done != 0;

@@ -67,6 +67,8 @@ struct Plain32Args {
   const float* I_in;
   float4* M_out;
   float* I_out;
+  float4* CM;  // [R][N] compensation of the Euler update (mobile species)
+  float* CI;   // [R][N] compensation (immobile buffer)
   Consts32 k;
   Protocol P;
   Channels C;
@@ -89,17 +91,20 @@ struct ResidentArgs {
   int32_t off_bits;
   int32_t steps;
   const TetRec* geo;
-  const int32_t* n_local;
-  const int32_t* n_chtet;
-  const int32_t* ch_ptr;
+  int32_t prestep_first;  // run the protocol of the first step before it
+  int32_t initial_row;    // ... and write the t = 0 states row
+  const int32_t* n_local; // [C] elements in each partition
+  const int32_t* n_chtet; // [1] channel elements (partition 0, offsets 0..n-1)
+  const int32_t* ch_ptr;  // [n_chtet+1] CSR of channel entries per channel element
   const ChanEntry32* ch_list;
-  int32_t ch_stride;
   const uint16_t* ryr_cleft_code;
   const uint16_t* ryr_jsr_code;
   const uint16_t* lcc_code;
   const float* lcc_rest;
-  float4* M;
+  float4* M;   // [R][C][P] state
   float* I;
+  float4* CM;  // [R][C][P] compensation
+  float* CI;
   Consts32 k;
   Protocol P_;
   Channels C;
@@ -109,5 +114,6 @@ size_t resident_smem_bytes(int P, int NR, int NL);
 int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
                     cudaStream_t st);
 int resident_max_clusters(int C, int threads, size_t smem);
+bool resident_cluster_supported(int C);
 
 }  // namespace srs

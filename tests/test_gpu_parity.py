@@ -3,6 +3,7 @@
 Bars:
   * FP64 plain engine: bit-exact with the oracle (PHILOX gating), and with the
     reference's own golden rows where no random numbers are involved;
+  * FP32 plain engine: bit-exact with the oracle's FP32 restatement (gating on);
   * FP32 resident engine: bit-exact with the FP32 plain engine (same per-element
     arithmetic), for every cluster size;
   * FP32 engines vs FP64: relative error <= 1e-5 on concentrations
@@ -105,6 +106,27 @@ def test_fp64_deterministic_run_equals_reference_golden(srs):
     rows, _, _ = sim.run_simulation()
     assert np.array_equal(rows[0], d["rows"])
     assert np.array_equal(sim.get_state(0)["states"], d["states"])
+
+
+def test_fp32_plain_bit_exact_with_fp32_oracle(srs, oracle):
+    p = golden_params(srs)
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [51, 52, 53]
+    sim = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    st0 = [sim.get_state(r) for r in range(len(seeds))]
+    n = 800
+    sim.explicit_step(n)
+    m = oracle_mesh(oracle, p)
+    for r, sd in enumerate(seeds):
+        s0 = st0[r]
+        st = m.to_fp32(s0["states"])
+        ryr, lcc, lccv, res = (s0["ryr"].copy(), s0["lcc"].copy(), s0["lccv"].copy(),
+                               s0["residuals"].copy())
+        m.steps_fp32(st, sd, 0, n, ryr, lcc, lccv, res, gating=True)
+        got = sim.get_state(r)
+        assert np.array_equal(got["states"], m.from_fp32(st))
+        assert np.array_equal(got["ryr"], ryr) and np.array_equal(got["residuals"], res)
+        assert np.array_equal(got["lcc"], lcc) and np.array_equal(got["lccv"], lccv)
 
 
 def test_fp32_plain_within_tolerance_of_fp64(srs):
