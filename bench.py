@@ -279,8 +279,11 @@ def run_ours(args):
     grid = srs.Grid(p, base)
     R, S = args.realizations, args.launch_steps
     seeds = [1 + rank * R + i for i in range(R)]
+    from srs_gb300 import tuner
+    tuned = tuner.tune_resident(grid, p, R, seeds=seeds)
     sim = srs.Simulation(grid, p, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
-                         steps_per_launch=S)
+                         steps_per_launch=S, cluster_size=tuned["cluster_size"],
+                         threads_per_cta=tuned["threads_per_cta"])
     cfg = sim.config()
     # warm-up launches
     for _ in range(args.warmup):
@@ -317,7 +320,8 @@ def run_ours(args):
     # end to end through the public API with host buffers
     pe = wl.default_spark_params(T_FINAL=(S - 0.5) * DT_MS, OUTPUT_STATES_INTERVAL=S * DT_MS / 4)
     sim_e = srs.Simulation(grid, pe, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
-                           steps_per_launch=S)
+                           steps_per_launch=S, cluster_size=tuned["cluster_size"],
+                           threads_per_cta=tuned["threads_per_cta"])
     cfg_e = sim_e.config()
     sim_e.run_simulation()  # warm
     barrier(dist)
@@ -351,6 +355,8 @@ def run_ours(args):
                 "engine": "resident", "cluster_size": cfg["cluster_size"],
                 "threads_per_cta": cfg["threads_per_cta"], "smem_bytes": cfg["smem_bytes"],
                 "l2": "inputs larger than L2 (212 MB state), no flush",
+                "tuner": {"trials": len(tuned["trials"]),
+                          "best_ms_per_step": tuned["ms_per_step"]},
                 "parallelism": "replicas x%d" % ws},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": cfg_e["reset_h2d_bytes"],
                     "d2h_bytes_per_step": d2h,

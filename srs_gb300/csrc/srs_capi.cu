@@ -1060,7 +1060,7 @@ int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* 
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        for (int c : {1, 2, 4, 8, 16}) {
+        for (int c : {1, 2, 3, 4, 5, 6, 8, 16}) {
           int Pm = (s->N + c - 1) / c;
           Pm = (Pm + 3) & ~3;
           if (resident_smem_bytes(Pm, s->NR, s->NL) <= (size_t)optin) {

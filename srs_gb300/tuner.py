@@ -1,0 +1,68 @@
+"""Autotuner of the resident engine.
+
+Chooses the cluster size (CTAs sharing one realization), the threads per CTA
+and the time steps per persistent launch for a given grid and batch by timing
+short trial launches of each candidate on the device (CUDA events on the
+engine's stream).  Results are cached per (element count, channel count,
+realizations, device) in a JSON file next to the package, so later runs start
+with the tuned configuration.
+"""
+import json
+import os
+
+import srs_gb300 as srs
+
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tuned.json")
+
+
+def _key(grid, R):
+    try:
+        import torch
+        dev = torch.cuda.get_device_name(0)
+    except Exception:  # noqa: BLE001 - the name only labels the cache entry
+        dev = "cuda"
+    return "%s|N%d|R%d|L%d|B%d" % (dev, grid.n_ele, grid.n_ryr, grid.n_lcc, R)
+
+
+def tune_resident(grid, params, R, seeds=None, clusters=(1, 2, 3, 4, 5, 6, 8),
+                  threads=(512, 768, 1024), trial_steps=200, repeats=2, use_cache=True,
+                  verbose=False):
+    """Returns dict(cluster_size, threads_per_cta, ms_per_step, trials)."""
+    key = _key(grid, R)
+    cache = {}
+    if use_cache and os.path.exists(CACHE):
+        try:
+            cache = json.load(open(CACHE))
+        except ValueError:
+            cache = {}
+        if key in cache:
+            return cache[key]
+    trials = []
+    for C in clusters:
+        for T in threads:
+            try:
+                sim = srs.Simulation(grid, params, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                                     threads_per_cta=T, cluster_size=C,
+                                     steps_per_launch=trial_steps)
+            except srs.SrsError as e:
+                if verbose:
+                    print("tuner: C=%d T=%d skipped (%s)" % (C, T, e))
+                continue
+            sim.advance_async(trial_steps)
+            sim.synchronize()
+            ms = min(sim.time_advance(trial_steps) for _ in range(repeats))
+            trials.append(dict(cluster_size=C, threads_per_cta=T, ms_per_step=ms / trial_steps))
+            if verbose:
+                print("tuner: C=%d T=%d %.4f ms/step" % (C, T, ms / trial_steps))
+            del sim
+    if not trials:
+        raise RuntimeError("no resident configuration fits this grid")
+    best = min(trials, key=lambda d: d["ms_per_step"])
+    out = dict(best, trials=trials)
+    if use_cache:
+        cache[key] = out
+        try:
+            json.dump(cache, open(CACHE, "w"), indent=1)
+        except OSError:
+            pass
+    return out
