@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-tune", action="store_true", help="use the default configuration")
     return ap.parse_args()
 
 
@@ -280,7 +282,10 @@ def run_ours(args):
     R, S = args.realizations, args.launch_steps
     seeds = [1 + rank * R + i for i in range(R)]
     from srs_gb300 import tuner
-    tuned = tuner.tune_resident(grid, p, R, seeds=seeds)
+    if args.no_tune:
+        tuned = dict(cluster_size=0, threads_per_cta=0, ms_per_step=None, trials=[])
+    else:
+        tuned = tuner.tune_resident(grid, p, R, seeds=seeds)
     sim = srs.Simulation(grid, p, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
                          steps_per_launch=S, cluster_size=tuned["cluster_size"],
                          threads_per_cta=tuned["threads_per_cta"])
@@ -318,25 +323,31 @@ def run_ours(args):
                     % peak_kind}
 
     # end to end through the public API with host buffers
-    pe = wl.default_spark_params(T_FINAL=(S - 0.5) * DT_MS, OUTPUT_STATES_INTERVAL=S * DT_MS / 4)
-    sim_e = srs.Simulation(grid, pe, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
-                           steps_per_launch=S, cluster_size=tuned["cluster_size"],
-                           threads_per_cta=tuned["threads_per_cta"])
-    cfg_e = sim_e.config()
-    sim_e.run_simulation()  # warm
-    barrier(dist)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rows_bytes = 0
-    for _ in range(args.e2e_steps):
-        sim_e.reset()
-        rows, t_end, n_steps = sim_e.run_simulation()
-        rows_bytes = sum(r.nbytes for r in rows)
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.e2e_steps)
-    e2e_val = ws * R * S * DT_MS / e2e_s
-    row_cap = int(pe.reals[0] / pe.reals[2]) + 8
-    d2h = R * row_cap * sim_e.row_width() * 4 + 2 * cfg_e["ctl_bytes"]
+    e2e = None
+    if not args.no_e2e:
+        pe = wl.default_spark_params(T_FINAL=(S - 0.5) * DT_MS, OUTPUT_STATES_INTERVAL=S * DT_MS / 4)
+        sim_e = srs.Simulation(grid, pe, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                               steps_per_launch=S, cluster_size=tuned["cluster_size"],
+                               threads_per_cta=tuned["threads_per_cta"])
+        cfg_e = sim_e.config()
+        sim_e.run_simulation()  # warm
+        barrier(dist)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rows_bytes = 0
+        for _ in range(args.e2e_steps):
+            sim_e.reset()
+            rows, t_end, n_steps = sim_e.run_simulation()
+            rows_bytes = sum(r.nbytes for r in rows)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.e2e_steps)
+        e2e_val = ws * R * S * DT_MS / e2e_s
+        row_cap = int(pe.reals[0] / pe.reals[2]) + 8
+        d2h = R * row_cap * sim_e.row_width() * 4 + 2 * cfg_e["ctl_bytes"]
+
+        e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": cfg_e["reset_h2d_bytes"],
+               "d2h_bytes_per_step": d2h,
+               "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)" % (S, rows_bytes)}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -358,10 +369,7 @@ def run_ours(args):
                 "tuner": {"trials": len(tuned["trials"]),
                           "best_ms_per_step": tuned["ms_per_step"]},
                 "parallelism": "replicas x%d" % ws},
-            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": cfg_e["reset_h2d_bytes"],
-                    "d2h_bytes_per_step": d2h,
-                    "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)"
-                            % (S, rows_bytes)},
+            "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,
