@@ -199,6 +199,65 @@ void srs_box_mesh_default(srs_box_mesh_spec* spec);
 int srs_box_mesh_write(const srs_box_mesh_spec* spec, const char* base, int* report_ints,
                        double* report_max_a0);
 
+/* ---- allocation-free step ---------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory — a framework that owns every allocation through its own pool, code
+ * running while a stream is captured into a CUDA graph, a real-time loop that
+ * must not touch the allocator — srs_explicit_step_fp64_noalloc performs one
+ * ExplicitStep (cpu/RunSimulation.cpp:591-654, FP64, reference operation
+ * order, followed by gating unless `nogating`) for up to
+ * SRS_NOALLOC_MAX_REALIZATIONS realizations, reading states_in and writing
+ * states_out, with every array a device buffer owned by the caller.  It calls
+ * no cudaMalloc/cudaFree.  Its only other device memory is a fixed array
+ * compiled into the library (per GPU, held until the process exits, about
+ * 22 KB), shared by all calls and reused without reallocation: each call
+ * clears it first, and calls whose work overlaps on the GPU race on it, so
+ * serialise them.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Arrays use the reference numbering and the layouts returned by
+ * srs_grid_get_operator / srs_grid_get_elements / srs_grid_get_channels:
+ *   aij[5N], nij[4N]; br4[4N] = boundary rates of Ca, ATP, CMDN, dye;
+ *   bhi[N] = TTArea*B_TOT_SL_HI/(V0*1e-15), blo[N] the same with B_TOT_SL_LO;
+ *   flags[N]: bit0 JSR, bit1 troponin C, bit2 element has channel entries;
+ *   chan_ptr[N+1], chan_list[2*nnz] = (kind, channel) per entry, RyRs in
+ *   index order (kind 0 cleft side, 1 JSR side) then LCCs (kind 2);
+ *   states_in/out[R][6N]; ryr_states[R][NR], lcc/lccv_states[R][NL],
+ *   residuals[R][NR+NL] updated in place.  `reals` (ParamStruct::Reals) and
+ *   `seeds` (Philox key per realization) are host arrays; `step` is the time
+ *   step index that keys the draws; `status` (optional, device) receives bit
+ *   0 on a non-finite value; `stream` is a cudaStream_t (NULL: default). */
+#define SRS_NOALLOC_MAX_REALIZATIONS 256
+typedef struct srs_noalloc_step {
+  int n_ele, n_realizations, n_ryr, n_lcc;
+  const double* aij;
+  const int* nij;
+  const double* br4;
+  const double* v0;
+  const double* bhi;
+  const double* blo;
+  const int* flags;
+  const int* chan_ptr;
+  const int* chan_list;
+  const int* ryr_ele;
+  const int* ryr_jsr;
+  const int* ryr_nb;
+  const int* lcc_ele;
+  const double* states_in;
+  double* states_out;
+  int* ryr_states;
+  int* lcc_states;
+  int* lccv_states;
+  double* residuals;
+  unsigned int* status;
+  const double* reals;
+  const uint64_t* seeds;
+  int64_t step;
+  double v_m, ca_nsr;
+  int nogating;
+  void* stream;
+} srs_noalloc_step;
+int srs_explicit_step_fp64_noalloc(const srs_noalloc_step* d);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,6 +111,21 @@ class BoxMeshSpec(C.Structure):
                 ("lcc_half", C.c_double), ("lcc_seed", C.c_uint64), ("seed", C.c_uint64)]
 
 
+NOALLOC_MAX_REALIZATIONS = 256
+
+
+class NoallocStep(C.Structure):
+    """srs_noalloc_step: one FP64 ExplicitStep on caller-owned device buffers."""
+    _fields_ = [("n_ele", C.c_int), ("n_realizations", C.c_int), ("n_ryr", C.c_int),
+                ("n_lcc", C.c_int)] + [
+        (n, C.c_void_p) for n in ("aij", "nij", "br4", "v0", "bhi", "blo", "flags", "chan_ptr",
+                                  "chan_list", "ryr_ele", "ryr_jsr", "ryr_nb", "lcc_ele",
+                                  "states_in", "states_out", "ryr_states", "lcc_states",
+                                  "lccv_states", "residuals", "status", "reals", "seeds")] + [
+        ("step", C.c_int64), ("v_m", C.c_double), ("ca_nsr", C.c_double), ("nogating", C.c_int),
+        ("stream", C.c_void_p)]
+
+
 # Every symbol declared in include/srs_gb300.h with its ctypes signature.
 _P = C.c_void_p
 _SIGS = {
@@ -143,6 +158,7 @@ _SIGS = {
     "srs_write_grid_vtk": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
     "srs_box_mesh_default": (None, [C.POINTER(BoxMeshSpec)]),
     "srs_box_mesh_write": (C.c_int, [C.POINTER(BoxMeshSpec), C.c_char_p, _P, _P]),
+    "srs_explicit_step_fp64_noalloc": (C.c_int, [C.POINTER(NoallocStep)]),
 }
 
 
@@ -172,6 +188,11 @@ def _ptr(a):
 
 def library():
     return _lib
+
+
+def explicit_step_fp64_noalloc(desc):
+    """srs_explicit_step_fp64_noalloc on a filled NoallocStep."""
+    _check(_lib.srs_explicit_step_fp64_noalloc(C.byref(desc)))
 
 
 def default_parameters():

@@ -30,6 +30,11 @@ int fail(int code, const std::string& msg) {
   } while (0)
 }  // namespace
 
+namespace srs {
+// Records an error for srs_last_error() from other translation units.
+int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace srs
+
 struct srs_grid {
   Mesh m;
   Operator op;
@@ -109,6 +114,9 @@ int dev_alloc(srs_sim* s, T** dst, size_t n) {
     if (rc_ != SRS_OK) return rc_; \
   } while (0)
 
+}  // namespace
+
+namespace srs {
 // Gating and flux constants for membrane potential V (cpu/RunSimulation.cpp:
 // 149-161, 185-197, 239-375), evaluated in double precision on the host.
 void gate_consts(const srs_params& p, double V, srs_gate_consts* g) {
@@ -149,6 +157,10 @@ void lcc_flux_consts(const srs_params& p, double V, double* A, double* E, double
   *Em1 = std::exp(2 * V * F_over_RT) - 1;
   *B = 0.34 * p.reals[R_CA_0];
 }
+
+}  // namespace srs
+
+namespace {
 
 void fill_protocol_consts(srs_sim* s) {
   Protocol& P = s->P;

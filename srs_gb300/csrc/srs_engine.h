@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "../../include/srs_gb300.h"
 #include "srs_sim.cuh"
 
 namespace srs {
@@ -110,6 +111,12 @@ struct ResidentArgs {
   Channels C;
   ChanState CS;
 };
+// Host-side constants (double precision, from the parameter set and the
+// membrane potential V): gating rates and the LCC flux terms.
+void gate_consts(const srs_params& p, double V, srs_gate_consts* g);
+void lcc_flux_consts(const srs_params& p, double V, double* A, double* E, double* Em1, double* B,
+                     double* Vg);
+
 size_t resident_smem_bytes(int P, int NR, int NL);
 int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
                     cudaStream_t st);
