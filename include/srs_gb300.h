@@ -170,6 +170,31 @@ typedef struct srs_sim_config {
 } srs_sim_config;
 int srs_sim_get_config(const srs_sim* s, srs_sim_config* c);
 
+/* ---- line scan (linescan/main.cpp:160-225) --------------------------------
+ * PSF-weighted bound-dye fluorescence at sample points on a line, from the
+ * current state of every realization:
+ *   F_i = sum_j V0_j [CaDye]_j N(r_ij; sigma) + padding voxels at f0_pad,
+ * restricted to |r_ij|^2 < r_thresh.  axis 0/1/2 scans x/y/z; the line
+ * passes through (offset1, offset2) in the other two coordinates in the
+ * reference's convention (X: (y,z) = (o1,o2); Y: (x,z) = (o1,o2);
+ * Z: (x,y) = (o1,o2), with the PSF variances rotated as the reference does).
+ * Samples sit at x_min + i*res for i < (int)((x_max - x_min)/res).  Padding
+ * voxels of edge pad_res fill [pad_min, pad_max]^3 outside `domain`
+ * (xmin, xmax, ymin, ymax, zmin, zmax). */
+typedef struct srs_linescan_desc {
+  int axis;
+  double offset1, offset2;
+  double x_min, x_max, res;
+  double var_x, var_y, var_z;
+  double r_thresh;
+  double f0_pad, pad_res, pad_min, pad_max;
+  double domain[6];
+} srs_linescan_desc;
+int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples);
+/* out[R][n_samples]: F of every realization now; rest[n_samples] (optional):
+ * F of the equilibrium state (for dF/F0). */
+int srs_linescan(srs_sim* s, double* out, double* rest);
+
 /* ---- output formats (cpu/OutputFuncs.cpp) -------------------------------- */
 /* WriteToGridFiles (cpu/OutputFuncs.cpp:42-220): legacy ASCII VTK of the
  * current state of realization r at time t. */

@@ -111,6 +111,15 @@ class BoxMeshSpec(C.Structure):
                 ("lcc_half", C.c_double), ("lcc_seed", C.c_uint64), ("seed", C.c_uint64)]
 
 
+class LinescanDesc(C.Structure):
+    """srs_linescan_desc (linescan/main.cpp:160-225)."""
+    _fields_ = [("axis", C.c_int), ("offset1", C.c_double), ("offset2", C.c_double),
+                ("x_min", C.c_double), ("x_max", C.c_double), ("res", C.c_double),
+                ("var_x", C.c_double), ("var_y", C.c_double), ("var_z", C.c_double),
+                ("r_thresh", C.c_double), ("f0_pad", C.c_double), ("pad_res", C.c_double),
+                ("pad_min", C.c_double), ("pad_max", C.c_double), ("domain", C.c_double * 6)]
+
+
 NOALLOC_MAX_REALIZATIONS = 256
 
 
@@ -159,6 +168,8 @@ _SIGS = {
     "srs_box_mesh_default": (None, [C.POINTER(BoxMeshSpec)]),
     "srs_box_mesh_write": (C.c_int, [C.POINTER(BoxMeshSpec), C.c_char_p, _P, _P]),
     "srs_explicit_step_fp64_noalloc": (C.c_int, [C.POINTER(NoallocStep)]),
+    "srs_linescan_setup": (C.c_int, [_P, C.POINTER(LinescanDesc), C.POINTER(C.c_int)]),
+    "srs_linescan": (C.c_int, [_P, _P, _P]),
 }
 
 
@@ -364,6 +375,27 @@ class Simulation:
                          n_steps.ctypes.data_as(C.POINTER(C.c_int64)))
         _check(_lib.srs_run_simulation(self._h, C.byref(out)))
         return [rows[r, :n_rows[r]].copy() for r in range(self.R)], t_end, n_steps
+
+    def linescan_setup(self, **kw):
+        """Line scan along an axis (see srs_linescan_desc); returns sample count."""
+        d = LinescanDesc()
+        for k, v in kw.items():
+            if k == "domain":
+                for i, x in enumerate(v):
+                    d.domain[i] = float(x)
+            else:
+                setattr(d, k, v)
+        n = C.c_int()
+        _check(_lib.srs_linescan_setup(self._h, C.byref(d), C.byref(n)))
+        self._ls_n = n.value
+        return n.value
+
+    def linescan(self):
+        """(F[R][n_samples], F_rest[n_samples]) of the current state."""
+        out = np.zeros((self.R, self._ls_n))
+        rest = np.zeros(self._ls_n)
+        _check(_lib.srs_linescan(self._h, _ptr(out), _ptr(rest)))
+        return out, rest
 
     def write_grid_vtk(self, r, path, run=0, rank=0, n=0, t=0.0):
         _check(_lib.srs_write_grid_vtk(self._h, r, str(path).encode(), run, rank, n, float(t)))

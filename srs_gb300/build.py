@@ -41,6 +41,7 @@ def _units():
         ("k_fp32.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_fp32.cu")]),
         ("srs_capi.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "srs_capi.cu")]),
         ("k_noalloc.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_noalloc.cu")]),
+        ("k_linescan.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_linescan.cu")]),
         ("srs_host.o", common_cc + ["-c", os.path.join(CSRC, "srs_host.cpp")]),
         ("meshgen.o", common_cc + ["-c", os.path.join(CSRC, "meshgen.cpp")]),
     ]

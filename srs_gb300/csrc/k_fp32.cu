@@ -387,7 +387,7 @@ __device__ void resident_prestep(const ResidentArgs& a, RealCtl& ctl, const floa
 }
 
 template <int C>
-__global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
+__global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int P = a.P;
   float4* buf0 = reinterpret_cast<float4*>(smem);
@@ -405,6 +405,12 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
   float* s_jl = s_jr + NR;
   double* s_res = reinterpret_cast<double*>(
       (reinterpret_cast<uintptr_t>(s_jl + NL) + 7) & ~(uintptr_t)7);
+  // channel-entry CSR of partition 0, staged once per launch
+  int32_t* s_cptr = reinterpret_cast<int32_t*>(s_res + NCH);
+  ChanEntry32* s_clist = reinterpret_cast<ChanEntry32*>(
+      (reinterpret_cast<uintptr_t>(s_cptr + a.n_chtet[0] + 1) + 15) & ~(uintptr_t)15);
+  (void)s_jr;
+  (void)s_jl;
 
   uint32_t rank = 0;
   if constexpr (C > 1) {
@@ -422,9 +428,11 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
   const uint32_t off_mask = (1u << a.off_bits) - 1u;
   const Consts32& k = a.k;
   const Protocol& P_ = a.P_;
-  // regular elements: rank 0 leaves warp 0 to the channel work
-  const int t0 = (rank == 0) ? tid - 32 : tid;
-  const int tstride = (rank == 0) ? nthr - 32 : nthr;
+  if (rank == 0) {
+    const int nnz = a.ch_ptr[n_ch];
+    for (int i = tid; i <= n_ch; i += nthr) s_cptr[i] = a.ch_ptr[i];
+    for (int i = tid; i < nnz; i += nthr) s_clist[i] = a.ch_list[i];
+  }
 
   if (tid < 32) {
     for (int q = lane; q < C; q += 32) {
@@ -472,68 +480,37 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
         const float4* src = cur ? buf1 : buf0;
         float4* dst = cur ? buf0 : buf1;
         const uint32_t* bs = tail->base[cur];
-        if (chan_warp) {
-          // ---- channel work: flux, channel elements, gating, next protocol --
-          RealCtl& ctl = tail->ctl;
+        // ---- every element of this partition; the elements that carry
+        // channels (head of partition 0) add the release flux of their
+        // channels, computed from the state of this step ----------------
+        {
+          const RealCtl& ctl = tail->ctl;
           const int v = ctl.vsel;
-          for (int i = lane; i < NR; i += 32) {
-            float J = 0.0f;
-            if (s_ryr[i]) {
-              float us = src[a.ryr_cleft_code[i] & off_mask].x;
-              float uj = src[a.ryr_jsr_code[i] & off_mask].x;
-              J = k.jr_scale * ((k.dc0 + uj) - us);
-            }
-            s_jr[i] = J;
-          }
-          for (int i = lane; i < NL; i += 32) {
-            float J = 0.0f;
-            if ((s_lcc[i] == 6 || s_lcc[i] == 12) && s_lccv[i] == 2) {
-              float c = a.lcc_rest[i] + src[a.lcc_code[i] & off_mask].x;
-              J = k.lccA[v] * fmaf(c, k.lccE[v], -k.lccB);
-            }
-            s_jl[i] = J;
-          }
-          __syncwarp();
-          for (int i = lane; i < n_ch; i += 32) {
-            const TetRec g = geo[i];
-            float flux = 0.0f;
-            for (int q = a.ch_ptr[i]; q < a.ch_ptr[i + 1]; ++q) {
-              ChanEntry32 e = a.ch_list[q];
-              float J = (e.kind < 2) ? s_jr[e.ch] : s_jl[e.ch];
-              flux = fmaf(J, e.s, flux);
-            }
-            float4 nv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) nv[q] = resident_nb<C>(bs, src, g.nb[q], a.off_bits, off_mask);
-            float4 out, cm = cmb[i];
-            float imo, ci = cib[i];
-            tet_update(k, src[i], immb[i], nv[0], nv[1], nv[2], nv[3],
-                       make_float4(g.a[0], g.a[1], g.a[2], g.a[3]), g.flags, g.bsl, 0.0f, flux,
-                       cm, ci, &out, &imo);
-            dst[i] = out;
-            immb[i] = imo;
-            cmb[i] = cm;
-            cib[i] = ci;
-            bad |= !isfinite(out.x);
-          }
-          __syncwarp();
-          // gating after this step reads the channel elements just written
-          if (!P_.nogating) resident_gate(a, ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
-          if (lane == 0) {
-            ctl.step += 1;
-            ctl.t += P_.dt;
-          }
-          __syncwarp();
-          resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane);
-          if (lane == 0) tail->done_flag[s & 1] = ctl.done;
-        } else {
-          // ---- all other elements ------------------------------------------
-          for (int i = n_ch + t0; i < n_loc; i += tstride) {
+          for (int i = tid; i < n_loc; i += nthr) {
             const float4* gp = reinterpret_cast<const float4*>(geo + i);
             float4 ga = __ldg(gp);
             float4 gb = __ldg(gp + 1);
             uint32_t w0 = __float_as_uint(gb.x), w1 = __float_as_uint(gb.y);
             uint32_t c0 = w0 & 0xffffu, c1 = w0 >> 16, c2 = w1 & 0xffffu, c3 = w1 >> 16;
+            const uint32_t fl = __float_as_uint(gb.w);
+            float flux = 0.0f;
+            if (i < n_ch) {
+              for (int q = s_cptr[i]; q < s_cptr[i + 1]; ++q) {
+                ChanEntry32 e = s_clist[q];
+                float J = 0.0f;
+                if (e.kind < 2) {
+                  if (s_ryr[e.ch]) {
+                    float us = src[a.ryr_cleft_code[e.ch] & off_mask].x;
+                    float uj = src[a.ryr_jsr_code[e.ch] & off_mask].x;
+                    J = k.jr_scale * ((k.dc0 + uj) - us);
+                  }
+                } else if ((s_lcc[e.ch] == 6 || s_lcc[e.ch] == 12) && s_lccv[e.ch] == 2) {
+                  float c = a.lcc_rest[e.ch] + src[i].x;
+                  J = k.lccA[v] * fmaf(c, k.lccE[v], -k.lccB);
+                }
+                flux = fmaf(J, e.s, flux);
+              }
+            }
             float4 n0, n1, n2, n3;
             if constexpr (C == 1) {
               n0 = ld_smem_f4(bs[0] + c0 * 16u);
@@ -548,13 +525,28 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
             }
             float4 out, cm = cmb[i];
             float imo, ci = cib[i];
-            tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, __float_as_uint(gb.w), gb.z, 0.0f,
-                       0.0f, cm, ci, &out, &imo);
+            tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci, &out,
+                       &imo);
             dst[i] = out;
             immb[i] = imo;
             cmb[i] = cm;
             cib[i] = ci;
             bad |= !isfinite(out.x);
+          }
+        }
+        if (rank == 0) {
+          __syncthreads();  // every channel element of this step is written
+          if (chan_warp) {
+            // ---- gating of this step and protocol of the next ----------------
+            RealCtl& ctl = tail->ctl;
+            if (!P_.nogating) resident_gate(a, ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
+            if (lane == 0) {
+              ctl.step += 1;
+              ctl.t += P_.dt;
+            }
+            __syncwarp();
+            resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane);
+            if (lane == 0) tail->done_flag[s & 1] = ctl.done;
           }
         }
         step_barrier<C>();
@@ -592,13 +584,16 @@ __global__ void __launch_bounds__(1024, 1) k_resident32(ResidentArgs a) {
   step_barrier<C>();  // no CTA leaves while others may read its shared memory
 }
 
-size_t resident_smem_bytes(int P, int NR, int NL) {
+size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries) {
   size_t b = (size_t)P * (3 * sizeof(float4) + 2 * sizeof(float));
   b += sizeof(ResidentSmemTail);
   b += (size_t)(NR + 2 * NL + NR) * sizeof(int32_t);
   b += (size_t)(NR + NL) * sizeof(float);
   b = (b + 7) & ~(size_t)7;
   b += (size_t)(NR + NL) * sizeof(double);
+  b += (size_t)(n_chtet + 1) * sizeof(int32_t);
+  b = (b + 15) & ~(size_t)15;
+  b += (size_t)n_entries * sizeof(ChanEntry32);
   return b;
 }
 

@@ -85,6 +85,10 @@ struct srs_sim {
   int graph_plain_len = 0;
   void* h_stage = nullptr;  // pinned host staging for state uploads
   size_t h_stage_bytes = 0;
+  // line scan
+  LinescanArgs ls{};
+  std::vector<double> ls_rest;  // F at the equilibrium state
+  double* d_ls_out = nullptr;
 };
 
 namespace {
@@ -592,7 +596,7 @@ int setup_resident(srs_sim* s, int C, int threads) {
   if (!resident_cluster_supported(C)) return fail(SRS_ERR_UNSUPPORTED, "unsupported cluster size");
   s->C = C;
   s->threads = threads;
-  s->smem = resident_smem_bytes(s->P_stride, s->NR, s->NL);
+  s->smem = resident_smem_bytes(s->P_stride, s->NR, s->NL, s->part_nch[0], 2 * s->NR + s->NL);
   int maxc = resident_max_clusters(C, threads, s->smem);
   if (maxc <= 0) return fail(SRS_ERR_UNSUPPORTED, "resident configuration does not fit on the device");
   s->n_clusters = std::min(maxc, s->R);
@@ -1066,7 +1070,9 @@ int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* 
     else if (d->engine == SRS_ENGINE_PLAIN) rc = setup_plain32(s);
     else {
       // resident: smallest cluster whose partition fits in shared memory
-      int threads = d->threads_per_cta > 0 ? d->threads_per_cta : 1024;
+      int threads = d->threads_per_cta > 0 ? d->threads_per_cta : 512;
+      if (threads > 768 || threads % 32)
+        rc = fail(SRS_ERR_INPUT, "resident engine: threads_per_cta must be a multiple of 32, <= 768");
       int C = d->cluster_size;
       if (C <= 0) {
         int dev = 0, optin = 0;
@@ -1075,7 +1081,8 @@ int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* 
         for (int c : {1, 2, 3, 4, 5, 6, 8, 16}) {
           int Pm = (s->N + c - 1) / c;
           Pm = (Pm + 3) & ~3;
-          if (resident_smem_bytes(Pm, s->NR, s->NL) <= (size_t)optin) {
+          if (resident_smem_bytes(Pm, s->NR, s->NL, 2 * s->NR + s->NL, 2 * s->NR + s->NL) <=
+              (size_t)optin) {
             C = c;
             break;
           }
@@ -1366,6 +1373,140 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
   refresh_args(s);
   if (st_bits & 1) return fail(SRS_ERR_NONFINITE, "a realization produced a non-finite Ca value");
   if (st_bits & 4) return fail(SRS_ERR_INPUT, "row_capacity too small for the run");
+  return SRS_OK;
+}
+
+int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
+  if (!s || !d || d->res <= 0 || d->r_thresh <= 0) return fail(SRS_ERR_INPUT, "bad line-scan description");
+  // linescan/main.cpp:160-190: line position and PSF widths by scan axis
+  double sx = std::sqrt(d->var_x), sy = std::sqrt(d->var_y), sz = std::sqrt(d->var_z);
+  if (d->axis == 2) {
+    sx = std::sqrt(d->var_z);
+    sy = std::sqrt(d->var_x);
+    sz = std::sqrt(d->var_y);
+  } else if (d->axis != 0 && d->axis != 1) {
+    return fail(SRS_ERR_INPUT, "axis must be 0, 1 or 2");
+  }
+  const int ns = (int)((d->x_max - d->x_min) / d->res);
+  if (ns <= 0) return fail(SRS_ERR_INPUT, "no line-scan samples");
+  const double alpha = 1.0 / std::pow(2 * 3.14159265358979323846, 1.5);
+  auto pdf = [&](double rx, double ry, double rz) {
+    return alpha * std::exp(-0.5 * ((rx * rx / (sx * sx)) + (ry * ry / (sy * sy)) + (rz * rz / (sz * sz)))) /
+           (sx * sy * sz);
+  };
+  auto center = [&](int i, double* c) {
+    double xi = d->x_min + i * d->res;
+    if (d->axis == 0) { c[0] = xi; c[1] = d->offset1; c[2] = d->offset2; }
+    else if (d->axis == 1) { c[0] = d->offset1; c[1] = xi; c[2] = d->offset2; }
+    else { c[0] = d->offset1; c[1] = d->offset2; c[2] = xi; }
+  };
+  // element centroids from the node file (linescan/main.cpp:95-110)
+  const Mesh& m = s->m;
+  std::vector<double> cx(m.N), cy(m.N), cz(m.N);
+  for (int j = 0; j < m.N; ++j) {
+    double x = 0, y = 0, z = 0;
+    for (int k = 0; k < 4; ++k) {
+      int v = m.ele_nodes[4 * (size_t)j + k];
+      x += m.node_x[v];
+      y += m.node_y[v];
+      z += m.node_z[v];
+    }
+    cx[j] = x / 4.0;
+    cy[j] = y / 4.0;
+    cz[j] = z / 4.0;
+  }
+  // padding voxels at the resting fluorescence (AddPointGrid, :275-313)
+  std::vector<double> px, py, pz, pv;
+  auto add_grid = [&](double x0, double x1, double y0, double y1, double z0, double z1) {
+    double dx = d->pad_res, dy = d->pad_res, dz = d->pad_res;
+    if (x0 > x1) dx = -dx;
+    if (y0 > y1) dy = -dy;
+    if (z0 > z1) dz = -dz;
+    int nx = (int)((x1 - x0) / dx), ny = (int)((y1 - y0) / dy), nz = (int)((z1 - z0) / dz);
+    for (int i = 0; i < nx; ++i)
+      for (int j = 0; j < ny; ++j)
+        for (int k = 0; k < nz; ++k) {
+          px.push_back(x0 + i * dx + 0.5 * dx);
+          py.push_back(y0 + j * dy + 0.5 * dy);
+          pz.push_back(z0 + k * dz + 0.5 * dz);
+          pv.push_back(std::fabs(dx * dy * dz));
+        }
+  };
+  if (d->pad_res > 0) {
+    const double* D = d->domain;
+    double a0 = d->pad_min, a1 = d->pad_max;
+    add_grid(a0, a1, a0, a1, D[5], a1);
+    add_grid(a0, a1, a0, a1, D[4], a0);
+    add_grid(D[0], a0, a0, a1, D[4], D[5]);
+    add_grid(D[1], a1, a0, a1, D[4], D[5]);
+    add_grid(D[0], D[1], D[2], a0, D[4], D[5]);
+    add_grid(D[0], D[1], D[3], a1, D[4], D[5]);
+  }
+  std::vector<int32_t> ptr(ns + 1, 0), col;
+  std::vector<double> w, pad(ns, 0.0);
+  s->ls_rest.assign(ns, 0.0);
+  std::vector<double> S6;
+  initial_states(m, s->p, &S6);
+  for (int i = 0; i < ns; ++i) {
+    double c[3];
+    center(i, c);
+    ptr[i] = (int32_t)col.size();
+    double rest = 0.0;
+    for (int j = 0; j < m.N; ++j) {
+      double rx = cx[j] - c[0], ry = cy[j] - c[1], rz = cz[j] - c[2];
+      if (rx * rx + ry * ry + rz * rz < d->r_thresh) {
+        double wj = m.V0[j] * pdf(rx, ry, rz);
+        col.push_back(s->eng_of_ref[j]);
+        w.push_back(wj);
+        rest += wj * S6[SP_DYE * (size_t)m.N + j];
+      }
+    }
+    double pd = 0.0;
+    for (size_t q = 0; q < px.size(); ++q) {
+      double rx = px[q] - c[0], ry = py[q] - c[1], rz = pz[q] - c[2];
+      if (rx * rx + ry * ry + rz * rz < d->r_thresh) pd += pv[q] * d->f0_pad * pdf(rx, ry, rz);
+    }
+    pad[i] = pd;
+    s->ls_rest[i] = pd + rest;
+  }
+  ptr[ns] = (int32_t)col.size();
+  LinescanArgs& a = s->ls;
+  a.n_samples = ns;
+  a.n_state = (int32_t)eng_count(s);
+  SRS_TRY(dev_upload(s, (int32_t**)&a.ptr, ptr.data(), ptr.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.col, col.data(), col.size()));
+  SRS_TRY(dev_upload(s, (double**)&a.w, w.data(), w.size()));
+  SRS_TRY(dev_upload(s, (double**)&a.pad, pad.data(), pad.size()));
+  if (s->d.precision != SRS_FP64) {
+    std::vector<double> rd(eng_count(s), 0.0);
+    for (size_t e = 0; e < rd.size(); ++e) {
+      int j = s->ref_of_eng[e];
+      if (j >= 0 && s->m.domain[j] == DOMAIN_CYTO) rd[e] = s->rv.dye;
+    }
+    SRS_TRY(dev_upload(s, (double**)&a.rest_dye, rd.data(), rd.size()));
+  }
+  SRS_TRY(dev_alloc(s, &s->d_ls_out, (size_t)s->R * ns));
+  a.out = s->d_ls_out;
+  if (n_samples) *n_samples = ns;
+  return SRS_OK;
+}
+
+int srs_linescan(srs_sim* s, double* out, double* rest) {
+  if (!s || !s->ls.ptr) return fail(SRS_ERR_STATE, "call srs_linescan_setup first");
+  LinescanArgs a = s->ls;
+  if (s->d.precision == SRS_FP64) {
+    a.S64 = s->d_S[0];
+  } else {
+    a.M = s->d_M[0];
+    a.CM = s->d_CM;
+  }
+  if (launch_linescan(a, s->R, s->st)) return fail(SRS_ERR_CUDA, "line-scan launch failed");
+  s->launches++;
+  if (out)
+    SRS_CUDA(cudaMemcpyAsync(out, s->d_ls_out, sizeof(double) * s->R * a.n_samples,
+                             cudaMemcpyDeviceToHost, s->st));
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  if (rest) std::memcpy(rest, s->ls_rest.data(), sizeof(double) * a.n_samples);
   return SRS_OK;
 }
 

@@ -111,13 +111,29 @@ struct ResidentArgs {
   Channels C;
   ChanState CS;
 };
+// Line scan: F[r][i] = pad[i] + sum_q w[q] * dye(col[q]) over ptr[i]..ptr[i+1].
+struct LinescanArgs {
+  int32_t n_samples;
+  int32_t n_state;       // elements per realization in the engine layout
+  const int32_t* ptr;    // [n_samples + 1]
+  const int32_t* col;    // engine element indices
+  const double* w;       // V0 * PSF weight
+  const double* pad;     // [n_samples] padding-voxel contribution
+  const double* S64;     // FP64 engine state [R][6][N] (or null)
+  const float4* M;       // FP32 engines: deviations [R][n_state]
+  const float4* CM;      //   and their compensation terms
+  const double* rest_dye;  // [n_state] resting bound dye per element
+  double* out;           // [R][n_samples]
+};
+int launch_linescan(const LinescanArgs& a, int R, cudaStream_t st);
+
 // Host-side constants (double precision, from the parameter set and the
 // membrane potential V): gating rates and the LCC flux terms.
 void gate_consts(const srs_params& p, double V, srs_gate_consts* g);
 void lcc_flux_consts(const srs_params& p, double V, double* A, double* E, double* Em1, double* B,
                      double* Vg);
 
-size_t resident_smem_bytes(int P, int NR, int NL);
+size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries);
 int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
                     cudaStream_t st);
 int resident_max_clusters(int C, int threads, size_t smem);
