@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-tune", action="store_true", help="use the default configuration")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost leg")
+    ap.add_argument("--adjoint-realizations", type=int, default=64)
+    ap.add_argument("--adjoint-steps", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -263,6 +266,47 @@ def run_reference(args):
     return 0
 
 
+def adjoint_cost(srs, grid, p, args):
+    """Cost of the pathwise adjoint against the forward pass it differentiates:
+    the config mesh x R realizations, n explicit steps with gating, the x
+    line scan through the cluster sampled every 128 steps, checkpoints every
+    256 steps; wall time of srs_adjoint (checkpointed forward, segment
+    recomputation with trajectory recording, reverse sweep) over wall time of
+    the same n steps of the resident engine."""
+    import numpy as np
+    import torch
+    Ra, n, te = args.adjoint_realizations, args.adjoint_steps, 128
+    from srs_gb300 import tuner
+    t = tuner.tune_resident(grid, p, Ra, seeds=list(range(1, Ra + 1)))
+    sim = srs.Simulation(grid, p, Ra, srs.FP32, srs.ENGINE_RESIDENT, seeds=list(range(1, Ra + 1)),
+                         cluster_size=t["cluster_size"], threads_per_cta=t["threads_per_cta"],
+                         steps_per_launch=256)
+    ns = sim.linescan_setup(axis=0, offset1=0.0, offset2=0.1, x_min=-1.0, x_max=1.0, res=0.05,
+                            var_x=0.0289, var_y=0.1154, var_z=0.0289, r_thresh=1.0, f0_pad=0.0,
+                            pad_res=0.0, pad_min=0.0, pad_max=0.0, domain=(0, 0, 0, 0, 0, 0))
+    sim.reset()
+    _, f0 = sim.linescan()
+    sim.adjoint(512, te, f0, checkpoint_every=256)  # warm-up: kernels, allocator
+    sim.reset()
+    sim.time_advance(512)
+    sim.reset()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.advance_async(n)
+    sim.synchronize()
+    fwd = time.perf_counter() - t0
+    sim.reset()
+    t0 = time.perf_counter()
+    loss, grad, _ = sim.adjoint(n, te, f0, checkpoint_every=256)
+    adj = time.perf_counter() - t0
+    if not np.isfinite(grad).all():
+        raise SystemExit("non-finite adjoint gradient")
+    return {"workload": "adjoint: config mesh x %d realizations, %d steps, line scan of %d samples "
+                        "every %d steps, checkpoints every 256" % (Ra, n, ns, te),
+            "cluster_size": sim.config()["cluster_size"], "forward_s": fwd, "adjoint_s": adj,
+            "cost_ratio": adj / fwd}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     dist = dist_init(ws)
@@ -349,6 +393,10 @@ def run_ours(args):
                "d2h_bytes_per_step": d2h,
                "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)" % (S, rows_bytes)}
 
+    adj = None
+    if rank == 0 and not args.no_adjoint:
+        adj = adjoint_cost(srs, grid, p, args)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, cores, kind, sample = cpu_sample(base, p, args.cpu_seconds)
@@ -374,6 +422,7 @@ def run_ours(args):
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "adjoint": adj,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -195,6 +195,63 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples);
  * F of the equilibrium state (for dF/F0). */
 int srs_linescan(srs_sim* s, double* out, double* rest);
 
+/* ---- pathwise adjoint -------------------------------------------------------
+ * No reference counterpart: the reference has no derivatives.  Gradient of a
+ * line-scan dF/F0 loss with respect to the parameters of the deterministic
+ * integrator (the diffusion / buffer / pump / release terms of
+ * cpu/RunSimulation.cpp:25-164), conditioned on the recorded gating
+ * trajectory (pathwise sensitivity: channel states are held at the values
+ * the forward run drew).
+ *
+ * From the current state, every realization runs n_steps explicit steps
+ * (the srs_explicit_step loop, no protocol events).  At the ticks
+ * k*tick_every (k = 1 .. n_steps/tick_every) the line scan of
+ * srs_linescan_setup gives F_ki, and
+ *   L_r = 1/2 sum_k sum_i (F_ki / f0_i - 1 - target_rki)^2.
+ * Returned: loss[r], grad[r][SRS_N_ADJ] = dL_r/dtheta (parameter order
+ * below, each the derivative with respect to that ParamStruct::Reals entry)
+ * and optionally grad_state[r][6][N] = dL_r/d(initial state), reference
+ * numbering and species order.  The state is checkpointed every
+ * checkpoint_every steps (0: 256) and each segment is recomputed once for
+ * the reverse sweep; the simulation is left at the state after n_steps.
+ * FP32 resident engine only (SRS_ERR_UNSUPPORTED otherwise). */
+#define SRS_N_ADJ 18
+enum {
+  SRS_ADJ_D_CA = 0,
+  SRS_ADJ_D_DYE = 1,
+  SRS_ADJ_K_ON_CMDN = 2,
+  SRS_ADJ_K_OFF_CMDN = 3,
+  SRS_ADJ_K_ON_TRPN = 4,
+  SRS_ADJ_K_OFF_TRPN = 5,
+  SRS_ADJ_K_ON_CSQN = 6,
+  SRS_ADJ_K_OFF_CSQN = 7,
+  SRS_ADJ_K_ON_DYE = 8,
+  SRS_ADJ_K_OFF_DYE = 9,
+  SRS_ADJ_V_RYR = 10,
+  SRS_ADJ_A_P = 11,
+  SRS_ADJ_B_TOT_SL = 12,
+  SRS_ADJ_K_D_SL = 13,
+  SRS_ADJ_D_ATP = 14,
+  SRS_ADJ_D_CMDN = 15,
+  SRS_ADJ_K_ON_ATP = 16,
+  SRS_ADJ_K_OFF_ATP = 17
+};
+typedef struct srs_adjoint_desc {
+  int64_t n_steps;
+  int tick_every;
+  int checkpoint_every;
+  const double* f0;      /* [n_samples] reference fluorescence F0 */
+  const double* target;  /* [R][n_steps/tick_every][n_samples], or NULL (zero) */
+} srs_adjoint_desc;
+typedef struct srs_adjoint_out {
+  double* loss;        /* [R] */
+  double* grad;        /* [R][SRS_N_ADJ] */
+  double* grad_state;  /* [R][6][N] or NULL */
+} srs_adjoint_out;
+/* ParamStruct::Reals index of each gradient entry. */
+int srs_adjoint_param_index(int k);
+int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out);
+
 /* ---- output formats (cpu/OutputFuncs.cpp) -------------------------------- */
 /* WriteToGridFiles (cpu/OutputFuncs.cpp:42-220): legacy ASCII VTK of the
  * current state of realization r at time t. */

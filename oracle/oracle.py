@@ -68,6 +68,11 @@ class Oracle:
         L.or_log.argtypes = [C.c_double]
         L.or_log.restype = C.c_double
         L.or_philox4x32_10.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
+        L.or_adjoint.argtypes = [vp] * 8 + [C.c_uint64, C.c_int64, C.c_int, C.c_int] + [vp] * 6
+        L.or_adjoint.restype = C.c_double
+        L.or_adjoint_loss.argtypes = [vp] * 8 + [C.c_uint64, C.c_int64, C.c_int, C.c_int] + [vp] * 4
+        L.or_adjoint_loss.restype = C.c_double
+        self.adj_params = np.ctypeslib.as_array((C.c_int * 18).in_dll(L, "or_adj_params")).copy()
 
 
 class Mesh:
@@ -145,6 +150,25 @@ class Mesh:
         self.o.lib.or_steps_fp32(self.h, _p(self.reals), _p(g), _p(st["U"]), _p(st["Im"]), _p(st["CM"]),
                                  _p(st["CI"]), C.c_uint64(seed), step0, n, _p(ryr), _p(lcc), _p(lccv),
                                  _p(res), int(gating))
+
+    def adjoint(self, ints, S0, ch, seed, n_steps, tick_every, W, pad, f0, target, grad=True,
+                grad_state=False):
+        """Pathwise adjoint (FP64): line-scan loss L and, if grad, dL/dtheta in
+        the order of Oracle.adj_params (and dL/dS0 [6][N] if grad_state).
+        ch: dict(ryr, lcc, lccv, residuals) of the initial channel state;
+        W: dense [n_samples][N] line-scan weights, pad: [n_samples];
+        target: [n_ticks][n_samples]."""
+        W = _f64(W)
+        args = [self.h, _p(_i32(ints)), _p(self.reals), _p(_f64(S0)), _p(_i32(ch["ryr"])),
+                _p(_i32(ch["lcc"])), _p(_i32(ch["lccv"])), _p(_f64(ch["residuals"])),
+                C.c_uint64(seed), int(n_steps), int(tick_every), W.shape[0], _p(W), _p(_f64(pad)),
+                _p(_f64(f0)), _p(_f64(target))]
+        if not grad:
+            return self.o.lib.or_adjoint_loss(*args), None
+        g = np.zeros(18)
+        lam0 = np.zeros(6 * self.N) if grad_state else None
+        L = self.o.lib.or_adjoint(*args, _p(g), _p(lam0))
+        return (L, g, lam0) if grad_state else (L, g)
 
     def gating_philox(self, V, ca, seed, step, ryr, lcc, lccv, res):
         self.o.lib.or_gating_philox(self.h, _p(self.reals), float(V), _p(_f64(ca)), C.c_uint64(seed),

@@ -1270,3 +1270,305 @@ void or_steps_fp32(const or_mesh* m, const double* R, const double* G, float* U,
   free(rest);
   free(ca);
 }
+
+/* ---- pathwise adjoint, FP64 (restatement used to check the GPU adjoint) ----
+ * Forward: n steps of ExplicitStep with PHILOX gating from the given state;
+ * the channel states of every step are recorded and the adjoint is taken
+ * with them held fixed (pathwise sensitivity).  Loss at ticks k*te
+ * (k = 1..n/te) of the bound-dye line scan F_i = pad_i + sum_j W_ij y_j:
+ *   L = 1/2 sum_k sum_i (F_ki / F0_i - 1 - target_ki)^2.
+ * Parameters (indices of ParamStruct::Reals) are listed in or_adj_params. */
+#define OR_N_ADJ 18
+const int or_adj_params[OR_N_ADJ] = {OR_D_CA, OR_D_DYE, OR_K_ON_CMDN, OR_K_OFF_CMDN,
+                                     OR_K_ON_TRPN, OR_K_OFF_TRPN, OR_K_ON_CSQN, OR_K_OFF_CSQN,
+                                     OR_K_ON_DYE, OR_K_OFF_DYE, OR_V_RYR, OR_A_P,
+                                     OR_B_TOT_SL_HI, OR_K_D_SL_HI, OR_D_ATP, OR_D_CMDN,
+                                     OR_K_ON_ATP, OR_K_OFF_ATP};
+
+static double tick_loss(const or_mesh* m, int ns, const double* W, const double* pad, const double* F0,
+                        const double* target, const double* S, double* dLdy) {
+  int N = m->N, i, j;
+  double L = 0;
+  for (i = 0; i < ns; ++i) {
+    double F = pad[i], e;
+    for (j = 0; j < N; ++j) F += W[(size_t)i * N + j] * S[S_DYE * N + j];
+    e = F / F0[i] - 1.0 - target[i];
+    L += 0.5 * e * e;
+    if (dLdy)
+      for (j = 0; j < N; ++j) dLdy[j] += e * W[(size_t)i * N + j] / F0[i];
+  }
+  return L;
+}
+
+/* one step of the transposed linearised dynamics: out += dt * J(x)^T lam,
+ * grad += dt * (dF/dtheta)(x)^T lam */
+static void adj_step(const or_mesh* m, const double* R, const double* G, const double* x, const int* ryr,
+                     const int* lcc, const int* lccv, const double* lam, double* out, double* grad) {
+  int N = m->N, j, k, i;
+  double dt = R[OR_T_STEP];
+  const double *c = x + S_CA * N, *yd = x + S_DYE * N, *at = x + S_ATP * N, *cm = x + S_CMDN * N;
+  const double *tr = x + S_TRPN * N, *cq = x + S_CSQN * N;
+  const double P_CaL = (9.13e-13) * (1e12) * (1e-3), F_over_RT = 96.5 / (310 * 8.314);
+  double V = G[0], A, E, Em1;
+  double* Bv = malloc(sizeof(double) * N);
+  double* Gv = malloc(sizeof(double) * N);
+  if (fabs(V) < 1e-6) V = 1e-6;
+  A = -P_CaL * V * (2 * F_over_RT);
+  E = exp(2 * V * F_over_RT);
+  Em1 = exp(2 * V * F_over_RT) - 1;
+  /* pre-buffer Ca rate G and buffer factor B of every element */
+  for (j = 0; j < N; ++j) {
+    double Kh = R[OR_K_D_SL_HI], Kl = R[OR_K_D_SL_LO];
+    double bhi = m->TT[j] * R[OR_B_TOT_SL_HI] / (m->V0[j] * (1e-15));
+    double blo = m->TT[j] * R[OR_B_TOT_SL_LO] / (m->V0[j] * (1e-15));
+    double g = R[OR_D_CA] * (m->aij[5 * j] * c[j]) + m->br[S_CA * N + j];
+    for (k = 0; k < 4; ++k) g += R[OR_D_CA] * m->aij[5 * j + 1 + k] * c[m->nij[4 * j + k]];
+    if (m->domain[j] == 0) {
+      if (m->tropc[j]) {
+        double Ki = c[j] / R[OR_K_D_i], Ksr = G[1] / R[OR_K_D_SR], Dc, vc;
+        Ki *= Ki;
+        Ksr *= Ksr;
+        Dc = 0.104217 + 17.923 * Ksr + Ki * (1.75583e6 + Ksr * 7.61673e6) + Ki * Ki * (6.08463e11 + Ksr * 4.50544e11);
+        vc = (Ki * Ki * 3.24873e12 + Ki * (9.17846e6 - 11478.2 * Ksr) - 0.329904 * Ksr) / Dc;
+        g -= R[OR_K_ON_TRPN] * (R[OR_B_TOT_TRPN] - tr[j]) * c[j] - R[OR_K_OFF_TRPN] * tr[j];
+        g -= 2e-3 * vc * R[OR_A_P];
+      }
+      g -= R[OR_K_ON_DYE] * (R[OR_B_TOT_DYE] - yd[j]) * c[j] - R[OR_K_OFF_DYE] * yd[j];
+      g -= R[OR_K_ON_ATP] * (R[OR_B_TOT_ATP] - at[j]) * c[j] - R[OR_K_OFF_ATP] * at[j];
+      g -= R[OR_K_ON_CMDN] * (R[OR_B_TOT_CMDN] - cm[j]) * c[j] - R[OR_K_OFF_CMDN] * cm[j];
+    } else {
+      g -= R[OR_K_ON_CSQN] * (R[OR_B_T_JSR] - cq[j]) * c[j] - R[OR_K_OFF_CSQN] * cq[j];
+      g += (G[1] - c[j]) * R[OR_V_REFILL];
+    }
+    Gv[j] = g;
+    Bv[j] = 1 + bhi * Kh / ((Kh + c[j]) * (Kh + c[j])) + blo * Kl / ((Kl + c[j]) * (Kl + c[j]));
+  }
+  for (i = 0; i < m->NR; ++i)
+    if (ryr[i]) {
+      double J = R[OR_V_RYR] * (c[m->ryr_jsr[i]] - c[m->ryr_ele[i]]) * R[OR_V_CELL];
+      Gv[m->ryr_ele[i]] += J / m->V0[m->ryr_ele[i]];
+      Gv[m->ryr_jsr[i]] -= J / m->V0[m->ryr_jsr[i]];
+    }
+  for (i = 0; i < m->NL; ++i)
+    if ((lcc[i] == 6 || lcc[i] == 12) && lccv[i] == 2) {
+      int e = m->lcc_ele[i];
+      Gv[e] += A * (c[e] * E - 0.34 * R[OR_CA_0]) / Em1 / m->V0[e];
+    }
+  /* rows of J, scattered into columns */
+  for (j = 0; j < N; ++j) {
+    double lc = lam[S_CA * N + j], B = Bv[j], w = lc / B;
+    double Kh = R[OR_K_D_SL_HI], Kl = R[OR_K_D_SL_LO];
+    double bhi = m->TT[j] * R[OR_B_TOT_SL_HI] / (m->V0[j] * (1e-15));
+    double blo = m->TT[j] * R[OR_B_TOT_SL_LO] / (m->V0[j] * (1e-15));
+    double dB = -2 * bhi * Kh / ((Kh + c[j]) * (Kh + c[j]) * (Kh + c[j])) -
+                2 * blo * Kl / ((Kl + c[j]) * (Kl + c[j]) * (Kl + c[j]));
+    double dGdc = R[OR_D_CA] * m->aij[5 * j];
+    int sp;
+    double Dsp[4] = {R[OR_D_DYE], R[OR_D_ATP], R[OR_D_CMDN], 0};
+    int sidx[3] = {S_DYE, S_ATP, S_CMDN};
+    /* Ca diffusion: d(G/B)/dc_k = D a_k / B */
+    for (k = 0; k < 4; ++k) out[S_CA * N + m->nij[4 * j + k]] += dt * R[OR_D_CA] * m->aij[5 * j + 1 + k] * w;
+    /* mobile buffers diffusion */
+    for (sp = 0; sp < 3; ++sp) {
+      double lb = lam[sidx[sp] * N + j];
+      out[sidx[sp] * N + j] += dt * Dsp[sp] * m->aij[5 * j] * lb;
+      for (k = 0; k < 4; ++k) out[sidx[sp] * N + m->nij[4 * j + k]] += dt * Dsp[sp] * m->aij[5 * j + 1 + k] * lb;
+    }
+    {
+      double Lc = m->aij[5 * j] * c[j], Ly = m->aij[5 * j] * yd[j];
+      double La = m->aij[5 * j] * at[j], Lm = m->aij[5 * j] * cm[j];
+      for (k = 0; k < 4; ++k) {
+        Lc += m->aij[5 * j + 1 + k] * c[m->nij[4 * j + k]];
+        Ly += m->aij[5 * j + 1 + k] * yd[m->nij[4 * j + k]];
+        La += m->aij[5 * j + 1 + k] * at[m->nij[4 * j + k]];
+        Lm += m->aij[5 * j + 1 + k] * cm[m->nij[4 * j + k]];
+      }
+      /* boundary rates are D times a fixed source */
+      if (R[OR_D_CA] != 0) Lc += m->br[S_CA * N + j] / R[OR_D_CA];
+      if (R[OR_D_DYE] != 0) Ly += m->br[S_DYE * N + j] / R[OR_D_DYE];
+      if (R[OR_D_ATP] != 0) La += m->br[S_ATP * N + j] / R[OR_D_ATP];
+      if (R[OR_D_CMDN] != 0) Lm += m->br[S_CMDN * N + j] / R[OR_D_CMDN];
+      grad[0] += dt * w * Lc;
+      grad[1] += dt * lam[S_DYE * N + j] * Ly;
+      grad[14] += dt * lam[S_ATP * N + j] * La;
+      grad[15] += dt * lam[S_CMDN * N + j] * Lm;
+    }
+    /* boundary rates of the mobile buffers hold their resting values
+     * c0 B/(Kd + c0), Kd = koff/kon (cpu/InitFuncs.cpp:1005-1039, restated in or_mesh_load) */
+    {
+      int q;
+      const int sp2[3] = {S_DYE, S_CMDN, S_ATP}, kon2[3] = {OR_K_ON_DYE, OR_K_ON_CMDN, OR_K_ON_ATP},
+                koff2[3] = {OR_K_OFF_DYE, OR_K_OFF_CMDN, OR_K_OFF_ATP}, g2[3] = {8, 2, 16};
+      for (q = 0; q < 3; ++q) {
+        double brs = m->br[sp2[q] * N + j];
+        if (brs != 0) {
+          double kon = R[kon2[q]], Kd = R[koff2[q]] / kon, den = Kd + R[OR_C_0_CA];
+          grad[g2[q]] += dt * lam[sp2[q] * N + j] * brs * Kd / (kon * den);
+          grad[g2[q] + 1] += dt * lam[sp2[q] * N + j] * brs * (-1.0 / (kon * den));
+        }
+      }
+    }
+    if (m->domain[j] == 0) {
+      /* buffers: r_b = kon (B - b) c - koff b;  F_c -= r_b,  F_b += r_b */
+      struct { int s, kon, koff, btot, gkon; } bf[4] = {{S_DYE, OR_K_ON_DYE, OR_K_OFF_DYE, OR_B_TOT_DYE, 8},
+                                                       {S_ATP, OR_K_ON_ATP, OR_K_OFF_ATP, OR_B_TOT_ATP, 16},
+                                                       {S_CMDN, OR_K_ON_CMDN, OR_K_OFF_CMDN, OR_B_TOT_CMDN, 2},
+                                                       {S_TRPN, OR_K_ON_TRPN, OR_K_OFF_TRPN, OR_B_TOT_TRPN, 4}};
+      int q, nb = m->tropc[j] ? 4 : 3;
+      for (q = 0; q < nb; ++q) {
+        double b = x[bf[q].s * N + j], kon = R[bf[q].kon], koff = R[bf[q].koff];
+        double alpha = kon * (R[bf[q].btot] - b), beta = kon * c[j] + koff;
+        double lb = lam[bf[q].s * N + j];
+        dGdc -= alpha;
+        out[bf[q].s * N + j] += dt * beta * w;    /* dF_c/db = +beta/B */
+        out[bf[q].s * N + j] += dt * (-beta) * lb; /* dF_b/db = -beta */
+        out[S_CA * N + j] += dt * alpha * lb;     /* dF_b/dc = alpha */
+        if (bf[q].gkon >= 0) {
+          double dr_kon = (R[bf[q].btot] - b) * c[j], dr_koff = -b;
+          grad[bf[q].gkon] += dt * (lb - w) * dr_kon;
+          grad[bf[q].gkon + 1] += dt * (lb - w) * dr_koff;
+        }
+      }
+      if (m->tropc[j]) {
+        double Kd = R[OR_K_D_i], Ki = (c[j] / Kd) * (c[j] / Kd), Ksr = (G[1] / R[OR_K_D_SR]) * (G[1] / R[OR_K_D_SR]);
+        double d0 = 0.104217 + 17.923 * Ksr, d1 = 1.75583e6 + Ksr * 7.61673e6, d2 = 6.08463e11 + Ksr * 4.50544e11;
+        double n1 = 9.17846e6 - 11478.2 * Ksr, n0 = 0.329904 * Ksr;
+        double Dn = d0 + Ki * d1 + Ki * Ki * d2, Nn = Ki * Ki * 3.24873e12 + Ki * n1 - n0;
+        double dN = 2 * Ki * 3.24873e12 + n1, dD = d1 + 2 * Ki * d2;
+        double dv_dKi = (dN * Dn - Nn * dD) / (Dn * Dn), dKi_dc = 2 * c[j] / (Kd * Kd);
+        dGdc -= 2e-3 * R[OR_A_P] * dv_dKi * dKi_dc;
+        grad[11] += dt * w * (-2e-3 * Nn / Dn);
+      }
+    } else {
+      double b = cq[j], kon = R[OR_K_ON_CSQN], koff = R[OR_K_OFF_CSQN];
+      double alpha = kon * (R[OR_B_T_JSR] - b), beta = kon * c[j] + koff, lb = lam[S_CSQN * N + j];
+      dGdc -= alpha;
+      dGdc -= R[OR_V_REFILL];
+      out[S_CSQN * N + j] += dt * beta * w;
+      out[S_CSQN * N + j] += dt * (-beta) * lb;
+      out[S_CA * N + j] += dt * alpha * lb;
+      grad[6] += dt * (lb - w) * (R[OR_B_T_JSR] - b) * c[j];
+      grad[7] += dt * (lb - w) * (-b);
+    }
+    /* element-local channel terms */
+    for (i = 0; i < m->NR; ++i)
+      if (ryr[i] && (m->ryr_ele[i] == j || m->ryr_jsr[i] == j)) dGdc -= R[OR_V_RYR] * R[OR_V_CELL] / m->V0[j];
+    for (i = 0; i < m->NL; ++i)
+      if (m->lcc_ele[i] == j && (lcc[i] == 6 || lcc[i] == 12) && lccv[i] == 2) dGdc += A * E / Em1 / m->V0[j];
+    /* dF_c/dc_j = dG/dc / B - G B' / B^2 */
+    out[S_CA * N + j] += dt * (dGdc / B - Gv[j] * dB / (B * B)) * lc;
+    /* SL buffer capacity and affinity */
+    {
+      double cc = c[j];
+      double dB_dBtot = (m->TT[j] / (m->V0[j] * (1e-15))) * Kh / ((Kh + cc) * (Kh + cc));
+      double dB_dK = bhi * (cc - Kh) / ((Kh + cc) * (Kh + cc) * (Kh + cc));
+      grad[12] += dt * lc * (-Gv[j] / (B * B)) * dB_dBtot;
+      grad[13] += dt * lc * (-Gv[j] / (B * B)) * dB_dK;
+    }
+  }
+  /* RyR cross terms and V_RYR */
+  for (i = 0; i < m->NR; ++i)
+    if (ryr[i]) {
+      int cl = m->ryr_ele[i], js = m->ryr_jsr[i];
+      double v = R[OR_V_RYR] * R[OR_V_CELL];
+      double wcl = lam[S_CA * N + cl] / Bv[cl], wjs = lam[S_CA * N + js] / Bv[js];
+      out[S_CA * N + js] += dt * v / m->V0[cl] * wcl; /* dF_cl/dc_js */
+      out[S_CA * N + cl] += dt * v / m->V0[js] * wjs; /* dF_js/dc_cl */
+      grad[10] += dt * (wcl / m->V0[cl] - wjs / m->V0[js]) * R[OR_V_CELL] * (c[js] - c[cl]);
+    }
+  free(Bv);
+  free(Gv);
+}
+
+double or_adjoint(const or_mesh* m, const int* I, const double* R, const double* S0, const int* ryr0,
+                  const int* lcc0, const int* lccv0, const double* res0, uint64_t seed, int64_t n_steps,
+                  int tick_every, int ns, const double* W, const double* pad, const double* F0,
+                  const double* target, double* grad, double* lam0) {
+  int N = m->N, NR = m->NR, NL = m->NL, k;
+  int64_t n;
+  double G[2], L = 0;
+  double* X = malloc(sizeof(double) * 6 * N * (size_t)(n_steps + 1));
+  int* RY = malloc(sizeof(int) * NR * (size_t)(n_steps + 1));
+  int* LC = malloc(sizeof(int) * NL * (size_t)(n_steps + 1) + 4);
+  int* LV = malloc(sizeof(int) * NL * (size_t)(n_steps + 1) + 4);
+  double* res = malloc(sizeof(double) * (NR + NL + 1));
+  double *lam = calloc(6 * (size_t)N, sizeof(double)), *nxt = malloc(sizeof(double) * 6 * N);
+  double* dLdy = malloc(sizeof(double) * N);
+  G[0] = R[OR_DEFAULT_VM];
+  G[1] = R[OR_DEFAULT_CA_NSR];
+  memcpy(X, S0, sizeof(double) * 6 * N);
+  memcpy(RY, ryr0, sizeof(int) * NR);
+  memcpy(LC, lcc0, sizeof(int) * NL);
+  memcpy(LV, lccv0, sizeof(int) * NL);
+  memcpy(res, res0, sizeof(double) * (NR + NL));
+  /* forward: x_{n+1} from x_n with the channel states of step n */
+  for (n = 0; n < n_steps; ++n) {
+    double* xn1 = X + 6 * (size_t)N * (n + 1);
+    memcpy(xn1, X + 6 * (size_t)N * n, sizeof(double) * 6 * N);
+    memcpy(RY + NR * (n + 1), RY + NR * n, sizeof(int) * NR);
+    memcpy(LC + NL * (n + 1), LC + NL * n, sizeof(int) * NL);
+    memcpy(LV + NL * (n + 1), LV + NL * n, sizeof(int) * NL);
+    or_explicit_step(m, R, G, xn1, RY + NR * n, LC + NL * n, LV + NL * n);
+    if (!I[OI_FLAG_NO_GATING])
+      or_gating_philox(m, R, G[0], xn1, seed, n, RY + NR * (n + 1), LC + NL * (n + 1), LV + NL * (n + 1), res);
+    if ((n + 1) % tick_every == 0)
+      L += tick_loss(m, ns, W, pad, F0, target + (size_t)ns * ((n + 1) / tick_every - 1), xn1, NULL);
+  }
+  /* backward */
+  for (k = 0; k < OR_N_ADJ; ++k) grad[k] = 0;
+  for (n = n_steps; n >= 1; --n) {
+    int j;
+    if (n % tick_every == 0) {
+      memset(dLdy, 0, sizeof(double) * N);
+      tick_loss(m, ns, W, pad, F0, target + (size_t)ns * (n / tick_every - 1), X + 6 * (size_t)N * n, dLdy);
+      for (j = 0; j < N; ++j) lam[S_DYE * N + j] += dLdy[j];
+    }
+    /* lam_{n-1} = lam_n + dt J(x_{n-1})^T lam_n */
+    memcpy(nxt, lam, sizeof(double) * 6 * N);
+    adj_step(m, R, G, X + 6 * (size_t)N * (n - 1), RY + NR * (n - 1), LC + NL * (n - 1), LV + NL * (n - 1), lam,
+             nxt, grad);
+    memcpy(lam, nxt, sizeof(double) * 6 * N);
+  }
+  if (lam0) memcpy(lam0, lam, sizeof(double) * 6 * N);
+  free(X);
+  free(RY);
+  free(LC);
+  free(LV);
+  free(res);
+  free(lam);
+  free(nxt);
+  free(dLdy);
+  return L;
+}
+
+/* loss only (same forward), for finite differences */
+double or_adjoint_loss(const or_mesh* m, const int* I, const double* R, const double* S0, const int* ryr0,
+                       const int* lcc0, const int* lccv0, const double* res0, uint64_t seed, int64_t n_steps,
+                       int tick_every, int ns, const double* W, const double* pad, const double* F0,
+                       const double* target) {
+  int N = m->N, NR = m->NR, NL = m->NL;
+  int64_t n;
+  double G[2], L = 0;
+  double* S = malloc(sizeof(double) * 6 * N);
+  int *ry = malloc(sizeof(int) * (NR + 1)), *lc = malloc(sizeof(int) * (NL + 1)), *lv = malloc(sizeof(int) * (NL + 1));
+  double* res = malloc(sizeof(double) * (NR + NL + 1));
+  G[0] = R[OR_DEFAULT_VM];
+  G[1] = R[OR_DEFAULT_CA_NSR];
+  memcpy(S, S0, sizeof(double) * 6 * N);
+  memcpy(ry, ryr0, sizeof(int) * NR);
+  memcpy(lc, lcc0, sizeof(int) * NL);
+  memcpy(lv, lccv0, sizeof(int) * NL);
+  memcpy(res, res0, sizeof(double) * (NR + NL));
+  for (n = 0; n < n_steps; ++n) {
+    or_explicit_step(m, R, G, S, ry, lc, lv);
+    if (!I[OI_FLAG_NO_GATING]) or_gating_philox(m, R, G[0], S, seed, n, ry, lc, lv, res);
+    if ((n + 1) % tick_every == 0)
+      L += tick_loss(m, ns, W, pad, F0, target + (size_t)ns * ((n + 1) / tick_every - 1), S, NULL);
+  }
+  free(S);
+  free(ry);
+  free(lc);
+  free(lv);
+  free(res);
+  return L;
+}

@@ -43,6 +43,11 @@ R = dict(T_FINAL=0, T_STEP=1, OUTPUT_STATES_INTERVAL=2, OUTPUT_GRID_INTERVAL=3, 
          RYR_K_PLUS=45, RYR_K_MINUS=46, RYR_PHI_M=47, RYR_PHI_B=48, K_D_i=49, K_D_SR=50, A_P=51,
          LCC_DURATION=52, T_CLAMP=53, V_CLAMP=54, INIT_RYR_HOLD=55)
 SPECIES = ("CA", "ATP", "CMDN", "TRPN", "CSQN", "DYE")
+# parameters of the adjoint gradient, in srs_adjoint order (SRS_ADJ_*)
+ADJ_PARAMS = ("D_CA", "D_DYE", "K_ON_CMDN", "K_OFF_CMDN", "K_ON_TRPN", "K_OFF_TRPN", "K_ON_CSQN",
+              "K_OFF_CSQN", "K_ON_DYE", "K_OFF_DYE", "V_RYR", "A_P", "B_TOT_SL_HI", "K_D_SL_HI",
+              "D_ATP", "D_CMDN", "K_ON_ATP", "K_OFF_ATP")
+N_ADJ = len(ADJ_PARAMS)
 
 
 class SrsError(RuntimeError):
@@ -123,6 +128,15 @@ class LinescanDesc(C.Structure):
 NOALLOC_MAX_REALIZATIONS = 256
 
 
+class _AdjDesc(C.Structure):
+    _fields_ = [("n_steps", C.c_int64), ("tick_every", C.c_int), ("checkpoint_every", C.c_int),
+                ("f0", C.c_void_p), ("target", C.c_void_p)]
+
+
+class _AdjOut(C.Structure):
+    _fields_ = [("loss", C.c_void_p), ("grad", C.c_void_p), ("grad_state", C.c_void_p)]
+
+
 class NoallocStep(C.Structure):
     """srs_noalloc_step: one FP64 ExplicitStep on caller-owned device buffers."""
     _fields_ = [("n_ele", C.c_int), ("n_realizations", C.c_int), ("n_ryr", C.c_int),
@@ -170,6 +184,8 @@ _SIGS = {
     "srs_explicit_step_fp64_noalloc": (C.c_int, [C.POINTER(NoallocStep)]),
     "srs_linescan_setup": (C.c_int, [_P, C.POINTER(LinescanDesc), C.POINTER(C.c_int)]),
     "srs_linescan": (C.c_int, [_P, _P, _P]),
+    "srs_adjoint_param_index": (C.c_int, [C.c_int]),
+    "srs_adjoint": (C.c_int, [_P, C.POINTER(_AdjDesc), C.POINTER(_AdjOut)]),
 }
 
 
@@ -396,6 +412,28 @@ class Simulation:
         rest = np.zeros(self._ls_n)
         _check(_lib.srs_linescan(self._h, _ptr(out), _ptr(rest)))
         return out, rest
+
+    def adjoint(self, n_steps, tick_every, f0, target=None, checkpoint_every=0, grad_state=False):
+        """srs_adjoint: pathwise gradient of the line-scan dF/F0 loss.
+
+        Returns (loss[R], grad[R][N_ADJ] in ADJ_PARAMS order, and
+        dL/d(initial state)[R][6][N] when grad_state is true, else None)."""
+        f0 = np.ascontiguousarray(f0, dtype=np.float64)
+        if len(f0) != getattr(self, "_ls_n", -1):
+            raise ValueError("f0 needs one value per line-scan sample (call linescan_setup first)")
+        n_ticks = int(n_steps) // int(tick_every)
+        tg = None
+        if target is not None:
+            tg = np.ascontiguousarray(np.broadcast_to(target, (self.R, n_ticks, len(f0))),
+                                      dtype=np.float64)
+        loss = np.zeros(self.R)
+        grad = np.zeros((self.R, N_ADJ))
+        gs = np.zeros((self.R, 6, self.grid.n_ele)) if grad_state else None
+        d = _AdjDesc(int(n_steps), int(tick_every), int(checkpoint_every), f0.ctypes.data,
+                     tg.ctypes.data if tg is not None else None)
+        o = _AdjOut(loss.ctypes.data, grad.ctypes.data, gs.ctypes.data if gs is not None else None)
+        _check(_lib.srs_adjoint(self._h, C.byref(d), C.byref(o)))
+        return loss, grad, gs
 
     def write_grid_vtk(self, r, path, run=0, rank=0, n=0, t=0.0):
         _check(_lib.srs_write_grid_vtk(self._h, r, str(path).encode(), run, rank, n, float(t)))

@@ -42,6 +42,7 @@ def _units():
         ("srs_capi.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "srs_capi.cu")]),
         ("k_noalloc.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_noalloc.cu")]),
         ("k_linescan.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_linescan.cu")]),
+        ("k_adjoint.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_adjoint.cu")]),
         ("srs_host.o", common_cc + ["-c", os.path.join(CSRC, "srs_host.cpp")]),
         ("meshgen.o", common_cc + ["-c", os.path.join(CSRC, "meshgen.cpp")]),
     ]

@@ -1,0 +1,427 @@
+// k_adjoint.cu — pathwise adjoint of the FP32 resident engine.
+//
+// The forward map is the explicit Euler step of ExplicitStep
+// (cpu/RunSimulation.cpp:591-647), x_n = x_{n-1} + dt F(x_{n-1}; theta, g_{n-1}),
+// with the channel states g_{n-1} of every step held fixed: gating is not
+// differentiable, so the gradient is the one of the recorded path.  The
+// adjoint recursion is
+//   lambda_{n-1} = lambda_n + dt J(x_{n-1})^T lambda_n,
+//   dL/dtheta   += dt (dF/dtheta)(x_{n-1})^T lambda_n,
+// with lambda_n += dL/dx_n injected at the line-scan ticks.
+//
+// One thread-block cluster holds one realization, partitioned exactly like
+// the forward resident engine.  Every step each element publishes
+// (lambda_Ca / B_SL, lambda_ATP, lambda_CMDN, lambda_dye) into a
+// double-buffered shared-memory slot; after one cluster barrier every element
+// gathers its four neighbours' slots (through distributed shared memory when
+// they sit in another CTA), so the transposed diffusion operator needs the
+// transposed coefficients aT only.  The state x_{n-1}, its Ca rate before the
+// rapid-buffer factor (G) and the channel states come from the trajectory
+// the forward engine recorded for the segment.  Lambda lives in HBM/L2 in
+// owner-only arrays with Kahan compensation, like the forward state.
+//
+// Parameter gradients: every thread keeps a compensated FP32 sum per
+// parameter over its elements and the steps of the segment; at the end of a
+// realization the sums are reduced in FP64 and added in FP64 to the
+// per-realization gradient, which therefore accumulates over segments (the
+// long reverse sweep) in double precision.
+#include "srs_cluster.cuh"
+#include "srs_engine.h"
+
+namespace srs {
+
+namespace {
+
+constexpr int NA = SRS_N_ADJ;
+
+struct KSum {
+  float s[NA];
+  float c[NA];
+};
+
+__device__ __forceinline__ void kadd(float& s, float& c, float v) {
+  float y = v - c;
+  float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// One buffer reaction r = kon (B - b) c - koff b of an element: adds its
+// Jacobian-transpose terms and its kon/koff gradient terms.
+__device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& ak, int q, float c,
+                                           float ub, float lb, float w, float& ob, float& oc,
+                                           float& dG, float* g, int gi) {
+  const float free = k.bfree[q] - ub;
+  const float alpha = k.kon[q] * free;
+  const float beta = fmaf(k.kon[q], c, k.koff[q]);
+  dG -= alpha;            // dF_Ca/dCa (times B)
+  ob += beta * (w - lb);  // dF_Ca/db * lambda_Ca + dF_b/db * lambda_b
+  oc += alpha * lb;       // dF_b/dCa * lambda_b
+  const float d = lb - w;
+  g[gi] += d * free * c;              // dr/dkon = (B - b) c
+  g[gi + 1] -= d * (ak.brest[q] + ub);  // dr/dkoff = -b
+}
+
+}  // namespace
+
+// Shared memory: float4 pub[2][P]; double red[32][NA]; int32 cptr[n_ch+1];
+// ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16].
+size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries) {
+  size_t b = (size_t)2 * P * sizeof(float4);
+  b += (size_t)32 * NA * sizeof(double);
+  b += (size_t)(n_chtet + 1) * sizeof(int32_t);
+  b = (b + 15) & ~(size_t)15;
+  b += (size_t)n_entries * sizeof(ChanEntry32);
+  b += 2 * 16 * sizeof(uint32_t);
+  return b;
+}
+
+template <int C>
+__global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int P = a.P;
+  float4* pub0 = reinterpret_cast<float4*>(smem);
+  float4* pub1 = pub0 + P;
+  double* red = reinterpret_cast<double*>(pub1 + P);
+  int32_t* s_cptr = reinterpret_cast<int32_t*>(red + 32 * NA);
+  const int n_ch0 = a.n_chtet[0];
+  ChanEntry32* s_clist = reinterpret_cast<ChanEntry32*>(
+      (reinterpret_cast<uintptr_t>(s_cptr + n_ch0 + 1) + 15) & ~(uintptr_t)15);
+  const int n_ent = a.ch_ptr[n_ch0];
+  uint32_t* s_base = reinterpret_cast<uint32_t*>(s_clist + n_ent);  // [2][16]
+
+  uint32_t rank = 0;
+  if constexpr (C > 1) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+  const int cid = blockIdx.x / C, ncl = gridDim.x / C;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int n_loc = a.n_local[rank];
+  const int n_ch = rank == 0 ? n_ch0 : 0;
+  const size_t NE = (size_t)C * P;
+  const TetRec* geo = a.geo + (size_t)rank * P;
+  const float4* aT = a.aT + (size_t)rank * P;
+  const uint32_t mask = (1u << a.off_bits) - 1u;
+  const Consts32& k = a.k;
+  const AdjConsts& ak = a.ak;
+  const int NR = a.NR, NL = a.NL, W = NR + 2 * NL + 1;
+
+  if (rank == 0) {
+    for (int i = tid; i <= n_ch; i += nthr) s_cptr[i] = a.ch_ptr[i];
+    for (int i = tid; i < n_ent; i += nthr) s_clist[i] = a.ch_list[i];
+  }
+  if (tid < C) {
+    s_base[tid] = (C > 1) ? map_rank(smem_addr(pub0), tid) : smem_addr(pub0);
+    s_base[16 + tid] = (C > 1) ? map_rank(smem_addr(pub1), tid) : smem_addr(pub1);
+  }
+  step_barrier<C>();
+
+  for (int r = cid; r < a.R; r += ncl) {
+    const size_t roff = (size_t)r * NE + (size_t)rank * P;  // lambda, this partition
+    KSum gs;
+#pragma unroll
+    for (int p = 0; p < NA; ++p) gs.s[p] = gs.c[p] = 0.0f;
+    int cur = 0;
+    for (int t = a.n_steps; t >= 1; --t) {
+      const int64_t n = a.s0 + t;  // step x_{n-1} -> x_n
+      float4* pub = cur ? pub1 : pub0;
+      const uint32_t* bs = s_base + 16 * cur;
+      const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * P;
+      const bool tick = a.tick_every > 0 && (n % a.tick_every) == 0;
+      const double* coef = nullptr;
+      if (tick) {
+        const int64_t slot = n / a.tick_every - a.s0 / a.tick_every - 1;
+        coef = a.coef + ((size_t)slot * a.R + r) * a.n_samples;
+      }
+      // ---- publish lambda_n (with the tick injection of step n) --------
+      for (int i = tid; i < n_loc; i += nthr) {
+        float4 L = a.lam[roff + i];
+        if (tick) {
+          const int e = (int)(rank * P + i);
+          double inj = 0.0;
+          for (int q = a.wt_ptr[e]; q < a.wt_ptr[e + 1]; ++q) inj += coef[a.wt_idx[q]] * a.wt_w[q];
+          L.w += (float)inj;
+        }
+        const float4* gp = reinterpret_cast<const float4*>(geo + i);
+        const float4 gb = __ldg(gp + 1);
+        const float bsl = gb.z;
+        const uint32_t fl = __float_as_uint(gb.w);
+        const float c = ((fl & 1u) ? k.c0j : k.c0) + a.traj_u[xoff + i].x;
+        float B = 1.0f;
+        if (bsl != 0.0f) {
+          const float kc = k.khi + c;
+          B = fmaf(bsl, 1.0f / (kc * kc), 1.0f);
+        }
+        pub[i] = make_float4(L.x / B, L.y, L.z, L.w);
+      }
+      step_barrier<C>();
+      // ---- lambda_{n-1} = lambda_n + dt J(x_{n-1})^T lambda_n ----------
+      const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
+      for (int i = tid; i < n_loc; i += nthr) {
+        const float4 x = a.traj_u[xoff + i];
+        const float xim = a.traj_im[xoff + i];
+        const float G = a.traj_g[xoff + i];
+        const float4* gp = reinterpret_cast<const float4*>(geo + i);
+        const float4 ga = __ldg(gp);
+        const float4 gb = __ldg(gp + 1);
+        const float4 at = __ldg(aT + i);
+        const uint32_t w0 = __float_as_uint(gb.x), w1 = __float_as_uint(gb.y);
+        const uint32_t c0 = w0 & 0xffffu, c1 = w0 >> 16, c2 = w1 & 0xffffu, c3 = w1 >> 16;
+        const float bsl = gb.z;
+        const uint32_t fl = __float_as_uint(gb.w);
+        const float4 me = pub[i];
+        float4 n0, n1, n2, n3;
+        if constexpr (C == 1) {
+          n0 = ld_smem_f4(bs[0] + c0 * 16u);
+          n1 = ld_smem_f4(bs[0] + c1 * 16u);
+          n2 = ld_smem_f4(bs[0] + c2 * 16u);
+          n3 = ld_smem_f4(bs[0] + c3 * 16u);
+        } else {
+          n0 = ld_dsmem_f4(bs[c0 >> a.off_bits] + (c0 & mask) * 16u);
+          n1 = ld_dsmem_f4(bs[c1 >> a.off_bits] + (c1 & mask) * 16u);
+          n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & mask) * 16u);
+          n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & mask) * 16u);
+        }
+        const float sa = (ga.x + ga.y) + (ga.z + ga.w);
+        // transposed diffusion: S = sum_k aT_k lambda(nb_k) - (sum_k a_k) lambda(self)
+        float Sc = at.x * n0.x;
+        Sc = fmaf(at.y, n1.x, Sc);
+        Sc = fmaf(at.z, n2.x, Sc);
+        Sc = fmaf(at.w, n3.x, Sc);
+        Sc = fmaf(-sa, me.x, Sc);
+        float Sa = at.x * n0.y;
+        Sa = fmaf(at.y, n1.y, Sa);
+        Sa = fmaf(at.z, n2.y, Sa);
+        Sa = fmaf(at.w, n3.y, Sa);
+        Sa = fmaf(-sa, me.y, Sa);
+        float Sm = at.x * n0.z;
+        Sm = fmaf(at.y, n1.z, Sm);
+        Sm = fmaf(at.z, n2.z, Sm);
+        Sm = fmaf(at.w, n3.z, Sm);
+        Sm = fmaf(-sa, me.z, Sm);
+        float Sy = at.x * n0.w;
+        Sy = fmaf(at.y, n1.w, Sy);
+        Sy = fmaf(at.z, n2.w, Sy);
+        Sy = fmaf(at.w, n3.w, Sy);
+        Sy = fmaf(-sa, me.w, Sy);
+        float g[NA];
+#pragma unroll
+        for (int p = 0; p < NA; ++p) g[p] = 0.0f;
+        // D gradients: sum_j lambda_j (L u)_j = sum_j u_j (L^T lambda)_j
+        g[SRS_ADJ_D_CA] = x.x * Sc;
+        g[SRS_ADJ_D_ATP] = x.y * Sa;
+        g[SRS_ADJ_D_CMDN] = x.z * Sm;
+        g[SRS_ADJ_D_DYE] = x.w * Sy;
+        float oc = k.D[0] * Sc, oa = k.D[1] * Sa, om = k.D[2] * Sm, oy = k.D[3] * Sy, oi = 0.0f;
+        const float w = me.x;
+        const float lim = a.lam_im[roff + i];
+        float dG = 0.0f;
+        const bool jsr = (fl & 1u) != 0;
+        const float c = (jsr ? k.c0j : k.c0) + x.x;
+        if (!jsr) {
+          adj_buffer(k, ak, 0, c, x.w, me.w, w, oy, oc, dG, g, SRS_ADJ_K_ON_DYE);
+          adj_buffer(k, ak, 1, c, x.y, me.y, w, oa, oc, dG, g, SRS_ADJ_K_ON_ATP);
+          adj_buffer(k, ak, 2, c, x.z, me.z, w, om, oc, dG, g, SRS_ADJ_K_ON_CMDN);
+          if (fl & 2u) {
+            adj_buffer(k, ak, 3, c, xim, lim, w, oi, oc, dG, g, SRS_ADJ_K_ON_TRPN);
+            // SERCA v(Ki), Ki = (c / K_D_i)^2 (cpu/RunSimulation.cpp:83-91)
+            float Ki = c * k.inv_kdi;
+            Ki = Ki * Ki;
+            const float den = fmaf(Ki * Ki, k.sd2, fmaf(Ki, k.sd1, k.sd0));
+            const float num = fmaf(Ki * Ki, 3.24873e12f, fmaf(Ki, k.sn1, -k.sn0));
+            const float v = num / den;
+            const float dnum = fmaf(2.0f * Ki, 3.24873e12f, k.sn1);
+            const float dden = fmaf(2.0f * Ki, k.sd2, k.sd1);
+            const float dv = (dnum - v * dden) / den * (2.0f * c * k.inv_kdi * k.inv_kdi);
+            dG = fmaf(-k.serca_scale, dv, dG);
+            g[SRS_ADJ_A_P] = -w * ak.serca_per_ap * v;
+          }
+        } else {
+          adj_buffer(k, ak, 4, c, xim, lim, w, oi, oc, dG, g, SRS_ADJ_K_ON_CSQN);
+          dG -= k.refill_v;
+        }
+        if (i < n_ch) {
+          // channel elements and their RyR partners all sit in partition 0
+          for (int q = s_cptr[i]; q < s_cptr[i + 1]; ++q) {
+            const ChanEntry32 e = s_clist[q];
+            if (e.kind < 2) {
+              if (rec[e.ch]) {
+                const uint32_t oc_code = e.kind == 0 ? a.ryr_jsr_code[e.ch] : a.ryr_cleft_code[e.ch];
+                const float wo = pub[oc_code & mask].x;
+                const float so = e.kind == 0 ? a.ryr_s_js[e.ch] : a.ryr_s_cl[e.ch];
+                const float qv = fmaf(w, e.s, wo * so);
+                if (e.kind == 0) {
+                  oc = fmaf(-k.jr_scale, qv, oc);
+                  const float cj = k.c0j + a.traj_u[xoff + (oc_code & mask)].x;
+                  g[SRS_ADJ_V_RYR] = fmaf(qv * ak.v_cell, cj - c, g[SRS_ADJ_V_RYR]);
+                } else {
+                  oc = fmaf(k.jr_scale, qv, oc);
+                }
+              }
+            } else if ((rec[NR + e.ch] == 6 || rec[NR + e.ch] == 12) && rec[NR + NL + e.ch] == 2) {
+              const int vs = rec[W - 1];
+              dG = fmaf(k.lccA[vs] * k.lccE[vs], e.s, dG);
+            }
+          }
+        }
+        oc = fmaf(dG, w, oc);
+        if (bsl != 0.0f) {
+          // F_Ca = G / B(c):  -G B'(c) / B^2 lambda_Ca = 2 bsl G w / (B kc^3)
+          const float kc = k.khi + c;
+          const float kc2 = kc * kc;
+          const float B = fmaf(bsl, 1.0f / kc2, 1.0f);
+          const float GB = G / B;
+          oc = fmaf(2.0f * bsl * GB / (kc2 * kc), w, oc);
+          g[SRS_ADJ_B_TOT_SL] = -w * GB * (B - 1.0f) * ak.inv_btot_sl;
+          g[SRS_ADJ_K_D_SL] = -w * GB * bsl * (c - k.khi) / (k.khi * kc2 * kc);
+        }
+        // compensated update of lambda (owner-only state)
+        float4 L = make_float4(a.lam[roff + i].x, me.y, me.z, me.w);
+        float4 cm = a.lam_c4[roff + i];
+        float ci = a.lam_cim[roff + i];
+        float li = lim;
+        kadd(L.x, cm.x, k.dt * oc);
+        kadd(L.y, cm.y, k.dt * oa);
+        kadd(L.z, cm.z, k.dt * om);
+        kadd(L.w, cm.w, k.dt * oy);
+        kadd(li, ci, k.dt * oi);
+        a.lam[roff + i] = L;
+        a.lam_im[roff + i] = li;
+        a.lam_c4[roff + i] = cm;
+        a.lam_cim[roff + i] = ci;
+#pragma unroll
+        for (int p = 0; p < NA; ++p) kadd(gs.s[p], gs.c[p], g[p]);
+      }
+      cur ^= 1;
+    }
+    // ---- FP64 reduction of this realization's gradient ---------------------
+    const int warp = tid >> 5, lane = tid & 31, nw = nthr >> 5;
+#pragma unroll
+    for (int p = 0; p < NA; ++p) {
+      double v = (double)gs.s[p] - (double)gs.c[p];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp * NA + p] = v;
+    }
+    __syncthreads();
+    if (tid < NA) {
+      double v = 0.0;
+      for (int q = 0; q < nw; ++q) v += red[q * NA + tid];
+      atomicAdd(a.grad + (size_t)r * NA + tid, v * (double)k.dt);
+    }
+    step_barrier<C>();  // pub and red are reused by the next realization
+  }
+}
+
+// Line-scan loss at one tick: F_i = pad_i + sum_q w_q dye(col_q) from the
+// trajectory slot, e_i = F_i / F0_i - 1 - target_i, L += e_i^2 / 2 and
+// coef_i = e_i / F0_i (= dL/dF_i).  One block per realization; samples in
+// order, so the loss sum is deterministic.
+__global__ void k_adj_tick(AdjTickArgs a) {
+  const int r = blockIdx.x;
+  __shared__ double red[256];
+  double lacc = 0.0;
+  const float4* U = a.traj_u + (size_t)r * a.n_state;
+  for (int i = 0; i < a.n_samples; ++i) {
+    double acc = 0.0;
+    for (int q = a.ptr[i] + threadIdx.x; q < a.ptr[i + 1]; q += blockDim.x) {
+      const int e = a.col[q];
+      acc += a.w[q] * (a.rest_dye[e] + (double)U[e].w);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double F = a.pad[i] + red[0];
+      const double tg = a.target ? a.target[((size_t)r * a.n_ticks + a.tick) * a.n_samples + i] : 0.0;
+      const double e = F / a.f0[i] - 1.0 - tg;
+      a.coef[(size_t)r * a.n_samples + i] = e / a.f0[i];
+      lacc += 0.5 * e * e;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.loss[r] += lacc;
+}
+
+template <int C>
+static cudaError_t adj_attrs(size_t smem) {
+  cudaError_t e =
+      cudaFuncSetAttribute(k_adjoint32<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && C > 8)
+    e = cudaFuncSetAttribute(k_adjoint32<C>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+template <int C>
+static cudaLaunchConfig_t adj_cfg(int n_clusters, int threads, size_t smem, cudaStream_t st,
+                                  cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n_clusters * C);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+template <int C>
+static int launch_adjoint_t(const AdjArgs& a, int n_clusters, int threads, size_t smem,
+                            cudaStream_t st) {
+  if (adj_attrs<C>(smem) != cudaSuccess) return -1;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = adj_cfg<C>(n_clusters, threads, smem, st, attr);
+  return cudaLaunchKernelEx(&cfg, k_adjoint32<C>, a) == cudaSuccess ? 0 : -1;
+}
+
+template <int C>
+static int adjoint_max_clusters_t(int threads, size_t smem) {
+  if (adj_attrs<C>(smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = adj_cfg<C>(1, threads, smem, nullptr, attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_adjoint32<C>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+#define SRS_ADJ_SIZES(X) X(1) X(2) X(3) X(4) X(5) X(6) X(8) X(16)
+
+int launch_adjoint(const AdjArgs& a, int C, int n_clusters, int threads, size_t smem,
+                   cudaStream_t st) {
+  switch (C) {
+#define SRS_L(CC) \
+  case CC:        \
+    return launch_adjoint_t<CC>(a, n_clusters, threads, smem, st);
+    SRS_ADJ_SIZES(SRS_L)
+#undef SRS_L
+    default: return -1;
+  }
+}
+
+int adjoint_max_clusters(int C, int threads, size_t smem) {
+  switch (C) {
+#define SRS_M(CC) \
+  case CC:        \
+    return adjoint_max_clusters_t<CC>(threads, smem);
+    SRS_ADJ_SIZES(SRS_M)
+#undef SRS_M
+    default: return 0;
+  }
+}
+
+int launch_adj_tick(const AdjTickArgs& a, int R, cudaStream_t st) {
+  k_adj_tick<<<R, 256, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace srs

@@ -25,6 +25,7 @@
 //     while the other warps update everything else — one cluster barrier per
 //     time step, and the termination decision is known at that barrier.
 #include "srs_engine.h"
+#include "srs_cluster.cuh"
 #include "srs_protocol.cuh"
 
 namespace srs {
@@ -35,7 +36,8 @@ namespace srs {
 __device__ __forceinline__ void tet_update(const Consts32& k, float4 o, float im, float4 s1,
                                            float4 s2, float4 s3, float4 s4, float4 a,
                                            uint32_t fl, float bsl, float kb, float flux,
-                                           float4& cm, float& ci, float4* out, float* im_out) {
+                                           float4& cm, float& ci, float4* out, float* im_out,
+                                           float* g_out = nullptr) {
   float dx = a.x * (s1.x - o.x);
   dx = fmaf(a.y, s2.x - o.x, dx);
   dx = fmaf(a.z, s3.x - o.x, dx);
@@ -93,6 +95,7 @@ __device__ __forceinline__ void tet_update(const Consts32& k, float4 o, float im
     rca += fmaf(-u, k.refill_v, k.refill0);
   }
   rca += flux;
+  if (g_out) *g_out = rca;  // Ca rate before the rapid-buffer factor
   if (bsl != 0.0f) {  // rapid SL buffer (cpu/RunSimulation.cpp:15-22)
     float kc = k.khi + c;
     rca = rca / fmaf(bsl, 1.0f / (kc * kc), 1.0f);
@@ -232,47 +235,6 @@ int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStre
 // ===========================================================================
 // Resident FP32 engine
 // ===========================================================================
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint32_t map_rank(uint32_t addr, uint32_t rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ float4 ld_dsmem_f4(uint32_t addr) {
-  float4 v;
-  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "r"(addr));
-  return v;
-}
-__device__ __forceinline__ int32_t ld_dsmem_s32(uint32_t addr) {
-  int32_t v;
-  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr));
-  return v;
-}
-__device__ __forceinline__ float4 ld_smem_f4(uint32_t addr) {
-  float4 v;
-  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "r"(addr));
-  return v;
-}
-__device__ __forceinline__ void cluster_arrive_wait() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n"
-               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-template <int C>
-__device__ __forceinline__ void step_barrier() {
-  if constexpr (C == 1) {
-    __syncthreads();
-  } else {
-    cluster_arrive_wait();
-  }
-}
-
 // Shared-memory layout of one CTA (dynamic):
 //   float4 buf[2][P]; float4 cm[P]; float imm[P]; float ci[P]; then this
 //   tail, then the channel block (used by rank 0).
@@ -386,7 +348,10 @@ __device__ void resident_prestep(const ResidentArgs& a, RealCtl& ctl, const floa
   __syncwarp();
 }
 
-template <int C>
+// TRAJ: also record, for every step of the launch, the state the step starts
+// from, its Ca rate before the rapid-buffer factor and the channel states it
+// uses (the trajectory the adjoint is conditioned on).
+template <int C, bool TRAJ>
 __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int P = a.P;
@@ -424,6 +389,13 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
   const int n_loc = a.n_local[rank];
   const int n_ch = (rank == 0) ? a.n_chtet[0] : 0;  // channel elements: rank 0 only
   const bool chan_warp = (rank == 0) && (warp == 0);
+  // Element ranges: in partition 0, warp 0 owns the channel elements (which
+  // it gates right after updating them) and the other warps share the rest;
+  // elsewhere every thread strides over the whole partition.
+  const bool split = (rank == 0) && (n_ch > 0) && (nthr > 32);
+  const int e_begin = split ? (warp == 0 ? lane : n_ch + tid - 32) : tid;
+  const int e_end = split ? (warp == 0 ? n_ch : n_loc) : n_loc;
+  const int e_stride = split ? (warp == 0 ? 32 : nthr - 32) : nthr;
   const TetRec* geo = a.geo + (size_t)rank * P;
   const uint32_t off_mask = (1u << a.off_bits) - 1u;
   const Consts32& k = a.k;
@@ -480,13 +452,25 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         const float4* src = cur ? buf1 : buf0;
         float4* dst = cur ? buf0 : buf1;
         const uint32_t* bs = tail->base[cur];
+        if constexpr (TRAJ) {
+          if (chan_warp) {
+            const int W = NR + 2 * NL + 1;
+            int32_t* rec = a.traj_ch + ((size_t)s * a.R + r) * W;
+            for (int q = lane; q < NR; q += 32) rec[q] = s_ryr[q];
+            for (int q = lane; q < NL; q += 32) {
+              rec[NR + q] = s_lcc[q];
+              rec[NR + NL + q] = s_lccv[q];
+            }
+            if (lane == 0) rec[W - 1] = tail->ctl.vsel;
+          }
+        }
         // ---- every element of this partition; the elements that carry
         // channels (head of partition 0) add the release flux of their
         // channels, computed from the state of this step ----------------
         {
           const RealCtl& ctl = tail->ctl;
           const int v = ctl.vsel;
-          for (int i = tid; i < n_loc; i += nthr) {
+          for (int i = e_begin; i < e_end; i += e_stride) {
             const float4* gp = reinterpret_cast<const float4*>(geo + i);
             float4 ga = __ldg(gp);
             float4 gb = __ldg(gp + 1);
@@ -525,8 +509,18 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             }
             float4 out, cm = cmb[i];
             float imo, ci = cib[i];
-            tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci, &out,
-                       &imo);
+            if constexpr (TRAJ) {
+              const size_t o = ((size_t)s * a.R + r) * ((size_t)C * P) + (size_t)rank * P + i;
+              float g;
+              a.traj_u[o] = src[i];
+              a.traj_im[o] = immb[i];
+              tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
+                         &out, &imo, &g);
+              a.traj_g[o] = g;
+            } else {
+              tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
+                         &out, &imo);
+            }
             dst[i] = out;
             immb[i] = imo;
             cmb[i] = cm;
@@ -535,8 +529,9 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
           }
         }
         if (rank == 0) {
-          __syncthreads();  // every channel element of this step is written
+          if (!split) __syncthreads();  // every channel element of this step is written
           if (chan_warp) {
+            __syncwarp();  // warp 0 wrote the channel elements itself
             // ---- gating of this step and protocol of the next ----------------
             RealCtl& ctl = tail->ctl;
             if (!P_.nogating) resident_gate(a, ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
@@ -565,6 +560,11 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         a.I[roff + i] = immb[i];
         a.CM[roff + i] = cmb[i];
         a.CI[roff + i] = cib[i];
+        if constexpr (TRAJ) {
+          const size_t o = ((size_t)a.steps * a.R + r) * ((size_t)C * P) + (size_t)rank * P + i;
+          a.traj_u[o] = fin[i];
+          a.traj_im[o] = immb[i];
+        }
       }
       if (rank == 0) {
         for (int i = tid; i < NR; i += nthr) a.CS.ryr[(size_t)r * NR + i] = s_ryr[i];
@@ -597,19 +597,21 @@ size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries) {
   return b;
 }
 
-template <int C>
+template <int C, bool TRAJ>
 static cudaError_t set_attrs(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_resident32<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_resident32<C, TRAJ>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  if (C > 8) e = cudaFuncSetAttribute(k_resident32<C>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (C > 8)
+    e = cudaFuncSetAttribute(k_resident32<C, TRAJ>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                             1);
   return e;
 }
 
-template <int C>
+template <int C, bool TRAJ>
 static int launch_resident_t(const ResidentArgs& a, int n_clusters, int threads, size_t smem,
                              cudaStream_t st) {
-  if (set_attrs<C>(smem) != cudaSuccess) return -1;
+  if (set_attrs<C, TRAJ>(smem) != cudaSuccess) return -1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n_clusters * C);
   cfg.blockDim = dim3(threads);
@@ -622,13 +624,13 @@ static int launch_resident_t(const ResidentArgs& a, int n_clusters, int threads,
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, k_resident32<C>, a);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_resident32<C, TRAJ>, a);
   return e == cudaSuccess ? 0 : -1;
 }
 
 template <int C>
 static int max_clusters_t(int threads, size_t smem) {
-  if (set_attrs<C>(smem) != cudaSuccess) {
+  if (set_attrs<C, false>(smem) != cudaSuccess || set_attrs<C, true>(smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -644,11 +646,13 @@ static int max_clusters_t(int threads, size_t smem) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_resident32<C>, &cfg) != cudaSuccess) {
+  int n2 = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_resident32<C, false>, &cfg) != cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&n2, k_resident32<C, true>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
-  return n;
+  return n < n2 ? n : n2;
 }
 
 #define SRS_RESIDENT_SIZES(X) X(1) X(2) X(3) X(4) X(5) X(6) X(8) X(16)
@@ -658,7 +662,8 @@ int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, s
   switch (C) {
 #define SRS_L(CC) \
   case CC:        \
-    return launch_resident_t<CC>(a, n_clusters, threads, smem, st);
+    return a.traj_u ? launch_resident_t<CC, true>(a, n_clusters, threads, smem, st)   \
+                    : launch_resident_t<CC, false>(a, n_clusters, threads, smem, st);
     SRS_RESIDENT_SIZES(SRS_L)
 #undef SRS_L
     default: return -1;

@@ -89,6 +89,17 @@ struct srs_sim {
   LinescanArgs ls{};
   std::vector<double> ls_rest;  // F at the equilibrium state
   double* d_ls_out = nullptr;
+  std::vector<int32_t> ls_ptr_h, ls_col_h;  // host copy of the line-scan CSR
+  std::vector<double> ls_w_h;
+  int ls_version = 0;
+  // adjoint (built on first use)
+  float4* d_aT = nullptr;
+  float* d_ryr_s_cl = nullptr;
+  float* d_ryr_s_js = nullptr;
+  int32_t* d_wt_ptr = nullptr;
+  int32_t* d_wt_idx = nullptr;
+  double* d_wt_w = nullptr;
+  int adj_ls_version = -1;
 };
 
 namespace {
@@ -1470,6 +1481,10 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
     s->ls_rest[i] = pd + rest;
   }
   ptr[ns] = (int32_t)col.size();
+  s->ls_ptr_h = ptr;
+  s->ls_col_h = col;
+  s->ls_w_h = w;
+  s->ls_version++;
   LinescanArgs& a = s->ls;
   a.n_samples = ns;
   a.n_state = (int32_t)eng_count(s);
@@ -1507,6 +1522,338 @@ int srs_linescan(srs_sim* s, double* out, double* rest) {
                              cudaMemcpyDeviceToHost, s->st));
   SRS_CUDA(cudaStreamSynchronize(s->st));
   if (rest) std::memcpy(rest, s->ls_rest.data(), sizeof(double) * a.n_samples);
+  return SRS_OK;
+}
+
+static const int kAdjParam[SRS_N_ADJ] = {
+    R_D_CA,      R_D_DYE,       R_K_ON_CMDN, R_K_OFF_CMDN, R_K_ON_TRPN, R_K_OFF_TRPN,
+    R_K_ON_CSQN, R_K_OFF_CSQN,  R_K_ON_DYE,  R_K_OFF_DYE,  R_V_RYR,     R_A_P,
+    R_B_TOT_SL_HI, R_K_D_SL_HI, R_D_ATP,     R_D_CMDN,     R_K_ON_ATP,  R_K_OFF_ATP};
+
+int srs_adjoint_param_index(int k) { return (k >= 0 && k < SRS_N_ADJ) ? kAdjParam[k] : -1; }
+
+}  // extern "C"
+
+namespace {
+
+// Device scratch owned by one srs_adjoint call.
+struct Scratch {
+  std::vector<void*> p;
+  ~Scratch() {
+    for (void* q : p) cudaFree(q);
+  }
+  template <class T>
+  int get(T** out, size_t n) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return fail(SRS_ERR_NOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
+    p.push_back(q);
+    *out = (T*)q;
+    return SRS_OK;
+  }
+};
+
+// Transposed coefficients, RyR volume factors and the element -> sample map
+// of the line scan, in the resident engine layout.
+int adjoint_setup(srs_sim* s) {
+  if (s->d_aT && s->adj_ls_version == s->ls_version) return SRS_OK;
+  const int NE = (int)eng_count(s);
+  if (!s->d_aT) {
+    std::vector<float4> aT(NE, make_float4(0, 0, 0, 0));
+    for (int e = 0; e < NE; ++e) {
+      const int j = s->ref_of_eng[e];
+      if (j < 0) continue;
+      float v[4] = {0, 0, 0, 0};
+      for (int k = 0; k < 4; ++k) {
+        const int nj = s->op.nij[4 * (size_t)j + k];
+        if (nj == j || s->op.aij[5 * (size_t)j + 1 + k] == 0.0) continue;
+        for (int l = 0; l < 4; ++l)
+          if (s->op.nij[4 * (size_t)nj + l] == j) {
+            v[k] = (float)s->op.aij[5 * (size_t)nj + 1 + l];
+            break;
+          }
+      }
+      aT[e] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+    std::vector<float> scl(s->NR), sjs(s->NR);
+    for (int i = 0; i < s->NR; ++i) {
+      scl[i] = (float)(1.0 / s->m.V0[s->m.ryr_ele[i]]);
+      sjs[i] = (float)(-(1.0 / s->m.V0[s->m.ryr_jsr[i]]));
+    }
+    SRS_TRY(dev_upload(s, &s->d_aT, aT.data(), aT.size()));
+    SRS_TRY(dev_upload(s, &s->d_ryr_s_cl, scl.data(), scl.size()));
+    SRS_TRY(dev_upload(s, &s->d_ryr_s_js, sjs.data(), sjs.size()));
+  }
+  const int ns = s->ls.n_samples;
+  std::vector<int32_t> cnt(NE + 1, 0);
+  for (size_t q = 0; q < s->ls_col_h.size(); ++q) cnt[s->ls_col_h[q] + 1]++;
+  for (int e = 0; e < NE; ++e) cnt[e + 1] += cnt[e];
+  std::vector<int32_t> idx(s->ls_col_h.size());
+  std::vector<double> wv(s->ls_col_h.size());
+  std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int i = 0; i < ns; ++i)
+    for (int q = s->ls_ptr_h[i]; q < s->ls_ptr_h[i + 1]; ++q) {
+      const int e = s->ls_col_h[q];
+      idx[fill[e]] = i;
+      wv[fill[e]] = s->ls_w_h[q];
+      fill[e]++;
+    }
+  SRS_TRY(dev_upload(s, &s->d_wt_ptr, cnt.data(), cnt.size()));
+  SRS_TRY(dev_upload(s, &s->d_wt_idx, idx.data(), idx.size()));
+  SRS_TRY(dev_upload(s, &s->d_wt_w, wv.data(), wv.size()));
+  s->adj_ls_version = s->ls_version;
+  return SRS_OK;
+}
+
+// Device copies of the complete engine state of all realizations.
+struct StateSnap {
+  float4* M;
+  float* I;
+  float4* CM;
+  float* CI;
+  int32_t *ryr, *lcc, *lccv;
+  double* res;
+  RealCtl* ctl;
+};
+
+int snap_alloc(srs_sim* s, Scratch& sc, StateSnap* o) {
+  const size_t n = (size_t)s->R * eng_count(s);
+  SRS_TRY(sc.get(&o->M, n));
+  SRS_TRY(sc.get(&o->I, n));
+  SRS_TRY(sc.get(&o->CM, n));
+  SRS_TRY(sc.get(&o->CI, n));
+  SRS_TRY(sc.get(&o->ryr, (size_t)s->R * s->NR));
+  SRS_TRY(sc.get(&o->lcc, (size_t)s->R * s->NL));
+  SRS_TRY(sc.get(&o->lccv, (size_t)s->R * s->NL));
+  SRS_TRY(sc.get(&o->res, (size_t)s->R * s->NCH));
+  SRS_TRY(sc.get(&o->ctl, (size_t)s->R));
+  return SRS_OK;
+}
+
+int snap_copy(srs_sim* s, const StateSnap& o, bool save) {
+  const size_t n = (size_t)s->R * eng_count(s);
+  auto cp = [&](void* snap, void* live, size_t bytes) -> cudaError_t {
+    return save ? cudaMemcpyAsync(snap, live, bytes, cudaMemcpyDeviceToDevice, s->st)
+                : cudaMemcpyAsync(live, snap, bytes, cudaMemcpyDeviceToDevice, s->st);
+  };
+  SRS_CUDA(cp(o.M, s->d_M[0], n * sizeof(float4)));
+  SRS_CUDA(cp(o.I, s->d_I[0], n * sizeof(float)));
+  SRS_CUDA(cp(o.CM, s->d_CM, n * sizeof(float4)));
+  SRS_CUDA(cp(o.CI, s->d_CI, n * sizeof(float)));
+  SRS_CUDA(cp(o.ryr, s->d_ryr, (size_t)s->R * s->NR * 4));
+  SRS_CUDA(cp(o.lcc, s->d_lcc, (size_t)s->R * s->NL * 4));
+  SRS_CUDA(cp(o.lccv, s->d_lccv, (size_t)s->R * s->NL * 4));
+  SRS_CUDA(cp(o.res, s->d_res, (size_t)s->R * s->NCH * 8));
+  SRS_CUDA(cp(o.ctl, s->d_ctl, (size_t)s->R * sizeof(RealCtl)));
+  return SRS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
+  if (!s || !d || !out || !out->loss || !out->grad || !d->f0) return fail(SRS_ERR_INPUT, "null argument");
+  if (s->d.precision != SRS_FP32 || s->d.engine != SRS_ENGINE_RESIDENT)
+    return fail(SRS_ERR_UNSUPPORTED, "the adjoint runs on the FP32 resident engine");
+  if (!s->ls.ptr) return fail(SRS_ERR_STATE, "call srs_linescan_setup first");
+  if (d->n_steps < 1 || d->tick_every < 1 || d->checkpoint_every < 0)
+    return fail(SRS_ERR_INPUT, "n_steps and tick_every must be positive");
+  const int K = d->checkpoint_every > 0 ? d->checkpoint_every : 256;
+  const int R = s->R, NR = s->NR, NL = s->NL, W = NR + 2 * NL + 1, te = d->tick_every;
+  const size_t NE = eng_count(s);
+  const int ns = s->ls.n_samples;
+  const int64_t n_steps = d->n_steps, n_ticks = n_steps / te;
+  const int64_t nseg = (n_steps + K - 1) / K;
+  SRS_TRY(adjoint_setup(s));
+  // memory: checkpoints (nseg + 1), one segment of trajectory, lambda
+  const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
+                        (size_t)R * sizeof(RealCtl);
+  const size_t traj_b = (size_t)(K + 1) * R * NE * 20 + (size_t)K * R * NE * 4 + (size_t)K * R * W * 4;
+  const size_t need = snap_b * (size_t)(nseg + 1) + traj_b + (size_t)R * NE * 40 +
+                      (size_t)(K / te + 2) * R * ns * 8 + (size_t)R * n_ticks * ns * 8;
+  size_t free_b = 0, total_b = 0;
+  SRS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (need > free_b / 10 * 9)
+    return fail(SRS_ERR_NOMEM, "adjoint needs " + std::to_string(need >> 20) + " MiB of device memory (" +
+                                   std::to_string(free_b >> 20) + " MiB free): raise checkpoint_every "
+                                   "or lower n_steps");
+  Scratch sc;
+  std::vector<StateSnap> ck(nseg + 1);
+  for (auto& c : ck) SRS_TRY(snap_alloc(s, sc, &c));
+  float4* traj_u;
+  float *traj_im, *traj_g;
+  int32_t* traj_ch;
+  SRS_TRY(sc.get(&traj_u, (size_t)(K + 1) * R * NE));
+  SRS_TRY(sc.get(&traj_im, (size_t)(K + 1) * R * NE));
+  SRS_TRY(sc.get(&traj_g, (size_t)K * R * NE));
+  SRS_TRY(sc.get(&traj_ch, (size_t)K * R * W));
+  float4 *lam, *lam_c4;
+  float *lam_im, *lam_cim;
+  SRS_TRY(sc.get(&lam, (size_t)R * NE));
+  SRS_TRY(sc.get(&lam_c4, (size_t)R * NE));
+  SRS_TRY(sc.get(&lam_im, (size_t)R * NE));
+  SRS_TRY(sc.get(&lam_cim, (size_t)R * NE));
+  double *coef, *grad, *loss, *f0, *target = nullptr;
+  SRS_TRY(sc.get(&coef, (size_t)(K / te + 2) * R * ns));
+  SRS_TRY(sc.get(&grad, (size_t)R * SRS_N_ADJ));
+  SRS_TRY(sc.get(&loss, (size_t)R));
+  SRS_TRY(sc.get(&f0, (size_t)ns));
+  SRS_CUDA(cudaMemcpyAsync(f0, d->f0, sizeof(double) * ns, cudaMemcpyHostToDevice, s->st));
+  if (d->target && n_ticks > 0) {
+    SRS_TRY(sc.get(&target, (size_t)R * n_ticks * ns));
+    SRS_CUDA(cudaMemcpyAsync(target, d->target, sizeof(double) * R * n_ticks * ns,
+                             cudaMemcpyHostToDevice, s->st));
+  }
+  s->P.run_protocol = 0;
+  refresh_args(s);
+  // ---- forward with checkpoints ------------------------------------------------
+  for (int64_t k = 0; k < nseg; ++k) {
+    SRS_TRY(snap_copy(s, ck[k], true));
+    SRS_TRY(resident_launch(s, (int)std::min<int64_t>(K, n_steps - k * K)));
+  }
+  SRS_TRY(snap_copy(s, ck[nseg], true));
+  {
+    std::vector<RealCtl> ctl(R);
+    SRS_CUDA(cudaMemcpyAsync(ctl.data(), ck[nseg].ctl, sizeof(RealCtl) * R, cudaMemcpyDeviceToHost, s->st));
+    SRS_CUDA(cudaStreamSynchronize(s->st));
+    for (auto& c : ctl) {
+      if (c.status & 1u) return fail(SRS_ERR_NONFINITE, "a realization produced a non-finite Ca value");
+      if (c.done) return fail(SRS_ERR_STATE, "a realization is finished; reset it before the adjoint");
+    }
+  }
+  // ---- reverse sweep -----------------------------------------------------------
+  SRS_CUDA(cudaMemsetAsync(lam, 0, sizeof(float4) * R * NE, s->st));
+  SRS_CUDA(cudaMemsetAsync(lam_c4, 0, sizeof(float4) * R * NE, s->st));
+  SRS_CUDA(cudaMemsetAsync(lam_im, 0, sizeof(float) * R * NE, s->st));
+  SRS_CUDA(cudaMemsetAsync(lam_cim, 0, sizeof(float) * R * NE, s->st));
+  SRS_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * R * SRS_N_ADJ, s->st));
+  SRS_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * R, s->st));
+  AdjArgs aa{};
+  aa.R = R;
+  aa.P = s->P_stride;
+  aa.off_bits = s->off_bits;
+  aa.geo = s->ar.geo;
+  aa.aT = s->d_aT;
+  aa.n_local = s->ar.n_local;
+  aa.n_chtet = s->ar.n_chtet;
+  aa.ch_ptr = s->ar.ch_ptr;
+  aa.ch_list = s->ar.ch_list;
+  aa.ryr_cleft_code = s->ar.ryr_cleft_code;
+  aa.ryr_jsr_code = s->ar.ryr_jsr_code;
+  aa.ryr_s_cl = s->d_ryr_s_cl;
+  aa.ryr_s_js = s->d_ryr_s_js;
+  aa.NR = NR;
+  aa.NL = NL;
+  aa.traj_u = traj_u;
+  aa.traj_im = traj_im;
+  aa.traj_g = traj_g;
+  aa.traj_ch = traj_ch;
+  aa.tick_every = te;
+  aa.n_samples = ns;
+  aa.coef = coef;
+  aa.wt_ptr = s->d_wt_ptr;
+  aa.wt_idx = s->d_wt_idx;
+  aa.wt_w = s->d_wt_w;
+  aa.lam = lam;
+  aa.lam_im = lam_im;
+  aa.lam_c4 = lam_c4;
+  aa.lam_cim = lam_cim;
+  aa.grad = grad;
+  aa.k = s->ar.k;
+  {
+    const RestValues& rv = s->rv;
+    const double brest[5] = {rv.dye, rv.atp, rv.cmdn, rv.trpn, rv.csqn};
+    for (int q = 0; q < 5; ++q) aa.ak.brest[q] = (float)brest[q];
+    const double bt = s->p.reals[R_B_TOT_SL_HI];
+    aa.ak.inv_btot_sl = bt != 0.0 ? (float)(1.0 / bt) : 0.0f;
+    aa.ak.serca_per_ap = 2e-3f;
+    aa.ak.v_cell = (float)s->p.reals[R_V_CELL];
+  }
+  const int n_ent = 2 * NR + NL;
+  const size_t adj_smem = adjoint_smem_bytes(s->P_stride, s->part_nch[0], n_ent);
+  const int adj_threads = 512;
+  const int adj_ncl = std::min(adjoint_max_clusters(s->C, adj_threads, adj_smem), R);
+  if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
+  AdjTickArgs ta{};
+  ta.n_samples = ns;
+  ta.n_state = (int32_t)NE;
+  ta.n_ticks = (int32_t)n_ticks;
+  ta.ptr = s->ls.ptr;
+  ta.col = s->ls.col;
+  ta.w = s->ls.w;
+  ta.pad = s->ls.pad;
+  ta.f0 = f0;
+  ta.target = target;
+  ta.rest_dye = s->ls.rest_dye;
+  ta.loss = loss;
+  for (int64_t k = nseg - 1; k >= 0; --k) {
+    const int64_t s0 = k * K;
+    const int len = (int)std::min<int64_t>(K, n_steps - s0);
+    SRS_TRY(snap_copy(s, ck[k], false));
+    ResidentArgs ra = s->ar;
+    ra.steps = len;
+    ra.prestep_first = 0;
+    ra.initial_row = 0;
+    ra.traj_u = traj_u;
+    ra.traj_im = traj_im;
+    ra.traj_g = traj_g;
+    ra.traj_ch = traj_ch;
+    if (launch_resident(ra, s->C, s->n_clusters, s->threads, s->smem, s->st))
+      return fail(SRS_ERR_CUDA, std::string("trajectory launch: ") + cudaGetErrorString(cudaGetLastError()));
+    s->launches++;
+    for (int64_t n = (s0 / te + 1) * te; n <= s0 + len; n += te) {
+      ta.tick = (int32_t)(n / te - 1);
+      ta.traj_u = traj_u + (size_t)(n - s0) * R * NE;
+      ta.coef = coef + (size_t)(n / te - s0 / te - 1) * R * ns;
+      if (launch_adj_tick(ta, R, s->st)) return fail(SRS_ERR_CUDA, "tick launch failed");
+      s->launches++;
+    }
+    aa.n_steps = len;
+    aa.s0 = s0;
+    if (launch_adjoint(aa, s->C, adj_ncl, adj_threads, adj_smem, s->st))
+      return fail(SRS_ERR_CUDA, std::string("adjoint launch: ") + cudaGetErrorString(cudaGetLastError()));
+    s->launches++;
+  }
+  SRS_TRY(snap_copy(s, ck[nseg], false));
+  SRS_CUDA(cudaMemcpyAsync(out->loss, loss, sizeof(double) * R, cudaMemcpyDeviceToHost, s->st));
+  SRS_CUDA(cudaMemcpyAsync(out->grad, grad, sizeof(double) * R * SRS_N_ADJ, cudaMemcpyDeviceToHost, s->st));
+  std::vector<float4> hl, hc;
+  std::vector<float> hi, hci;
+  if (out->grad_state) {
+    hl.resize((size_t)R * NE);
+    hc.resize((size_t)R * NE);
+    hi.resize((size_t)R * NE);
+    hci.resize((size_t)R * NE);
+    SRS_CUDA(cudaMemcpyAsync(hl.data(), lam, sizeof(float4) * R * NE, cudaMemcpyDeviceToHost, s->st));
+    SRS_CUDA(cudaMemcpyAsync(hc.data(), lam_c4, sizeof(float4) * R * NE, cudaMemcpyDeviceToHost, s->st));
+    SRS_CUDA(cudaMemcpyAsync(hi.data(), lam_im, sizeof(float) * R * NE, cudaMemcpyDeviceToHost, s->st));
+    SRS_CUDA(cudaMemcpyAsync(hci.data(), lam_cim, sizeof(float) * R * NE, cudaMemcpyDeviceToHost, s->st));
+  }
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  SRS_CUDA(cudaGetLastError());
+  if (out->grad_state) {
+    const int N = s->N;
+    for (int r = 0; r < R; ++r) {
+      double* g = out->grad_state + (size_t)r * 6 * N;
+      for (int j = 0; j < N; ++j) {
+        const size_t e = (size_t)r * NE + s->eng_of_ref[j];
+        const float4 L = hl[e], Cc = hc[e];
+        const double li = (double)hi[e] - (double)hci[e];
+        const bool jsr = s->m.domain[j] == DOMAIN_JSR;
+        g[SP_CA * (size_t)N + j] = (double)L.x - (double)Cc.x;
+        g[SP_ATP * (size_t)N + j] = (double)L.y - (double)Cc.y;
+        g[SP_CMDN * (size_t)N + j] = (double)L.z - (double)Cc.z;
+        g[SP_DYE * (size_t)N + j] = (double)L.w - (double)Cc.w;
+        g[SP_TRPN * (size_t)N + j] = (!jsr && s->m.tropc[j]) ? li : 0.0;
+        g[SP_CSQN * (size_t)N + j] = jsr ? li : 0.0;
+      }
+    }
+  }
+  for (int r = 0; r < R; ++r)
+    for (int p = 0; p < SRS_N_ADJ; ++p)
+      if (!std::isfinite(out->grad[(size_t)r * SRS_N_ADJ + p]))
+        return fail(SRS_ERR_NONFINITE, "non-finite adjoint gradient");
   return SRS_OK;
 }
 

@@ -110,6 +110,15 @@ struct ResidentArgs {
   Protocol P_;
   Channels C;
   ChanState CS;
+  // Trajectory recording (null: off).  Step s of the launch stores the state
+  // it starts from (traj_u/traj_im slot s), its Ca rate before the rapid-buffer
+  // factor (traj_g slot s) and the channel states it uses (traj_ch slot s:
+  // RyR[NR], LCC[NL], LCC V-gate[NL], voltage selector); slot `steps` of
+  // traj_u/traj_im holds the final state.  Layout [slot][R][C*P].
+  float4* traj_u;
+  float* traj_im;
+  float* traj_g;
+  int32_t* traj_ch;
 };
 // Line scan: F[r][i] = pad[i] + sum_q w[q] * dye(col[q]) over ptr[i]..ptr[i+1].
 struct LinescanArgs {
@@ -126,6 +135,69 @@ struct LinescanArgs {
   double* out;           // [R][n_samples]
 };
 int launch_linescan(const LinescanArgs& a, int R, cudaStream_t st);
+
+// ---- pathwise adjoint (k_adjoint.cu) ---------------------------------------
+// FP32 constants of the Jacobian beyond Consts32.
+struct AdjConsts {
+  float brest[5];      // resting bound buffer: dye, ATP, CMDN, TRPN, CSQN
+  float inv_btot_sl;   // 1 / B_TOT_SL_HI (0 when B_TOT_SL_HI = 0)
+  float serca_per_ap;  // dF_Ca/dA_P = -serca_per_ap * v_cycle / B
+  float v_cell;        // V_CELL
+};
+
+struct AdjArgs {
+  int32_t R, P, off_bits;
+  int32_t n_steps;  // steps of the segment; the kernel runs t = n_steps .. 1
+  int64_t s0;       // global index of the state the segment starts from
+  const TetRec* geo;
+  const float4* aT;  // [C*P] coefficient of this element in each neighbour's row
+  const int32_t* n_local;
+  const int32_t* n_chtet;
+  const int32_t* ch_ptr;
+  const ChanEntry32* ch_list;
+  const uint16_t* ryr_cleft_code;
+  const uint16_t* ryr_jsr_code;
+  const float* ryr_s_cl;  // +1/V0 of each RyR's cleft element
+  const float* ryr_s_js;  // -1/V0 of each RyR's JSR element
+  int32_t NR, NL;
+  const float4* traj_u;    // trajectory of the segment (ResidentArgs layout)
+  const float* traj_im;
+  const float* traj_g;
+  const int32_t* traj_ch;
+  int32_t tick_every;      // loss ticks at global steps that are multiples
+  int32_t n_samples;
+  const double* coef;      // [tick slot][R][n_samples] dL/dF at the ticks of the segment
+  const int32_t* wt_ptr;   // [C*P + 1] element -> line-scan samples
+  const int32_t* wt_idx;
+  const double* wt_w;
+  float4* lam;   // [R][C*P] (Ca, ATP, CMDN, dye)
+  float* lam_im; // [R][C*P] immobile buffer
+  float4* lam_c4;  // Kahan compensation
+  float* lam_cim;
+  double* grad;  // [R][SRS_N_ADJ]
+  Consts32 k;
+  AdjConsts ak;
+};
+
+struct AdjTickArgs {
+  int32_t n_samples, n_state, n_ticks, tick;
+  const int32_t* ptr;
+  const int32_t* col;
+  const double* w;
+  const double* pad;
+  const double* f0;
+  const double* target;  // [R][n_ticks][n_samples] or null
+  const double* rest_dye;
+  const float4* traj_u;  // trajectory slot [R][n_state]
+  double* coef;          // [R][n_samples]
+  double* loss;          // [R]
+};
+
+size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries);
+int launch_adjoint(const AdjArgs& a, int C, int n_clusters, int threads, size_t smem,
+                   cudaStream_t st);
+int adjoint_max_clusters(int C, int threads, size_t smem);
+int launch_adj_tick(const AdjTickArgs& a, int R, cudaStream_t st);
 
 // Host-side constants (double precision, from the parameter set and the
 // membrane potential V): gating rates and the LCC flux terms.

@@ -1,0 +1,155 @@
+"""Device pathwise adjoint (srs_adjoint) against the FP64 oracle adjoint and
+against central finite differences of the device FP64 engine.
+
+Workload: the golden mesh, 4 realizations (seeds 11..14) from their reset
+state, 600 explicit steps with Philox gating, the x line scan of
+linescan/DefaultScan.xml sampled every 100 steps, loss
+  L_r = 1/2 sum_k sum_i (F_ki / F0_i - 1 - target_rki)^2,
+checkpoints every 200 steps (ticks fall on segment boundaries).
+Tolerances: loss 1e-5 relative (FP32 trajectory against FP64), gradients
+1e-3 relative (the finite-difference bar).
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_MESH, LINESCAN_DESC, linescan_weights, params_from_golden
+
+pytestmark = pytest.mark.gpu
+
+N_STEPS, TICK, K = 600, 100, 200
+SEEDS = [11, 12, 13, 14]
+
+
+def _params(srs):
+    p, _ = params_from_golden(srs, "spark")
+    p.ints[srs.I["FLAG_NO_FLUX_BOUNDARY"]] = 1
+    p.ints[srs.I["FLAG_NO_GATING"]] = 0
+    return p
+
+
+def _start(srs, p, precision, engine):
+    g = srs.Grid(p, GOLDEN_MESH)
+    sim = srs.Simulation(g, p, len(SEEDS), precision, engine, seeds=SEEDS)
+    sim.reset()
+    sim.linescan_setup(**LINESCAN_DESC)
+    return g, sim
+
+
+@pytest.fixture(scope="module")
+def case(srs):
+    p = _params(srs)
+    g, sim = _start(srs, p, srs.FP32, srs.ENGINE_RESIDENT)
+    _, f0 = sim.linescan()
+    start = [sim.get_state(r) for r in range(len(SEEDS))]
+    rng = np.random.default_rng(3)
+    target = rng.standard_normal((len(SEEDS), N_STEPS // TICK, len(f0))) * 0.01
+    loss, grad, gs = sim.adjoint(N_STEPS, TICK, f0, target, checkpoint_every=K, grad_state=True)
+    return dict(p=p, g=g, sim=sim, f0=f0, start=start, target=target, loss=loss, grad=grad, gs=gs)
+
+
+def test_adjoint_matches_fp64_oracle(srs, oracle, case):
+    from oracle import Mesh
+    p, g = case["p"], case["g"]
+    W, pad = linescan_weights(g)
+    m = Mesh(oracle, GOLDEN_MESH, 1, np.array(p.reals[:]))
+    ints = np.array(p.ints[:], np.int32)
+    N = g.n_ele
+    for r, seed in enumerate(SEEDS):
+        st = case["start"][r]
+        L, go, lam0 = m.adjoint(ints, st["states"], st, seed, N_STEPS, TICK, W, pad, case["f0"],
+                                case["target"][r], grad_state=True)
+        assert abs(case["loss"][r] - L) <= 1e-5 * L
+        scale = np.abs(go)
+        for k in range(srs.N_ADJ):
+            if scale[k] == 0:
+                continue
+            assert abs(case["grad"][r, k] - go[k]) <= 1e-3 * scale[k], (r, srs.ADJ_PARAMS[k],
+                                                                       case["grad"][r, k], go[k])
+        # dL/dS0: species by species, relative to the largest sensitivity
+        gs = case["gs"][r].reshape(-1)
+        for sp in range(6):
+            a, b = gs[sp * N:(sp + 1) * N], lam0[sp * N:(sp + 1) * N]
+            ref = np.abs(b).max()
+            if ref > 0:
+                assert np.abs(a - b).max() <= 1e-3 * ref, (r, sp)
+
+
+def test_adjoint_matches_fp64_finite_differences(srs, case):
+    """Central differences of the FP64 plain engine from the same start state
+    with the same seeds (common random numbers), h = 1e-4 |theta|."""
+    p0, f0, target = case["p"], case["f0"], case["target"]
+
+    def loss_of(p):
+        _, sim = _start(srs, p, srs.FP64, srs.ENGINE_PLAIN)
+        for r, st in enumerate(case["start"]):
+            sim.set_state(r, st["states"], st["ryr"], st["lcc"], st["lccv"], st["residuals"])
+        L = np.zeros(len(SEEDS))
+        for k in range(N_STEPS // TICK):
+            sim.explicit_step(TICK)
+            F, _ = sim.linescan()
+            e = F / f0[None, :] - 1.0 - target[:, k, :]
+            L += 0.5 * (e * e).sum(axis=1)
+        return L
+
+    L0 = loss_of(p0)
+    assert np.allclose(L0, case["loss"], rtol=1e-5)
+    checked = 0
+    for k, name in enumerate(srs.ADJ_PARAMS):
+        idx = srs.R[name]
+        h = 1e-4 * abs(p0.reals[idx])
+        hi, lo = p0.copy(), p0.copy()
+        hi.reals[idx] += h
+        lo.reals[idx] -= h
+        Lp, Lm = loss_of(hi), loss_of(lo)
+        if np.abs(Lp - Lm).sum() < 1e-9 * L0.sum():
+            continue  # below the loss's rounding
+        fd = (Lp - Lm).sum() / (2 * h)
+        adj = case["grad"][:, k].sum()
+        assert abs(adj - fd) <= 1e-3 * abs(fd), (name, adj, fd)
+        checked += 1
+    assert checked >= 12
+
+
+@pytest.mark.parametrize("K2,C", [(0, 1), (600, 2), (150, 3)])
+def test_adjoint_segmentation_and_cluster_size_do_not_change_the_result(srs, case, K2, C):
+    """The trajectory and lambda are bit-identical for any checkpoint interval
+    and cluster size; only the grouping of the FP32 partial sums of the
+    gradient changes (1e-6)."""
+    p = case["p"]
+    g = srs.Grid(p, GOLDEN_MESH)
+    sim = srs.Simulation(g, p, len(SEEDS), srs.FP32, srs.ENGINE_RESIDENT, seeds=SEEDS, cluster_size=C)
+    assert sim.config()["cluster_size"] == C
+    sim.reset()
+    sim.linescan_setup(**LINESCAN_DESC)
+    loss, grad, gs = sim.adjoint(N_STEPS, TICK, case["f0"], case["target"], checkpoint_every=K2,
+                                 grad_state=True)
+    assert np.array_equal(loss, case["loss"])
+    assert np.array_equal(gs, case["gs"])
+    assert np.allclose(grad, case["grad"], rtol=1e-6, atol=0)
+
+
+def test_adjoint_leaves_the_state_after_n_steps(srs, case):
+    p = case["p"]
+    _, ref = _start(srs, p, srs.FP32, srs.ENGINE_RESIDENT)
+    ref.explicit_step(N_STEPS)
+    for r in range(len(SEEDS)):
+        a, b = case["sim"].get_state(r), ref.get_state(r)
+        for key in ("states", "ryr", "lcc", "lccv", "residuals"):
+            assert np.array_equal(a[key], b[key]), key
+
+
+def test_adjoint_rejects_unsupported_configurations(srs, case):
+    p = case["p"]
+    _, plain = _start(srs, p, srs.FP32, srs.ENGINE_PLAIN)
+    with pytest.raises(srs.SrsError) as e:
+        plain.adjoint(10, 5, case["f0"])
+    assert e.value.status == -6  # SRS_ERR_UNSUPPORTED
+    g = srs.Grid(p, GOLDEN_MESH)
+    s2 = srs.Simulation(g, p, 1, srs.FP32, srs.ENGINE_RESIDENT, seeds=[1])
+    with pytest.raises(ValueError):
+        s2.adjoint(10, 5, case["f0"])  # no line scan set up
+    s2.reset()
+    s2.linescan_setup(**LINESCAN_DESC)
+    with pytest.raises(srs.SrsError) as e:
+        s2.adjoint(0, 5, case["f0"])
+    assert e.value.status == -1  # SRS_ERR_INPUT
