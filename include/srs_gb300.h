@@ -236,12 +236,16 @@ enum {
   SRS_ADJ_K_ON_ATP = 16,
   SRS_ADJ_K_OFF_ATP = 17
 };
+/* flags: SRS_ADJ_LAMBDA_GLOBAL keeps the adjoint state in global memory even
+ * where it fits on chip (the path taken for partitions too large for it). */
+#define SRS_ADJ_LAMBDA_GLOBAL 1
 typedef struct srs_adjoint_desc {
   int64_t n_steps;
   int tick_every;
   int checkpoint_every;
   const double* f0;      /* [n_samples] reference fluorescence F0 */
   const double* target;  /* [R][n_steps/tick_every][n_samples], or NULL (zero) */
+  int flags;
 } srs_adjoint_desc;
 typedef struct srs_adjoint_out {
   double* loss;        /* [R] */

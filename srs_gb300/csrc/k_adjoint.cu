@@ -65,17 +65,48 @@ __device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& a
 }  // namespace
 
 // Shared memory: float4 pub[2][P]; double red[32][NA]; int32 cptr[n_ch+1];
-// ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16].
-size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries) {
+// ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16]; then, when
+// `own_in_smem`, the owner state float4 c4[P], float lc[P], lim[P], cim[P].
+size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem) {
   size_t b = (size_t)2 * P * sizeof(float4);
   b += (size_t)32 * NA * sizeof(double);
   b += (size_t)(n_chtet + 1) * sizeof(int32_t);
   b = (b + 15) & ~(size_t)15;
   b += (size_t)n_entries * sizeof(ChanEntry32);
   b += 2 * 16 * sizeof(uint32_t);
+  if (own_in_smem) b += (size_t)P * (3 * sizeof(float) + sizeof(float4));
   return b;
 }
 
+namespace {
+
+// dL/dF injection of the tick at step n (0 when n is not a tick).
+__device__ __forceinline__ float tick_injection(const AdjArgs& a, int64_t n, int r, int e) {
+  if (a.tick_every <= 0 || n <= a.s0 || (n % a.tick_every) != 0) return 0.0f;
+  const int64_t slot = n / a.tick_every - a.s0 / a.tick_every - 1;
+  const double* coef = a.coef + ((size_t)slot * a.R + r) * a.n_samples;
+  double inj = 0.0;
+  for (int q = a.wt_ptr[e]; q < a.wt_ptr[e + 1]; ++q) inj += coef[a.wt_idx[q]] * a.wt_w[q];
+  return (float)inj;
+}
+
+// Rapid-buffer factor B(c) of UpdateFastBuffer (cpu/RunSimulation.cpp:15-22),
+// evaluated exactly as the forward engine evaluates it.
+__device__ __forceinline__ float sl_factor(const Consts32& k, float bsl, float c) {
+  if (bsl == 0.0f) return 1.0f;
+  const float kc = k.khi + c;
+  return fmaf(bsl, 1.0f / (kc * kc), 1.0f);
+}
+
+}  // namespace
+
+// Per step t = n_steps .. 1 of the segment (x_{n-1} -> x_n, n = s0 + t), after
+// one cluster barrier, every element reads the published slots of its
+// neighbours (pub[cur]), forms lambda_{n-1} and publishes it into pub[cur^1]
+// for the next step: lambda_ATP/CMDN/dye as they are (pub is their owner
+// storage during the segment) and lambda_Ca / B(x_{n-2}), with the tick
+// injection of step n-1 already added.  The last step writes lambda_{s0}
+// back to the global arrays for the next segment.
 template <int C>
 __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -89,6 +120,10 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       (reinterpret_cast<uintptr_t>(s_cptr + n_ch0 + 1) + 15) & ~(uintptr_t)15);
   const int n_ent = a.ch_ptr[n_ch0];
   uint32_t* s_base = reinterpret_cast<uint32_t*>(s_clist + n_ent);  // [2][16]
+  float4* sm_c4 = reinterpret_cast<float4*>(s_base + 32);
+  float* sm_lc = reinterpret_cast<float*>(sm_c4 + P);
+  float* sm_lim = sm_lc + P;
+  float* sm_cim = sm_lim + P;
 
   uint32_t rank = 0;
   if constexpr (C > 1) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
@@ -116,44 +151,42 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 
   for (int r = cid; r < a.R; r += ncl) {
     const size_t roff = (size_t)r * NE + (size_t)rank * P;  // lambda, this partition
+    // owner state: on chip when it fits, else the global arrays themselves
+    float* lc = a.own_in_smem ? sm_lc : a.lam_c + roff;
+    float* lim = a.own_in_smem ? sm_lim : a.lam_im + roff;
+    float* cim = a.own_in_smem ? sm_cim : a.lam_cim + roff;
+    float4* c4 = a.own_in_smem ? sm_c4 : a.lam_c4 + roff;
+    const int len = a.n_steps;
+    // ---- publish lambda_{s1} (with the tick injection of step s1) ----------
+    {
+      const size_t xo = ((size_t)(len - 1) * a.R + r) * NE + (size_t)rank * P;
+      for (int i = tid; i < n_loc; i += nthr) {
+        const float4 L = a.lam[roff + i];
+        const float4 gb = __ldg(reinterpret_cast<const float4*>(geo + i) + 1);
+        const uint32_t fl = __float_as_uint(gb.w);
+        const float c = ((fl & 1u) ? k.c0j : k.c0) + a.traj_u[xo + i].x;
+        const float inj = tick_injection(a, a.s0 + len, r, (int)(rank * P + i));
+        pub0[i] = make_float4(L.x / sl_factor(k, gb.z, c), L.y, L.z, L.w + inj);
+        lc[i] = L.x;
+        if (a.own_in_smem) {
+          lim[i] = a.lam_im[roff + i];
+          cim[i] = a.lam_cim[roff + i];
+          c4[i] = a.lam_c4[roff + i];
+        }
+      }
+    }
     KSum gs;
 #pragma unroll
     for (int p = 0; p < NA; ++p) gs.s[p] = gs.c[p] = 0.0f;
     int cur = 0;
-    for (int t = a.n_steps; t >= 1; --t) {
-      const int64_t n = a.s0 + t;  // step x_{n-1} -> x_n
-      float4* pub = cur ? pub1 : pub0;
+    for (int t = len; t >= 1; --t) {
+      step_barrier<C>();
+      const int64_t n = a.s0 + t;  // this step maps x_{n-1} to x_n
+      const float4* pub = cur ? pub1 : pub0;
+      float4* nxt = cur ? pub0 : pub1;
       const uint32_t* bs = s_base + 16 * cur;
       const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * P;
-      const bool tick = a.tick_every > 0 && (n % a.tick_every) == 0;
-      const double* coef = nullptr;
-      if (tick) {
-        const int64_t slot = n / a.tick_every - a.s0 / a.tick_every - 1;
-        coef = a.coef + ((size_t)slot * a.R + r) * a.n_samples;
-      }
-      // ---- publish lambda_n (with the tick injection of step n) --------
-      for (int i = tid; i < n_loc; i += nthr) {
-        float4 L = a.lam[roff + i];
-        if (tick) {
-          const int e = (int)(rank * P + i);
-          double inj = 0.0;
-          for (int q = a.wt_ptr[e]; q < a.wt_ptr[e + 1]; ++q) inj += coef[a.wt_idx[q]] * a.wt_w[q];
-          L.w += (float)inj;
-        }
-        const float4* gp = reinterpret_cast<const float4*>(geo + i);
-        const float4 gb = __ldg(gp + 1);
-        const float bsl = gb.z;
-        const uint32_t fl = __float_as_uint(gb.w);
-        const float c = ((fl & 1u) ? k.c0j : k.c0) + a.traj_u[xoff + i].x;
-        float B = 1.0f;
-        if (bsl != 0.0f) {
-          const float kc = k.khi + c;
-          B = fmaf(bsl, 1.0f / (kc * kc), 1.0f);
-        }
-        pub[i] = make_float4(L.x / B, L.y, L.z, L.w);
-      }
-      step_barrier<C>();
-      // ---- lambda_{n-1} = lambda_n + dt J(x_{n-1})^T lambda_n ----------
+      const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * P;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       for (int i = tid; i < n_loc; i += nthr) {
         const float4 x = a.traj_u[xoff + i];
@@ -212,7 +245,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         g[SRS_ADJ_D_DYE] = x.w * Sy;
         float oc = k.D[0] * Sc, oa = k.D[1] * Sa, om = k.D[2] * Sm, oy = k.D[3] * Sy, oi = 0.0f;
         const float w = me.x;
-        const float lim = a.lam_im[roff + i];
+        const float li = lim[i];
         float dG = 0.0f;
         const bool jsr = (fl & 1u) != 0;
         const float c = (jsr ? k.c0j : k.c0) + x.x;
@@ -221,7 +254,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           adj_buffer(k, ak, 1, c, x.y, me.y, w, oa, oc, dG, g, SRS_ADJ_K_ON_ATP);
           adj_buffer(k, ak, 2, c, x.z, me.z, w, om, oc, dG, g, SRS_ADJ_K_ON_CMDN);
           if (fl & 2u) {
-            adj_buffer(k, ak, 3, c, xim, lim, w, oi, oc, dG, g, SRS_ADJ_K_ON_TRPN);
+            adj_buffer(k, ak, 3, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_TRPN);
             // SERCA v(Ki), Ki = (c / K_D_i)^2 (cpu/RunSimulation.cpp:83-91)
             float Ki = c * k.inv_kdi;
             Ki = Ki * Ki;
@@ -235,7 +268,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
             g[SRS_ADJ_A_P] = -w * ak.serca_per_ap * v;
           }
         } else {
-          adj_buffer(k, ak, 4, c, xim, lim, w, oi, oc, dG, g, SRS_ADJ_K_ON_CSQN);
+          adj_buffer(k, ak, 4, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_CSQN);
           dG -= k.refill_v;
         }
         if (i < n_ch) {
@@ -273,20 +306,30 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           g[SRS_ADJ_B_TOT_SL] = -w * GB * (B - 1.0f) * ak.inv_btot_sl;
           g[SRS_ADJ_K_D_SL] = -w * GB * bsl * (c - k.khi) / (k.khi * kc2 * kc);
         }
-        // compensated update of lambda (owner-only state)
-        float4 L = make_float4(a.lam[roff + i].x, me.y, me.z, me.w);
-        float4 cm = a.lam_c4[roff + i];
-        float ci = a.lam_cim[roff + i];
-        float li = lim;
+        // compensated update of lambda
+        float4 L = make_float4(lc[i], me.y, me.z, me.w);
+        float4 cm = c4[i];
+        float ci = cim[i];
+        float lnew = li;
         kadd(L.x, cm.x, k.dt * oc);
         kadd(L.y, cm.y, k.dt * oa);
         kadd(L.z, cm.z, k.dt * om);
         kadd(L.w, cm.w, k.dt * oy);
-        kadd(li, ci, k.dt * oi);
-        a.lam[roff + i] = L;
-        a.lam_im[roff + i] = li;
-        a.lam_c4[roff + i] = cm;
-        a.lam_cim[roff + i] = ci;
+        kadd(lnew, ci, k.dt * oi);
+        if (t > 1) {
+          const float cprev = (jsr ? k.c0j : k.c0) + a.traj_u[xprev + i].x;
+          const float inj = tick_injection(a, n - 1, r, (int)(rank * P + i));
+          nxt[i] = make_float4(L.x / sl_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
+          lc[i] = L.x;
+          lim[i] = lnew;
+          c4[i] = cm;
+          cim[i] = ci;
+        } else {
+          a.lam[roff + i] = L;
+          a.lam_im[roff + i] = lnew;
+          a.lam_c4[roff + i] = cm;
+          a.lam_cim[roff + i] = ci;
+        }
 #pragma unroll
         for (int p = 0; p < NA; ++p) kadd(gs.s[p], gs.c[p], g[p]);
       }
@@ -313,7 +356,8 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 // Line-scan loss at one tick: F_i = pad_i + sum_q w_q dye(col_q) from the
 // trajectory slot, e_i = F_i / F0_i - 1 - target_i, L += e_i^2 / 2 and
 // coef_i = e_i / F0_i (= dL/dF_i).  One block per realization; samples in
-// order, so the loss sum is deterministic.
+// order, and the loss of each tick kept apart, so the host can sum the ticks
+// in time order whatever the segmentation.
 __global__ void k_adj_tick(AdjTickArgs a) {
   const int r = blockIdx.x;
   __shared__ double red[256];
@@ -340,7 +384,7 @@ __global__ void k_adj_tick(AdjTickArgs a) {
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) a.loss[r] += lacc;
+  if (threadIdx.x == 0) a.loss[r] = lacc;
 }
 
 template <int C>

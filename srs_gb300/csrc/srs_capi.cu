@@ -100,6 +100,8 @@ struct srs_sim {
   int32_t* d_wt_idx = nullptr;
   double* d_wt_w = nullptr;
   int adj_ls_version = -1;
+  // adjoint work buffers, kept between calls (name -> allocation)
+  std::vector<std::pair<void*, size_t>> adj_bufs;
 };
 
 namespace {
@@ -1126,6 +1128,7 @@ void srs_sim_destroy(srs_sim* s) {
   if (s->graph_plain) cudaGraphExecDestroy(s->graph_plain);
   if (s->st) cudaStreamSynchronize(s->st);
   for (void* p : s->allocs) cudaFree(p);
+  for (auto& b : s->adj_bufs) cudaFree(b.first);
   if (s->h_stage) cudaFreeHost(s->h_stage);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
@@ -1536,19 +1539,26 @@ int srs_adjoint_param_index(int k) { return (k >= 0 && k < SRS_N_ADJ) ? kAdjPara
 
 namespace {
 
-// Device scratch owned by one srs_adjoint call.
+// Device work buffers of srs_adjoint, numbered in request order and kept in
+// the simulation between calls (grown when a call needs more).
 struct Scratch {
-  std::vector<void*> p;
-  ~Scratch() {
-    for (void* q : p) cudaFree(q);
-  }
+  srs_sim* s;
+  size_t next = 0;
   template <class T>
   int get(T** out, size_t n) {
-    void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
-    if (e != cudaSuccess) return fail(SRS_ERR_NOMEM, std::string("adjoint scratch: ") + cudaGetErrorString(e));
-    p.push_back(q);
-    *out = (T*)q;
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    if (next == s->adj_bufs.size()) s->adj_bufs.push_back({nullptr, 0});
+    auto& b = s->adj_bufs[next++];
+    if (b.second < bytes) {
+      if (b.first) cudaFree(b.first);
+      b = {nullptr, 0};
+      void* q = nullptr;
+      cudaError_t e = cudaMalloc(&q, bytes);
+      if (e != cudaSuccess)
+        return fail(SRS_ERR_NOMEM, std::string("adjoint buffers: ") + cudaGetErrorString(e));
+      b = {q, bytes};
+    }
+    *out = (T*)b.first;
     return SRS_OK;
   }
 };
@@ -1670,15 +1680,17 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
                         (size_t)R * sizeof(RealCtl);
   const size_t traj_b = (size_t)(K + 1) * R * NE * 20 + (size_t)K * R * NE * 4 + (size_t)K * R * W * 4;
-  const size_t need = snap_b * (size_t)(nseg + 1) + traj_b + (size_t)R * NE * 40 +
+  const size_t need = snap_b * (size_t)(nseg + 1) + traj_b + (size_t)R * NE * 44 +
                       (size_t)(K / te + 2) * R * ns * 8 + (size_t)R * n_ticks * ns * 8;
-  size_t free_b = 0, total_b = 0;
+  size_t free_b = 0, total_b = 0, held = 0;
+  for (auto& b : s->adj_bufs) held += b.second;
   SRS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  free_b += held;
   if (need > free_b / 10 * 9)
     return fail(SRS_ERR_NOMEM, "adjoint needs " + std::to_string(need >> 20) + " MiB of device memory (" +
                                    std::to_string(free_b >> 20) + " MiB free): raise checkpoint_every "
                                    "or lower n_steps");
-  Scratch sc;
+  Scratch sc{s};
   std::vector<StateSnap> ck(nseg + 1);
   for (auto& c : ck) SRS_TRY(snap_alloc(s, sc, &c));
   float4* traj_u;
@@ -1694,23 +1706,50 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   SRS_TRY(sc.get(&lam_c4, (size_t)R * NE));
   SRS_TRY(sc.get(&lam_im, (size_t)R * NE));
   SRS_TRY(sc.get(&lam_cim, (size_t)R * NE));
+  float* lam_c;
+  SRS_TRY(sc.get(&lam_c, (size_t)R * NE));
   double *coef, *grad, *loss, *f0, *target = nullptr;
   SRS_TRY(sc.get(&coef, (size_t)(K / te + 2) * R * ns));
   SRS_TRY(sc.get(&grad, (size_t)R * SRS_N_ADJ));
-  SRS_TRY(sc.get(&loss, (size_t)R));
+  SRS_TRY(sc.get(&loss, (size_t)std::max<int64_t>(n_ticks, 1) * R));  // [tick][R]
   SRS_TRY(sc.get(&f0, (size_t)ns));
   SRS_CUDA(cudaMemcpyAsync(f0, d->f0, sizeof(double) * ns, cudaMemcpyHostToDevice, s->st));
-  if (d->target && n_ticks > 0) {
-    SRS_TRY(sc.get(&target, (size_t)R * n_ticks * ns));
+  {
+    double* tg;
+    SRS_TRY(sc.get(&tg, (size_t)R * std::max<int64_t>(n_ticks, 1) * ns));
+    if (d->target && n_ticks > 0) target = tg;
+  }
+  if (target) {
     SRS_CUDA(cudaMemcpyAsync(target, d->target, sizeof(double) * R * n_ticks * ns,
                              cudaMemcpyHostToDevice, s->st));
   }
   s->P.run_protocol = 0;
   refresh_args(s);
   // ---- forward with checkpoints ------------------------------------------------
+  // (the last segment records its trajectory on the way: it is the first
+  // one the reverse sweep needs)
+  auto traj_launch = [&](int len) -> int {
+    ResidentArgs ra = s->ar;
+    ra.steps = len;
+    ra.prestep_first = 0;
+    ra.initial_row = 0;
+    ra.traj_u = traj_u;
+    ra.traj_im = traj_im;
+    ra.traj_g = traj_g;
+    ra.traj_ch = traj_ch;
+    if (launch_resident(ra, s->C, s->n_clusters, s->threads, s->smem, s->st))
+      return fail(SRS_ERR_CUDA, std::string("trajectory launch: ") + cudaGetErrorString(cudaGetLastError()));
+    s->launches++;
+    return SRS_OK;
+  };
   for (int64_t k = 0; k < nseg; ++k) {
-    SRS_TRY(snap_copy(s, ck[k], true));
-    SRS_TRY(resident_launch(s, (int)std::min<int64_t>(K, n_steps - k * K)));
+    const int len = (int)std::min<int64_t>(K, n_steps - k * K);
+    if (k < nseg - 1) {
+      SRS_TRY(snap_copy(s, ck[k], true));
+      SRS_TRY(resident_launch(s, len));
+    } else {
+      SRS_TRY(traj_launch(len));
+    }
   }
   SRS_TRY(snap_copy(s, ck[nseg], true));
   {
@@ -1728,7 +1767,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   SRS_CUDA(cudaMemsetAsync(lam_im, 0, sizeof(float) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(lam_cim, 0, sizeof(float) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * R * SRS_N_ADJ, s->st));
-  SRS_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * R, s->st));
+  SRS_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * std::max<int64_t>(n_ticks, 1) * R, s->st));
   AdjArgs aa{};
   aa.R = R;
   aa.P = s->P_stride;
@@ -1759,6 +1798,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   aa.lam_im = lam_im;
   aa.lam_c4 = lam_c4;
   aa.lam_cim = lam_cim;
+  aa.lam_c = lam_c;
   aa.grad = grad;
   aa.k = s->ar.k;
   {
@@ -1771,9 +1811,16 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     aa.ak.v_cell = (float)s->p.reals[R_V_CELL];
   }
   const int n_ent = 2 * NR + NL;
-  const size_t adj_smem = adjoint_smem_bytes(s->P_stride, s->part_nch[0], n_ent);
   const int adj_threads = 512;
-  const int adj_ncl = std::min(adjoint_max_clusters(s->C, adj_threads, adj_smem), R);
+  // owner state of lambda on chip when it fits next to the published slots
+  size_t adj_smem = adjoint_smem_bytes(s->P_stride, s->part_nch[0], n_ent, true);
+  int adj_ncl = (d->flags & SRS_ADJ_LAMBDA_GLOBAL) ? 0 : adjoint_max_clusters(s->C, adj_threads, adj_smem);
+  aa.own_in_smem = adj_ncl > 0;
+  if (!aa.own_in_smem) {
+    adj_smem = adjoint_smem_bytes(s->P_stride, s->part_nch[0], n_ent, false);
+    adj_ncl = adjoint_max_clusters(s->C, adj_threads, adj_smem);
+  }
+  adj_ncl = std::min(adj_ncl, R);
   if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
   AdjTickArgs ta{};
   ta.n_samples = ns;
@@ -1786,24 +1833,16 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   ta.f0 = f0;
   ta.target = target;
   ta.rest_dye = s->ls.rest_dye;
-  ta.loss = loss;
   for (int64_t k = nseg - 1; k >= 0; --k) {
     const int64_t s0 = k * K;
     const int len = (int)std::min<int64_t>(K, n_steps - s0);
-    SRS_TRY(snap_copy(s, ck[k], false));
-    ResidentArgs ra = s->ar;
-    ra.steps = len;
-    ra.prestep_first = 0;
-    ra.initial_row = 0;
-    ra.traj_u = traj_u;
-    ra.traj_im = traj_im;
-    ra.traj_g = traj_g;
-    ra.traj_ch = traj_ch;
-    if (launch_resident(ra, s->C, s->n_clusters, s->threads, s->smem, s->st))
-      return fail(SRS_ERR_CUDA, std::string("trajectory launch: ") + cudaGetErrorString(cudaGetLastError()));
-    s->launches++;
+    if (k < nseg - 1) {
+      SRS_TRY(snap_copy(s, ck[k], false));
+      SRS_TRY(traj_launch(len));
+    }
     for (int64_t n = (s0 / te + 1) * te; n <= s0 + len; n += te) {
       ta.tick = (int32_t)(n / te - 1);
+      ta.loss = loss + (size_t)ta.tick * R;
       ta.traj_u = traj_u + (size_t)(n - s0) * R * NE;
       ta.coef = coef + (size_t)(n / te - s0 / te - 1) * R * ns;
       if (launch_adj_tick(ta, R, s->st)) return fail(SRS_ERR_CUDA, "tick launch failed");
@@ -1816,7 +1855,9 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     s->launches++;
   }
   SRS_TRY(snap_copy(s, ck[nseg], false));
-  SRS_CUDA(cudaMemcpyAsync(out->loss, loss, sizeof(double) * R, cudaMemcpyDeviceToHost, s->st));
+  std::vector<double> loss_t((size_t)std::max<int64_t>(n_ticks, 1) * R);
+  SRS_CUDA(cudaMemcpyAsync(loss_t.data(), loss, sizeof(double) * loss_t.size(), cudaMemcpyDeviceToHost,
+                           s->st));
   SRS_CUDA(cudaMemcpyAsync(out->grad, grad, sizeof(double) * R * SRS_N_ADJ, cudaMemcpyDeviceToHost, s->st));
   std::vector<float4> hl, hc;
   std::vector<float> hi, hci;
@@ -1832,6 +1873,11 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   }
   SRS_CUDA(cudaStreamSynchronize(s->st));
   SRS_CUDA(cudaGetLastError());
+  for (int r = 0; r < R; ++r) {  // ticks in time order: the same sum for any segmentation
+    double L = 0.0;
+    for (int64_t t = 0; t < n_ticks; ++t) L += loss_t[(size_t)t * R + r];
+    out->loss[r] = L;
+  }
   if (out->grad_state) {
     const int N = s->N;
     for (int r = 0; r < R; ++r) {

@@ -170,10 +170,12 @@ struct AdjArgs {
   const int32_t* wt_ptr;   // [C*P + 1] element -> line-scan samples
   const int32_t* wt_idx;
   const double* wt_w;
-  float4* lam;   // [R][C*P] (Ca, ATP, CMDN, dye)
+  float4* lam;   // [R][C*P] (Ca, ATP, CMDN, dye) at segment boundaries
   float* lam_im; // [R][C*P] immobile buffer
   float4* lam_c4;  // Kahan compensation
   float* lam_cim;
+  float* lam_c;    // [R][C*P] lambda_Ca within a segment (when not on chip)
+  int32_t own_in_smem;  // owner state of lambda in shared memory
   double* grad;  // [R][SRS_N_ADJ]
   Consts32 k;
   AdjConsts ak;
@@ -190,10 +192,10 @@ struct AdjTickArgs {
   const double* rest_dye;
   const float4* traj_u;  // trajectory slot [R][n_state]
   double* coef;          // [R][n_samples]
-  double* loss;          // [R]
+  double* loss;          // [R]: loss of this tick
 };
 
-size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries);
+size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem);
 int launch_adjoint(const AdjArgs& a, int C, int n_clusters, int threads, size_t smem,
                    cudaStream_t st);
 int adjoint_max_clusters(int C, int threads, size_t smem);

@@ -93,7 +93,7 @@ def test_adjoint_matches_fp64_finite_differences(srs, case):
 
     L0 = loss_of(p0)
     assert np.allclose(L0, case["loss"], rtol=1e-5)
-    checked = 0
+    checked = []
     for k, name in enumerate(srs.ADJ_PARAMS):
         idx = srs.R[name]
         h = 1e-4 * abs(p0.reals[idx])
@@ -106,8 +106,9 @@ def test_adjoint_matches_fp64_finite_differences(srs, case):
         fd = (Lp - Lm).sum() / (2 * h)
         adj = case["grad"][:, k].sum()
         assert abs(adj - fd) <= 1e-3 * abs(fd), (name, adj, fd)
-        checked += 1
-    assert checked >= 12
+        checked.append(name)
+    # the line scan over 600 steps resolves these at least
+    assert {"D_CA", "D_DYE", "K_ON_DYE", "K_OFF_DYE", "V_RYR"} <= set(checked), checked
 
 
 @pytest.mark.parametrize("K2,C", [(0, 1), (600, 2), (150, 3)])
@@ -126,6 +127,16 @@ def test_adjoint_segmentation_and_cluster_size_do_not_change_the_result(srs, cas
     assert np.array_equal(loss, case["loss"])
     assert np.array_equal(gs, case["gs"])
     assert np.allclose(grad, case["grad"], rtol=1e-6, atol=0)
+
+
+def test_adjoint_state_in_global_memory_gives_the_same_result(srs, case):
+    p = case["p"]
+    _, sim = _start(srs, p, srs.FP32, srs.ENGINE_RESIDENT)
+    loss, grad, gs = sim.adjoint(N_STEPS, TICK, case["f0"], case["target"], checkpoint_every=K,
+                                 grad_state=True, flags=srs.ADJ_LAMBDA_GLOBAL)
+    assert np.array_equal(loss, case["loss"])
+    assert np.array_equal(gs, case["gs"])
+    assert np.allclose(grad, case["grad"], rtol=1e-12, atol=0)
 
 
 def test_adjoint_leaves_the_state_after_n_steps(srs, case):

@@ -1,0 +1,36 @@
+"""torch.autograd binding of the adjoint (srs_gb300.autograd) against central
+finite differences of the FP64 engine with common random numbers."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_MESH, LINESCAN_DESC, params_from_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autograd_gradient_matches_finite_differences(srs):
+    torch = pytest.importorskip("torch")
+    from srs_gb300.autograd import AdjointProblem, LinescanLoss
+    p, _ = params_from_golden(srs, "spark")
+    p.ints[srs.I["FLAG_NO_FLUX_BOUNDARY"]] = 1
+    rng = np.random.default_rng(5)
+    prob = AdjointProblem(GOLDEN_MESH, p, [21, 22], LINESCAN_DESC, 400, 100,
+                          target=rng.standard_normal((2, 4, 20)) * 0.01, checkpoint_every=128)
+    theta = prob.theta0().requires_grad_()
+    loss = LinescanLoss.apply(theta, prob)
+    (g,) = torch.autograd.grad(loss, theta)
+    assert abs(loss.item() - prob.loss_fp64(theta.detach().numpy())) <= 1e-5 * loss.item()
+    th = theta.detach().numpy()
+    checked = 0
+    for k, name in enumerate(srs.ADJ_PARAMS):
+        h = 1e-4 * abs(th[k])
+        hi, lo = th.copy(), th.copy()
+        hi[k] += h
+        lo[k] -= h
+        Lp, Lm = prob.loss_fp64(hi), prob.loss_fp64(lo)
+        if abs(Lp - Lm) < 1e-9 * loss.item():
+            continue
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(g[k].item() - fd) <= 1e-3 * abs(fd), (name, g[k].item(), fd)
+        checked += 1
+    assert checked >= 10
