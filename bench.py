@@ -295,16 +295,21 @@ def adjoint_cost(srs, grid, p, args):
     sim.advance_async(n)
     sim.synchronize()
     fwd = time.perf_counter() - t0
-    sim.reset()
-    t0 = time.perf_counter()
-    loss, grad, _ = sim.adjoint(n, te, f0, checkpoint_every=256)
-    adj = time.perf_counter() - t0
-    if not np.isfinite(grad).all():
-        raise SystemExit("non-finite adjoint gradient")
-    return {"workload": "adjoint: config mesh x %d realizations, %d steps, line scan of %d samples "
-                        "every %d steps, checkpoints every 256" % (Ra, n, ns, te),
-            "cluster_size": sim.config()["cluster_size"], "forward_s": fwd, "adjoint_s": adj,
-            "cost_ratio": adj / fwd}
+    out = {"workload": "adjoint: config mesh x %d realizations, %d steps, line scan of %d samples "
+                       "every %d steps" % (Ra, n, ns, te),
+           "cluster_size": sim.config()["cluster_size"], "forward_s": fwd}
+    # K = 256: checkpoint + recompute; K = n: the forward pass keeps the trajectory
+    for K, key in ((256, "checkpoint_256"), (n, "whole_trajectory")):
+        sim.reset()
+        sim.adjoint(n, te, f0, checkpoint_every=K)  # warm: work buffers of this mode
+        sim.reset()
+        t0 = time.perf_counter()
+        loss, grad, _ = sim.adjoint(n, te, f0, checkpoint_every=K)
+        adj = time.perf_counter() - t0
+        if not np.isfinite(grad).all():
+            raise SystemExit("non-finite adjoint gradient")
+        out[key] = {"adjoint_s": adj, "cost_ratio": adj / fwd}
+    return out
 
 
 def run_ours(args):

@@ -195,6 +195,16 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples);
  * F of the equilibrium state (for dF/F0). */
 int srs_linescan(srs_sim* s, double* out, double* rest);
 
+/* ---- total Ca per compartment ---------------------------------------------
+ * No reference counterpart (the reference keeps no mass balance).  For every
+ * realization, out[2r] / out[2r+1] = sum over the cytosol / JSR elements of
+ * V0 * (free Ca + Ca bound to every buffer state + Ca bound to the rapid SL
+ * buffers at equilibrium), in uM um^3, accumulated in double precision from
+ * the current state (FP64 or FP32 engine).  Without sources (no SERCA, no
+ * refill, no LCC current, no-flux boundaries) the sum over both compartments
+ * is conserved by the explicit step. */
+int srs_sim_total_ca(srs_sim* s, double* out);
+
 /* ---- pathwise adjoint -------------------------------------------------------
  * No reference counterpart: the reference has no derivatives.  Gradient of a
  * line-scan dF/F0 loss with respect to the parameters of the deterministic
@@ -212,8 +222,11 @@ int srs_linescan(srs_sim* s, double* out, double* rest);
  * below, each the derivative with respect to that ParamStruct::Reals entry)
  * and optionally grad_state[r][6][N] = dL_r/d(initial state), reference
  * numbering and species order.  The state is checkpointed every
- * checkpoint_every steps (0: 256) and each segment is recomputed once for
- * the reverse sweep; the simulation is left at the state after n_steps.
+ * checkpoint_every steps and each segment but the last is recomputed once,
+ * recording its trajectory, for the reverse sweep; checkpoint_every = 0
+ * keeps the whole trajectory of the forward pass (no recomputation) when it
+ * takes at most half of the free device memory and checkpoints every 256
+ * steps otherwise.  The simulation is left at the state after n_steps.
  * FP32 resident engine only (SRS_ERR_UNSUPPORTED otherwise). */
 #define SRS_N_ADJ 18
 enum {

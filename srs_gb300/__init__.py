@@ -187,6 +187,7 @@ _SIGS = {
     "srs_explicit_step_fp64_noalloc": (C.c_int, [C.POINTER(NoallocStep)]),
     "srs_linescan_setup": (C.c_int, [_P, C.POINTER(LinescanDesc), C.POINTER(C.c_int)]),
     "srs_linescan": (C.c_int, [_P, _P, _P]),
+    "srs_sim_total_ca": (C.c_int, [_P, _P]),
     "srs_adjoint_param_index": (C.c_int, [C.c_int]),
     "srs_adjoint": (C.c_int, [_P, C.POINTER(_AdjDesc), C.POINTER(_AdjOut)]),
 }
@@ -415,6 +416,12 @@ class Simulation:
         rest = np.zeros(self._ls_n)
         _check(_lib.srs_linescan(self._h, _ptr(out), _ptr(rest)))
         return out, rest
+
+    def total_ca(self):
+        """[R][2] total Ca (uM um^3) of the cytosol and the JSR, FP64 sums."""
+        out = np.zeros((self.R, 2))
+        _check(_lib.srs_sim_total_ca(self._h, _ptr(out)))
+        return out
 
     def adjoint(self, n_steps, tick_every, f0, target=None, checkpoint_every=0, grad_state=False,
                 flags=0):

@@ -20,8 +20,9 @@
 // the forward engine recorded for the segment.  Lambda lives in HBM/L2 in
 // owner-only arrays with Kahan compensation, like the forward state.
 //
-// Parameter gradients: every thread keeps a compensated FP32 sum per
-// parameter over its elements and the steps of the segment; at the end of a
+// Parameter gradients: every thread sums its elements' terms of a step in
+// FP32 and adds that step sum to a compensated FP32 sum per parameter over
+// the steps of the segment; at the end of a
 // realization the sums are reduced in FP64 and added in FP64 to the
 // per-realization gradient, which therefore accumulates over segments (the
 // long reverse sweep) in double precision.
@@ -80,22 +81,28 @@ size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem) {
 
 namespace {
 
-// dL/dF injection of the tick at step n (0 when n is not a tick).
-__device__ __forceinline__ float tick_injection(const AdjArgs& a, int64_t n, int r, int e) {
-  if (a.tick_every <= 0 || n <= a.s0 || (n % a.tick_every) != 0) return 0.0f;
+// dL/dF coefficients of the tick at step n of realization r, or null when n
+// is not a tick of this segment (evaluated once per step, not per element).
+__device__ __forceinline__ const double* tick_coef(const AdjArgs& a, int64_t n, int r) {
+  if (a.tick_every <= 0 || n <= a.s0 || (n % a.tick_every) != 0) return nullptr;
   const int64_t slot = n / a.tick_every - a.s0 / a.tick_every - 1;
-  const double* coef = a.coef + ((size_t)slot * a.R + r) * a.n_samples;
+  return a.coef + ((size_t)slot * a.R + r) * a.n_samples;
+}
+
+__device__ __forceinline__ float tick_injection(const AdjArgs& a, const double* coef, int e) {
+  if (!coef) return 0.0f;
   double inj = 0.0;
   for (int q = a.wt_ptr[e]; q < a.wt_ptr[e + 1]; ++q) inj += coef[a.wt_idx[q]] * a.wt_w[q];
   return (float)inj;
 }
 
-// Rapid-buffer factor B(c) of UpdateFastBuffer (cpu/RunSimulation.cpp:15-22),
-// evaluated exactly as the forward engine evaluates it.
-__device__ __forceinline__ float sl_factor(const Consts32& k, float bsl, float c) {
+// 1 / B(c), B the rapid-buffer factor of UpdateFastBuffer
+// (cpu/RunSimulation.cpp:15-22).
+__device__ __forceinline__ float sl_inv_factor(const Consts32& k, float bsl, float c) {
   if (bsl == 0.0f) return 1.0f;
   const float kc = k.khi + c;
-  return fmaf(bsl, 1.0f / (kc * kc), 1.0f);
+  const float kc2 = kc * kc;
+  return kc2 / (kc2 + bsl);
 }
 
 }  // namespace
@@ -160,13 +167,14 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     // ---- publish lambda_{s1} (with the tick injection of step s1) ----------
     {
       const size_t xo = ((size_t)(len - 1) * a.R + r) * NE + (size_t)rank * P;
+      const double* coef = tick_coef(a, a.s0 + len, r);
       for (int i = tid; i < n_loc; i += nthr) {
         const float4 L = a.lam[roff + i];
         const float4 gb = __ldg(reinterpret_cast<const float4*>(geo + i) + 1);
         const uint32_t fl = __float_as_uint(gb.w);
         const float c = ((fl & 1u) ? k.c0j : k.c0) + a.traj_u[xo + i].x;
-        const float inj = tick_injection(a, a.s0 + len, r, (int)(rank * P + i));
-        pub0[i] = make_float4(L.x / sl_factor(k, gb.z, c), L.y, L.z, L.w + inj);
+        const float inj = tick_injection(a, coef, (int)(rank * P + i));
+        pub0[i] = make_float4(L.x * sl_inv_factor(k, gb.z, c), L.y, L.z, L.w + inj);
         lc[i] = L.x;
         if (a.own_in_smem) {
           lim[i] = a.lam_im[roff + i];
@@ -188,6 +196,10 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * P;
       const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * P;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
+      const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
+      float gstep[NA];  // this thread's contributions of this step
+#pragma unroll
+      for (int p = 0; p < NA; ++p) gstep[p] = 0.0f;
       for (int i = tid; i < n_loc; i += nthr) {
         const float4 x = a.traj_u[xoff + i];
         const float xim = a.traj_im[xoff + i];
@@ -260,10 +272,11 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
             Ki = Ki * Ki;
             const float den = fmaf(Ki * Ki, k.sd2, fmaf(Ki, k.sd1, k.sd0));
             const float num = fmaf(Ki * Ki, 3.24873e12f, fmaf(Ki, k.sn1, -k.sn0));
-            const float v = num / den;
+            const float iden = 1.0f / den;
+            const float v = num * iden;
             const float dnum = fmaf(2.0f * Ki, 3.24873e12f, k.sn1);
             const float dden = fmaf(2.0f * Ki, k.sd2, k.sd1);
-            const float dv = (dnum - v * dden) / den * (2.0f * c * k.inv_kdi * k.inv_kdi);
+            const float dv = (dnum - v * dden) * iden * (2.0f * c * k.inv_kdi * k.inv_kdi);
             dG = fmaf(-k.serca_scale, dv, dG);
             g[SRS_ADJ_A_P] = -w * ak.serca_per_ap * v;
           }
@@ -299,12 +312,13 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         if (bsl != 0.0f) {
           // F_Ca = G / B(c):  -G B'(c) / B^2 lambda_Ca = 2 bsl G w / (B kc^3)
           const float kc = k.khi + c;
-          const float kc2 = kc * kc;
-          const float B = fmaf(bsl, 1.0f / kc2, 1.0f);
-          const float GB = G / B;
-          oc = fmaf(2.0f * bsl * GB / (kc2 * kc), w, oc);
-          g[SRS_ADJ_B_TOT_SL] = -w * GB * (B - 1.0f) * ak.inv_btot_sl;
-          g[SRS_ADJ_K_D_SL] = -w * GB * bsl * (c - k.khi) / (k.khi * kc2 * kc);
+          const float ikc = 1.0f / kc;
+          const float bk2 = bsl * ikc * ikc;           // B - 1
+          const float GB = G / (1.0f + bk2);           // G / B
+          const float t3 = GB * bk2 * ikc;             // G bsl / (B kc^3)
+          oc = fmaf(2.0f * t3, w, oc);
+          g[SRS_ADJ_B_TOT_SL] = -w * GB * bk2 * ak.inv_btot_sl;
+          g[SRS_ADJ_K_D_SL] = -w * t3 * (c - k.khi) * ak.inv_khi;
         }
         // compensated update of lambda
         float4 L = make_float4(lc[i], me.y, me.z, me.w);
@@ -318,8 +332,8 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         kadd(lnew, ci, k.dt * oi);
         if (t > 1) {
           const float cprev = (jsr ? k.c0j : k.c0) + a.traj_u[xprev + i].x;
-          const float inj = tick_injection(a, n - 1, r, (int)(rank * P + i));
-          nxt[i] = make_float4(L.x / sl_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
+          const float inj = tick_injection(a, coef_next, (int)(rank * P + i));
+          nxt[i] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
           lc[i] = L.x;
           lim[i] = lnew;
           c4[i] = cm;
@@ -331,8 +345,10 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           a.lam_cim[roff + i] = ci;
         }
 #pragma unroll
-        for (int p = 0; p < NA; ++p) kadd(gs.s[p], gs.c[p], g[p]);
+        for (int p = 0; p < NA; ++p) gstep[p] += g[p];
       }
+#pragma unroll
+      for (int p = 0; p < NA; ++p) kadd(gs.s[p], gs.c[p], gstep[p]);
       cur ^= 1;
     }
     // ---- FP64 reduction of this realization's gradient ---------------------
@@ -354,37 +370,30 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 }
 
 // Line-scan loss at one tick: F_i = pad_i + sum_q w_q dye(col_q) from the
-// trajectory slot, e_i = F_i / F0_i - 1 - target_i, L += e_i^2 / 2 and
-// coef_i = e_i / F0_i (= dL/dF_i).  One block per realization; samples in
-// order, and the loss of each tick kept apart, so the host can sum the ticks
-// in time order whatever the segmentation.
+// trajectory slot, e_i = F_i / F0_i - 1 - target_i, coef_i = e_i / F0_i
+// (= dL/dF_i) and the loss term e_i^2 / 2, kept per sample so the host sums
+// them in a fixed order.  One block per (sample, realization).
 __global__ void k_adj_tick(AdjTickArgs a) {
-  const int r = blockIdx.x;
-  __shared__ double red[256];
-  double lacc = 0.0;
+  const int i = blockIdx.x, r = blockIdx.y;
   const float4* U = a.traj_u + (size_t)r * a.n_state;
-  for (int i = 0; i < a.n_samples; ++i) {
-    double acc = 0.0;
-    for (int q = a.ptr[i] + threadIdx.x; q < a.ptr[i + 1]; q += blockDim.x) {
-      const int e = a.col[q];
-      acc += a.w[q] * (a.rest_dye[e] + (double)U[e].w);
-    }
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      const double F = a.pad[i] + red[0];
-      const double tg = a.target ? a.target[((size_t)r * a.n_ticks + a.tick) * a.n_samples + i] : 0.0;
-      const double e = F / a.f0[i] - 1.0 - tg;
-      a.coef[(size_t)r * a.n_samples + i] = e / a.f0[i];
-      lacc += 0.5 * e * e;
-    }
-    __syncthreads();
+  double acc = 0.0;
+  for (int q = a.ptr[i] + threadIdx.x; q < a.ptr[i + 1]; q += blockDim.x) {
+    const int e = a.col[q];
+    acc += a.w[q] * (a.rest_dye[e] + (double)U[e].w);
   }
-  if (threadIdx.x == 0) a.loss[r] = lacc;
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double red[32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double F = a.pad[i];
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) F += red[q];
+    const double tg = a.target ? a.target[((size_t)r * a.n_ticks + a.tick) * a.n_samples + i] : 0.0;
+    const double e = F / a.f0[i] - 1.0 - tg;
+    a.coef[(size_t)r * a.n_samples + i] = e / a.f0[i];
+    a.loss[(size_t)r * a.n_samples + i] = 0.5 * e * e;
+  }
 }
 
 template <int C>
@@ -464,7 +473,7 @@ int adjoint_max_clusters(int C, int threads, size_t smem) {
 }
 
 int launch_adj_tick(const AdjTickArgs& a, int R, cudaStream_t st) {
-  k_adj_tick<<<R, 256, 0, st>>>(a);
+  k_adj_tick<<<dim3(a.n_samples, R), 128, 0, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

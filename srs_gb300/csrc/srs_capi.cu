@@ -100,6 +100,8 @@ struct srs_sim {
   int32_t* d_wt_idx = nullptr;
   double* d_wt_w = nullptr;
   int adj_ls_version = -1;
+  // total Ca (built on first use)
+  MassArgs mass{};
   // adjoint work buffers, kept between calls (name -> allocation)
   std::vector<std::pair<void*, size_t>> adj_bufs;
 };
@@ -1669,11 +1671,20 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   if (!s->ls.ptr) return fail(SRS_ERR_STATE, "call srs_linescan_setup first");
   if (d->n_steps < 1 || d->tick_every < 1 || d->checkpoint_every < 0)
     return fail(SRS_ERR_INPUT, "n_steps and tick_every must be positive");
-  const int K = d->checkpoint_every > 0 ? d->checkpoint_every : 256;
   const int R = s->R, NR = s->NR, NL = s->NL, W = NR + 2 * NL + 1, te = d->tick_every;
   const size_t NE = eng_count(s);
   const int ns = s->ls.n_samples;
   const int64_t n_steps = d->n_steps, n_ticks = n_steps / te;
+  int K = d->checkpoint_every;
+  if (K == 0) {
+    // automatic: keep the whole trajectory (no recomputation) when it takes
+    // at most half of the free device memory, else checkpoint every 256 steps
+    size_t free0 = 0, total0 = 0, held0 = 0;
+    for (auto& b : s->adj_bufs) held0 += b.second;
+    SRS_CUDA(cudaMemGetInfo(&free0, &total0));
+    const size_t whole = (size_t)(n_steps + 1) * R * (NE * 24 + (size_t)W * 4);
+    K = (n_steps <= INT32_MAX && whole <= (free0 + held0) / 2) ? (int)n_steps : 256;
+  }
   const int64_t nseg = (n_steps + K - 1) / K;
   SRS_TRY(adjoint_setup(s));
   // memory: checkpoints (nseg + 1), one segment of trajectory, lambda
@@ -1711,7 +1722,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   double *coef, *grad, *loss, *f0, *target = nullptr;
   SRS_TRY(sc.get(&coef, (size_t)(K / te + 2) * R * ns));
   SRS_TRY(sc.get(&grad, (size_t)R * SRS_N_ADJ));
-  SRS_TRY(sc.get(&loss, (size_t)std::max<int64_t>(n_ticks, 1) * R));  // [tick][R]
+  SRS_TRY(sc.get(&loss, (size_t)std::max<int64_t>(n_ticks, 1) * R * ns));  // [tick][R][sample]
   SRS_TRY(sc.get(&f0, (size_t)ns));
   SRS_CUDA(cudaMemcpyAsync(f0, d->f0, sizeof(double) * ns, cudaMemcpyHostToDevice, s->st));
   {
@@ -1767,7 +1778,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   SRS_CUDA(cudaMemsetAsync(lam_im, 0, sizeof(float) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(lam_cim, 0, sizeof(float) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * R * SRS_N_ADJ, s->st));
-  SRS_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * std::max<int64_t>(n_ticks, 1) * R, s->st));
+  SRS_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * std::max<int64_t>(n_ticks, 1) * R * ns, s->st));
   AdjArgs aa{};
   aa.R = R;
   aa.P = s->P_stride;
@@ -1809,6 +1820,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     aa.ak.inv_btot_sl = bt != 0.0 ? (float)(1.0 / bt) : 0.0f;
     aa.ak.serca_per_ap = 2e-3f;
     aa.ak.v_cell = (float)s->p.reals[R_V_CELL];
+    aa.ak.inv_khi = (float)(1.0 / s->p.reals[R_K_D_SL_HI]);
   }
   const int n_ent = 2 * NR + NL;
   const int adj_threads = 512;
@@ -1842,7 +1854,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     }
     for (int64_t n = (s0 / te + 1) * te; n <= s0 + len; n += te) {
       ta.tick = (int32_t)(n / te - 1);
-      ta.loss = loss + (size_t)ta.tick * R;
+      ta.loss = loss + (size_t)ta.tick * R * ns;
       ta.traj_u = traj_u + (size_t)(n - s0) * R * NE;
       ta.coef = coef + (size_t)(n / te - s0 / te - 1) * R * ns;
       if (launch_adj_tick(ta, R, s->st)) return fail(SRS_ERR_CUDA, "tick launch failed");
@@ -1855,7 +1867,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     s->launches++;
   }
   SRS_TRY(snap_copy(s, ck[nseg], false));
-  std::vector<double> loss_t((size_t)std::max<int64_t>(n_ticks, 1) * R);
+  std::vector<double> loss_t((size_t)std::max<int64_t>(n_ticks, 1) * R * ns);
   SRS_CUDA(cudaMemcpyAsync(loss_t.data(), loss, sizeof(double) * loss_t.size(), cudaMemcpyDeviceToHost,
                            s->st));
   SRS_CUDA(cudaMemcpyAsync(out->grad, grad, sizeof(double) * R * SRS_N_ADJ, cudaMemcpyDeviceToHost, s->st));
@@ -1875,7 +1887,8 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   SRS_CUDA(cudaGetLastError());
   for (int r = 0; r < R; ++r) {  // ticks in time order: the same sum for any segmentation
     double L = 0.0;
-    for (int64_t t = 0; t < n_ticks; ++t) L += loss_t[(size_t)t * R + r];
+    for (int64_t t = 0; t < n_ticks; ++t)
+      for (int i = 0; i < ns; ++i) L += loss_t[((size_t)t * R + r) * ns + i];
     out->loss[r] = L;
   }
   if (out->grad_state) {
@@ -1900,6 +1913,58 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     for (int p = 0; p < SRS_N_ADJ; ++p)
       if (!std::isfinite(out->grad[(size_t)r * SRS_N_ADJ + p]))
         return fail(SRS_ERR_NONFINITE, "non-finite adjoint gradient");
+  return SRS_OK;
+}
+
+int srs_sim_total_ca(srs_sim* s, double* out) {
+  if (!s || !out) return fail(SRS_ERR_INPUT, "null argument");
+  MassArgs& a = s->mass;
+  const size_t NE = eng_count(s);
+  if (!a.v0) {
+    const double* Rr = s->p.reals;
+    std::vector<double> v0(NE, 0.0), bhi(NE, 0.0), blo(NE, 0.0), rest4(4 * NE, 0.0), rimm(NE, 0.0);
+    std::vector<uint8_t> jsr(NE, 0);
+    for (size_t e = 0; e < NE; ++e) {
+      const int j = s->ref_of_eng[e];
+      if (j < 0) continue;
+      v0[e] = s->m.V0[j];
+      jsr[e] = s->m.domain[j] == DOMAIN_JSR;
+      bhi[e] = s->m.TT[j] * Rr[R_B_TOT_SL_HI] / (s->m.V0[j] * (1e-15));
+      blo[e] = s->m.TT[j] * Rr[R_B_TOT_SL_LO] / (s->m.V0[j] * (1e-15));
+      if (s->d.precision != SRS_FP64) {
+        const double f = jsr[e] ? 0.0 : 1.0;
+        rest4[4 * e] = s->rest_ca[e];
+        rest4[4 * e + 1] = f * s->rv.atp;
+        rest4[4 * e + 2] = f * s->rv.cmdn;
+        rest4[4 * e + 3] = f * s->rv.dye;
+        rimm[e] = s->rest_imm[e];
+      }
+    }
+    a.n_state = (int32_t)NE;
+    a.khi = Rr[R_K_D_SL_HI];
+    a.klo = Rr[R_K_D_SL_LO];
+    SRS_TRY(dev_upload(s, (double**)&a.v0, v0.data(), v0.size()));
+    SRS_TRY(dev_upload(s, (uint8_t**)&a.jsr, jsr.data(), jsr.size()));
+    SRS_TRY(dev_upload(s, (double**)&a.bhi, bhi.data(), bhi.size()));
+    SRS_TRY(dev_upload(s, (double**)&a.blo, blo.data(), blo.size()));
+    SRS_TRY(dev_upload(s, (double**)&a.rest4, rest4.data(), rest4.size()));
+    SRS_TRY(dev_upload(s, (double**)&a.rest_imm, rimm.data(), rimm.size()));
+    SRS_TRY(dev_alloc(s, &a.out, (size_t)2 * s->R));
+  }
+  MassArgs m = a;
+  if (s->d.precision == SRS_FP64) {
+    m.S64 = s->d_S[0];
+  } else {
+    m.M = s->d_M[0];
+    m.CM = s->d_CM;
+    m.I = s->d_I[0];
+    m.CI = s->d_CI;
+  }
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  if (launch_total_ca(m, s->R, s->st)) return fail(SRS_ERR_CUDA, "total-Ca launch failed");
+  s->launches++;
+  SRS_CUDA(cudaMemcpyAsync(out, m.out, sizeof(double) * 2 * s->R, cudaMemcpyDeviceToHost, s->st));
+  SRS_CUDA(cudaStreamSynchronize(s->st));
   return SRS_OK;
 }
 

@@ -136,6 +136,25 @@ struct LinescanArgs {
 };
 int launch_linescan(const LinescanArgs& a, int R, cudaStream_t st);
 
+// ---- total Ca per compartment (k_mass.cu) ------------------------------------
+struct MassArgs {
+  int32_t n_state;        // elements per realization in the engine layout
+  const double* v0;       // [n_state] volume (0 for padding slots)
+  const uint8_t* jsr;     // [n_state] 1 for JSR elements
+  const double* bhi;      // [n_state] rapid SL buffer capacities (uM)
+  const double* blo;
+  double khi, klo;
+  const double* S64;      // FP64 engine state [R][6][n_state], or null
+  const float4* M;        // FP32 engines: deviations and compensation
+  const float4* CM;
+  const float* I;
+  const float* CI;
+  const double* rest4;    // [n_state][4] rest of Ca, ATP, CMDN, dye
+  const double* rest_imm; // [n_state]
+  double* out;            // [R][2]: cytosol, JSR
+};
+int launch_total_ca(const MassArgs& a, int R, cudaStream_t st);
+
 // ---- pathwise adjoint (k_adjoint.cu) ---------------------------------------
 // FP32 constants of the Jacobian beyond Consts32.
 struct AdjConsts {
@@ -143,6 +162,7 @@ struct AdjConsts {
   float inv_btot_sl;   // 1 / B_TOT_SL_HI (0 when B_TOT_SL_HI = 0)
   float serca_per_ap;  // dF_Ca/dA_P = -serca_per_ap * v_cycle / B
   float v_cell;        // V_CELL
+  float inv_khi;       // 1 / K_D_SL_HI
 };
 
 struct AdjArgs {
@@ -192,7 +212,7 @@ struct AdjTickArgs {
   const double* rest_dye;
   const float4* traj_u;  // trajectory slot [R][n_state]
   double* coef;          // [R][n_samples]
-  double* loss;          // [R]: loss of this tick
+  double* loss;          // [R][n_samples]: loss terms of this tick
 };
 
 size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem);
