@@ -20,12 +20,12 @@
 // the forward engine recorded for the segment.  Lambda lives in HBM/L2 in
 // owner-only arrays with Kahan compensation, like the forward state.
 //
-// Parameter gradients: every thread sums its elements' terms of a step in
-// FP32 and adds that step sum to a compensated FP32 sum per parameter over
-// the steps of the segment; at the end of a
-// realization the sums are reduced in FP64 and added in FP64 to the
-// per-realization gradient, which therefore accumulates over segments (the
-// long reverse sweep) in double precision.
+// Parameter gradients: each step, every warp sums its elements' terms in FP32
+// (a warp-shuffle reduction) and adds that step sum to a per-warp FP64
+// accumulator in shared memory; at the end of a realization the warps' sums
+// are added in FP64 to the per-realization gradient, which therefore
+// accumulates over all steps and segments (the long reverse sweep) in double
+// precision.
 #include "srs_cluster.cuh"
 #include "srs_engine.h"
 
@@ -34,11 +34,6 @@ namespace srs {
 namespace {
 
 constexpr int NA = SRS_N_ADJ;
-
-struct KSum {
-  float s[NA];
-  float c[NA];
-};
 
 __device__ __forceinline__ void kadd(float& s, float& c, float v) {
   float y = v - c;
@@ -183,9 +178,9 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         }
       }
     }
-    KSum gs;
-#pragma unroll
-    for (int p = 0; p < NA; ++p) gs.s[p] = gs.c[p] = 0.0f;
+    const int warp = tid >> 5, lane = tid & 31, nw = nthr >> 5;
+    // per-warp FP64 accumulators of this realization's gradient
+    for (int q = tid; q < nw * NA; q += nthr) red[q] = 0.0;
     int cur = 0;
     for (int t = len; t >= 1; --t) {
       step_barrier<C>();
@@ -194,6 +189,9 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       float4* nxt = cur ? pub0 : pub1;
       const uint32_t* bs = s_base + 16 * cur;
       const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * P;
+      const float4* __restrict__ tu = a.traj_u + xoff;
+      const float* __restrict__ tim = a.traj_im + xoff;
+      const float* __restrict__ tg = a.traj_g + xoff;
       const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * P;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
@@ -201,9 +199,9 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 #pragma unroll
       for (int p = 0; p < NA; ++p) gstep[p] = 0.0f;
       for (int i = tid; i < n_loc; i += nthr) {
-        const float4 x = a.traj_u[xoff + i];
-        const float xim = a.traj_im[xoff + i];
-        const float G = a.traj_g[xoff + i];
+        const float4 x = __ldg(tu + i);
+        const float xim = __ldg(tim + i);
+        const float G = __ldg(tg + i);
         const float4* gp = reinterpret_cast<const float4*>(geo + i);
         const float4 ga = __ldg(gp);
         const float4 gb = __ldg(gp + 1);
@@ -220,10 +218,17 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           n2 = ld_smem_f4(bs[0] + c2 * 16u);
           n3 = ld_smem_f4(bs[0] + c3 * 16u);
         } else {
-          n0 = ld_dsmem_f4(bs[c0 >> a.off_bits] + (c0 & mask) * 16u);
-          n1 = ld_dsmem_f4(bs[c1 >> a.off_bits] + (c1 & mask) * 16u);
-          n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & mask) * 16u);
-          n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & mask) * 16u);
+          // neighbours in this CTA's own partition come from local shared memory
+          const uint32_t pub_addr = smem_addr(pub);
+          auto nb = [&](uint32_t code) -> float4 {
+            const uint32_t q = code >> a.off_bits;
+            if (q == rank) return ld_smem_f4(pub_addr + (code & mask) * 16u);
+            return ld_dsmem_f4(bs[q] + (code & mask) * 16u);
+          };
+          n0 = nb(c0);
+          n1 = nb(c1);
+          n2 = nb(c2);
+          n3 = nb(c3);
         }
         const float sa = (ga.x + ga.y) + (ga.z + ga.w);
         // transposed diffusion: S = sum_k aT_k lambda(nb_k) - (sum_k a_k) lambda(self)
@@ -347,18 +352,17 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 #pragma unroll
         for (int p = 0; p < NA; ++p) gstep[p] += g[p];
       }
+      // step sums of the warp (FP32 over its ~hundred terms) into its FP64
+      // accumulators: the sum over the steps runs in double precision
 #pragma unroll
-      for (int p = 0; p < NA; ++p) kadd(gs.s[p], gs.c[p], gstep[p]);
+      for (int p = 0; p < NA; ++p) {
+        float v = gstep[p];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp * NA + p] += (double)v;
+      }
       cur ^= 1;
     }
     // ---- FP64 reduction of this realization's gradient ---------------------
-    const int warp = tid >> 5, lane = tid & 31, nw = nthr >> 5;
-#pragma unroll
-    for (int p = 0; p < NA; ++p) {
-      double v = (double)gs.s[p] - (double)gs.c[p];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp * NA + p] = v;
-    }
     __syncthreads();
     if (tid < NA) {
       double v = 0.0;

@@ -470,10 +470,21 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         {
           const RealCtl& ctl = tail->ctl;
           const int v = ctl.vsel;
+          const uint32_t src_addr = smem_addr(src);
+          // geometry of the next element is loaded one iteration ahead
+          float4 ga_n = make_float4(0, 0, 0, 0), gb_n = ga_n;
+          if (e_begin < e_end) {
+            const float4* gp = reinterpret_cast<const float4*>(geo + e_begin);
+            ga_n = __ldg(gp);
+            gb_n = __ldg(gp + 1);
+          }
           for (int i = e_begin; i < e_end; i += e_stride) {
-            const float4* gp = reinterpret_cast<const float4*>(geo + i);
-            float4 ga = __ldg(gp);
-            float4 gb = __ldg(gp + 1);
+            const float4 ga = ga_n, gb = gb_n;
+            if (i + e_stride < e_end) {
+              const float4* gp = reinterpret_cast<const float4*>(geo + i + e_stride);
+              ga_n = __ldg(gp);
+              gb_n = __ldg(gp + 1);
+            }
             uint32_t w0 = __float_as_uint(gb.x), w1 = __float_as_uint(gb.y);
             uint32_t c0 = w0 & 0xffffu, c1 = w0 >> 16, c2 = w1 & 0xffffu, c3 = w1 >> 16;
             const uint32_t fl = __float_as_uint(gb.w);
@@ -502,10 +513,16 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
               n2 = ld_smem_f4(bs[0] + c2 * 16u);
               n3 = ld_smem_f4(bs[0] + c3 * 16u);
             } else {
-              n0 = ld_dsmem_f4(bs[c0 >> a.off_bits] + (c0 & off_mask) * 16u);
-              n1 = ld_dsmem_f4(bs[c1 >> a.off_bits] + (c1 & off_mask) * 16u);
-              n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & off_mask) * 16u);
-              n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & off_mask) * 16u);
+              // neighbours in this CTA's own partition come from local shared memory
+              auto nb = [&](uint32_t code) -> float4 {
+                const uint32_t q = code >> a.off_bits;
+                if (q == rank) return ld_smem_f4(src_addr + (code & off_mask) * 16u);
+                return ld_dsmem_f4(bs[q] + (code & off_mask) * 16u);
+              };
+              n0 = nb(c0);
+              n1 = nb(c1);
+              n2 = nb(c2);
+              n3 = nb(c3);
             }
             float4 out, cm = cmb[i];
             float imo, ci = cib[i];
