@@ -182,8 +182,12 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     // per-warp FP64 accumulators of this realization's gradient
     for (int q = tid; q < nw * NA; q += nthr) red[q] = 0.0;
     int cur = 0;
+    // barrier phases: the arrive after the publication of step t's slots is
+    // waited on after the interior elements of step t, whose neighbours'
+    // slots all live in this CTA (the __syncthreads orders those)
+    __syncthreads();
+    cl_arrive<C>();
     for (int t = len; t >= 1; --t) {
-      step_barrier<C>();
       const int64_t n = a.s0 + t;  // this step maps x_{n-1} to x_n
       const float4* pub = cur ? pub1 : pub0;
       float4* nxt = cur ? pub0 : pub1;
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       float gstep[NA];  // this thread's contributions of this step
 #pragma unroll
       for (int p = 0; p < NA; ++p) gstep[p] = 0.0f;
-      for (int i = tid; i < n_loc; i += nthr) {
+      auto element = [&](int i) {
         const float4 x = __ldg(tu + i);
         const float xim = __ldg(tim + i);
         const float G = __ldg(tg + i);
@@ -218,17 +222,10 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           n2 = ld_smem_f4(bs[0] + c2 * 16u);
           n3 = ld_smem_f4(bs[0] + c3 * 16u);
         } else {
-          // neighbours in this CTA's own partition come from local shared memory
-          const uint32_t pub_addr = smem_addr(pub);
-          auto nb = [&](uint32_t code) -> float4 {
-            const uint32_t q = code >> a.off_bits;
-            if (q == rank) return ld_smem_f4(pub_addr + (code & mask) * 16u);
-            return ld_dsmem_f4(bs[q] + (code & mask) * 16u);
-          };
-          n0 = nb(c0);
-          n1 = nb(c1);
-          n2 = nb(c2);
-          n3 = nb(c3);
+          n0 = ld_dsmem_f4(bs[c0 >> a.off_bits] + (c0 & mask) * 16u);
+          n1 = ld_dsmem_f4(bs[c1 >> a.off_bits] + (c1 & mask) * 16u);
+          n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & mask) * 16u);
+          n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & mask) * 16u);
         }
         const float sa = (ga.x + ga.y) + (ga.z + ga.w);
         // transposed diffusion: S = sum_k aT_k lambda(nb_k) - (sum_k a_k) lambda(self)
@@ -351,7 +348,16 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         }
 #pragma unroll
         for (int p = 0; p < NA; ++p) gstep[p] += g[p];
-      }
+      };
+      // interior elements (and the channel elements when they are interior)
+      const int i0 = n_ch + a.n_int[rank];
+      for (int i = (a.ch_interior ? 0 : n_ch) + tid; i < i0; i += nthr) element(i);
+      cl_wait<C>();
+      if (!a.ch_interior)
+        for (int i = tid; i < n_ch; i += nthr) element(i);
+      for (int i = i0 + tid; i < n_loc; i += nthr) element(i);
+      __syncthreads();
+      cl_arrive<C>();
       // step sums of the warp (FP32 over its ~hundred terms) into its FP64
       // accumulators: the sum over the steps runs in double precision
 #pragma unroll
@@ -362,6 +368,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       }
       cur ^= 1;
     }
+    cl_wait<C>();
     // ---- FP64 reduction of this realization's gradient ---------------------
     __syncthreads();
     if (tid < NA) {

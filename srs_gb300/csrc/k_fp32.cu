@@ -242,11 +242,11 @@ struct ResidentSmemTail {
   RealCtl ctl;
   uint32_t base[2][16];  // cluster addresses of buf[b] in CTA rank q
   int32_t bad;
-  // Termination flag published by rank 0's warp 0 in iteration s into slot
-  // s & 1 and read by every thread of the cluster after that iteration's
-  // barrier.  Two slots, so a thread still reading slot s & 1 never sees the
-  // write for s + 1.
-  int32_t done_flag[2];
+  // Termination flag published by rank 0's warp 0 in step s into slot s & 3
+  // and read by every thread of the cluster after the barrier that ends step
+  // s.  With speculation rank 0 can run one barrier phase ahead of a slow CTA,
+  // so four slots keep a flag from being rewritten while it is read.
+  int32_t done_flag[4];
 };
 
 template <int C>
@@ -393,9 +393,7 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
   // it gates right after updating them) and the other warps share the rest;
   // elsewhere every thread strides over the whole partition.
   const bool split = (rank == 0) && (n_ch > 0) && (nthr > 32);
-  const int e_begin = split ? (warp == 0 ? lane : n_ch + tid - 32) : tid;
-  const int e_end = split ? (warp == 0 ? n_ch : n_loc) : n_loc;
-  const int e_stride = split ? (warp == 0 ? 32 : nthr - 32) : nthr;
+  const int n_int = a.n_int[rank];  // interior elements follow the channel elements
   const TetRec* geo = a.geo + (size_t)rank * P;
   const uint32_t off_mask = (1u << a.off_bits) - 1u;
   const Consts32& k = a.k;
@@ -442,12 +440,19 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
       // protocol work that precedes the first step of a run
       if (a.prestep_first && !tail->ctl.done)
         resident_prestep(a, tail->ctl, buf0, s_ryr, s_lcc, s_lccv, r, a.initial_row, lane);
-      if (lane == 0) tail->done_flag[1] = tail->ctl.done;
+      if (lane == 0) tail->done_flag[3] = tail->ctl.done;
     }
     step_barrier<C>();
-    const bool skip = ((C > 1) ? ld_dsmem_s32(done_addr0 + 4u) : tail->done_flag[1]) != 0;
+    const bool skip = ((C > 1) ? ld_dsmem_s32(done_addr0 + 12u) : tail->done_flag[3]) != 0;
     int cur = 0;
     if (!skip) {
+      // Barrier phases: the arrive that ends step s is waited on at the top of
+      // step s + 1 -- after the step's interior elements when speculating
+      // (their neighbours are all in this CTA, so only this CTA's writes of
+      // step s are needed, which the __syncthreads below orders), before
+      // them otherwise.
+      cl_arrive<C>();
+      bool pending = true;
       for (int s = 0; s < a.steps; ++s) {
         const float4* src = cur ? buf1 : buf0;
         float4* dst = cur ? buf0 : buf1;
@@ -464,24 +469,22 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             if (lane == 0) rec[W - 1] = tail->ctl.vsel;
           }
         }
-        // ---- every element of this partition; the elements that carry
+        const int v = tail->ctl.vsel;
+        // one range of elements of this partition; elements that carry
         // channels (head of partition 0) add the release flux of their
-        // channels, computed from the state of this step ----------------
-        {
-          const RealCtl& ctl = tail->ctl;
-          const int v = ctl.vsel;
-          const uint32_t src_addr = smem_addr(src);
+        // channels, computed from the state of this step
+        auto update = [&](int lo, int hi, int stride) {
           // geometry of the next element is loaded one iteration ahead
           float4 ga_n = make_float4(0, 0, 0, 0), gb_n = ga_n;
-          if (e_begin < e_end) {
-            const float4* gp = reinterpret_cast<const float4*>(geo + e_begin);
+          if (lo < hi) {
+            const float4* gp = reinterpret_cast<const float4*>(geo + lo);
             ga_n = __ldg(gp);
             gb_n = __ldg(gp + 1);
           }
-          for (int i = e_begin; i < e_end; i += e_stride) {
+          for (int i = lo; i < hi; i += stride) {
             const float4 ga = ga_n, gb = gb_n;
-            if (i + e_stride < e_end) {
-              const float4* gp = reinterpret_cast<const float4*>(geo + i + e_stride);
+            if (i + stride < hi) {
+              const float4* gp = reinterpret_cast<const float4*>(geo + i + stride);
               ga_n = __ldg(gp);
               gb_n = __ldg(gp + 1);
             }
@@ -513,16 +516,10 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
               n2 = ld_smem_f4(bs[0] + c2 * 16u);
               n3 = ld_smem_f4(bs[0] + c3 * 16u);
             } else {
-              // neighbours in this CTA's own partition come from local shared memory
-              auto nb = [&](uint32_t code) -> float4 {
-                const uint32_t q = code >> a.off_bits;
-                if (q == rank) return ld_smem_f4(src_addr + (code & off_mask) * 16u);
-                return ld_dsmem_f4(bs[q] + (code & off_mask) * 16u);
-              };
-              n0 = nb(c0);
-              n1 = nb(c1);
-              n2 = nb(c2);
-              n3 = nb(c3);
+              n0 = ld_dsmem_f4(bs[c0 >> a.off_bits] + (c0 & off_mask) * 16u);
+              n1 = ld_dsmem_f4(bs[c1 >> a.off_bits] + (c1 & off_mask) * 16u);
+              n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & off_mask) * 16u);
+              n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & off_mask) * 16u);
             }
             float4 out, cm = cmb[i];
             float imo, ci = cib[i];
@@ -544,12 +541,20 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             cib[i] = ci;
             bad |= !isfinite(out.x);
           }
-        }
-        if (rank == 0) {
-          if (!split) __syncthreads();  // every channel element of this step is written
+        };
+        // channel elements, then gating of this step and the protocol of the
+        // next, by warp 0 of partition 0 (split) or after the whole CTA
+        auto channels = [&]() {
+          if (split) {
+            if (chan_warp) {
+              update(lane, n_ch, 32);
+              __syncwarp();  // warp 0 wrote the channel elements itself
+            }
+          } else {
+            update(tid, n_ch, nthr);
+            __syncthreads();
+          }
           if (chan_warp) {
-            __syncwarp();  // warp 0 wrote the channel elements itself
-            // ---- gating of this step and protocol of the next ----------------
             RealCtl& ctl = tail->ctl;
             if (!P_.nogating) resident_gate(a, ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
             if (lane == 0) {
@@ -558,15 +563,42 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             }
             __syncwarp();
             resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane);
-            if (lane == 0) tail->done_flag[s & 1] = ctl.done;
+            if (lane == 0) tail->done_flag[s & 3] = ctl.done;
+          }
+        };
+        // termination decided at the end of step s - 1
+        auto finished = [&]() -> bool {
+          if (s == 0) return false;
+          const uint32_t slot = (uint32_t)((s - 1) & 3);
+          return ((C > 1) ? ld_dsmem_s32(done_addr0 + 4u * slot) : tail->done_flag[slot]) != 0;
+        };
+        const bool worker = !(split && chan_warp);  // not the channel warp
+        const int wt = split ? tid - 32 : tid, wn = split ? nthr - 32 : nthr;
+        if (!a.speculate) {
+          cl_wait<C>();
+          pending = false;
+          if (finished()) break;
+        }
+        // interior elements: neighbours all in this partition
+        if (worker) update(n_ch + wt, n_ch + n_int, wn);
+        if (a.ch_interior && rank == 0 && n_ch > 0) channels();
+        if (a.speculate) {
+          cl_wait<C>();
+          pending = false;
+          if (finished()) {  // cannot happen when the host allows speculation
+            bad |= 2;
+            break;
           }
         }
-        step_barrier<C>();
+        // boundary elements: some neighbour in another partition
+        if (worker) update(n_ch + n_int + wt, n_loc, wn);
+        if (!a.ch_interior && rank == 0 && n_ch > 0) channels();
+        __syncthreads();
+        cl_arrive<C>();
+        pending = true;
         cur ^= 1;
-        const int done =
-            (C > 1) ? ld_dsmem_s32(done_addr0 + 4u * (uint32_t)(s & 1)) : tail->done_flag[s & 1];
-        if (done) break;
       }
+      if (pending) cl_wait<C>();
     }
     step_barrier<C>();
     // ---- store the realization ----------------------------------------------
@@ -595,9 +627,10 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
     }
     step_barrier<C>();  // shared memory is reused by the next realization
   }
-  if (bad) atomicOr(&tail->bad, 1);
+  if (bad) atomicOr(&tail->bad, bad);
   __syncthreads();
-  if (tid == 0 && tail->bad) atomicOr(&a.CS.ctl[0].status, 1u);
+  // status bit 0: non-finite Ca; bit 3: termination inside a speculating launch
+  if (tid == 0 && tail->bad) atomicOr(&a.CS.ctl[0].status, ((tail->bad & 1) ? 1u : 0u) | ((tail->bad & 2) ? 8u : 0u));
   step_barrier<C>();  // no CTA leaves while others may read its shared memory
 }
 

@@ -79,7 +79,8 @@ struct srs_sim {
   float* d_CI = nullptr;
   int C = 1, threads = 0, n_clusters = 0, P_stride = 0, off_bits = 0;
   size_t smem = 0;
-  std::vector<int> part_start, part_len, part_nch;  // resident partitions
+  std::vector<int> part_start, part_len, part_nch, part_nint;  // resident partitions
+  int ch_interior = 0;
   int64_t launches = 0;
   cudaGraphExec_t graph_plain = nullptr;
   int graph_plain_len = 0;
@@ -457,24 +458,54 @@ int setup_plain32(srs_sim* s) {
 
 // ---- FP32 resident engine ----------------------------------------------------
 int resident_partition(srs_sim* s, int C) {
-  // Elements carrying channels first (they form the head of partition 0 and
-  // are updated by its warp 0), then the RCM order of all other elements;
-  // the sequence is cut into C contiguous partitions of equal size.
+  // Order: the elements that carry channels, then breadth-first layers
+  // outward from them over the diffusion faces (so partition 0 holds the
+  // channels' neighbourhood and partitions are cut between layers); the
+  // sequence is cut into C contiguous partitions of equal size.  Inside each
+  // partition: channel elements (partition 0 only), then interior elements
+  // (every neighbour in the same partition), then boundary elements.
   const int N = s->N;
-  std::vector<int> base = rcm_order_by_domain(s->m, s->op);
+  const Mesh& m = s->m;
+  const Operator& op = s->op;
+  std::vector<int> base = rcm_order_by_domain(m, op);
   std::vector<char> has_ch(N, 0);
-  for (int i = 0; i < s->m.NR; ++i) has_ch[s->m.ryr_ele[i]] = has_ch[s->m.ryr_jsr[i]] = 1;
-  for (int i = 0; i < s->m.NL; ++i) has_ch[s->m.lcc_ele[i]] = 1;
+  for (int i = 0; i < m.NR; ++i) has_ch[m.ryr_ele[i]] = has_ch[m.ryr_jsr[i]] = 1;
+  for (int i = 0; i < m.NL; ++i) has_ch[m.lcc_ele[i]] = 1;
+  auto nbr = [&](int j, int k) -> int {
+    const int u = op.nij[4 * (size_t)j + k];
+    return (u != j && op.aij[5 * (size_t)j + 1 + k] != 0) ? u : -1;
+  };
   std::vector<int> seq;
   seq.reserve(N);
+  std::vector<char> seen(N, 0);
+  auto grow = [&](size_t h) {
+    for (; h < seq.size(); ++h)
+      for (int k = 0; k < 4; ++k) {
+        const int u = nbr(seq[h], k);
+        if (u >= 0 && !seen[u]) {
+          seen[u] = 1;
+          seq.push_back(u);
+        }
+      }
+  };
   for (int j : base)
-    if (has_ch[j]) seq.push_back(j);
+    if (has_ch[j]) {
+      seen[j] = 1;
+      seq.push_back(j);
+    }
   const int n_ch = (int)seq.size();
+  grow(0);
   for (int j : base)
-    if (!has_ch[j]) seq.push_back(j);
+    if (!seen[j]) {
+      seen[j] = 1;
+      const size_t h = seq.size();
+      seq.push_back(j);
+      grow(h);
+    }
   s->part_start.assign(C, 0);
   s->part_len.assign(C, 0);
   s->part_nch.assign(C, 0);
+  s->part_nint.assign(C, 0);
   int Pmax = 0;
   for (int q = 0; q < C; ++q) {
     int b0 = (int)((int64_t)N * q / C), e0 = (int)((int64_t)N * (q + 1) / C);
@@ -485,6 +516,30 @@ int resident_partition(srs_sim* s, int C) {
   if (n_ch > s->part_len[0])
     return fail(SRS_ERR_UNSUPPORTED, "channel elements do not fit in one partition");
   s->part_nch[0] = n_ch;
+  std::vector<int> part_of(N);
+  for (int q = 0; q < C; ++q)
+    for (int i = 0; i < s->part_len[q]; ++i) part_of[seq[s->part_start[q] + i]] = q;
+  auto interior = [&](int j) {
+    for (int k = 0; k < 4; ++k) {
+      const int u = nbr(j, k);
+      if (u >= 0 && part_of[u] != part_of[j]) return false;
+    }
+    return true;
+  };
+  s->ch_interior = 1;
+  for (int i = 0; i < n_ch; ++i) s->ch_interior &= interior(seq[i]) ? 1 : 0;
+  std::vector<int> order;
+  order.reserve(N);
+  for (int q = 0; q < C; ++q) {
+    const int b0 = s->part_start[q], e0 = b0 + s->part_len[q];
+    const int c0 = q == 0 ? n_ch : 0;
+    for (int i = b0; i < b0 + c0; ++i) order.push_back(seq[i]);
+    for (int i = b0 + c0; i < e0; ++i)
+      if (interior(seq[i])) order.push_back(seq[i]);
+    s->part_nint[q] = (int)order.size() - b0 - c0;
+    for (int i = b0 + c0; i < e0; ++i)
+      if (!interior(seq[i])) order.push_back(seq[i]);
+  }
   int bits = 1;
   while ((1 << bits) < Pmax) ++bits;
   int rank_bits = 0;
@@ -496,7 +551,7 @@ int resident_partition(srs_sim* s, int C) {
   s->eng_of_ref.assign(N, -1);
   for (int q = 0; q < C; ++q)
     for (int i = 0; i < s->part_len[q]; ++i) {
-      int j = seq[s->part_start[q] + i];
+      int j = order[s->part_start[q] + i];
       s->ref_of_eng[(size_t)q * s->P_stride + i] = j;
       s->eng_of_ref[j] = q * s->P_stride + i;
     }
@@ -572,6 +627,8 @@ int setup_resident(srs_sim* s, int C, int threads) {
   SRS_TRY(dev_upload(s, (TetRec**)&a.geo, geo.data(), geo.size()));
   SRS_TRY(dev_upload(s, (int32_t**)&a.n_local, s->part_len.data(), s->part_len.size()));
   SRS_TRY(dev_upload(s, (int32_t**)&a.n_chtet, s->part_nch.data(), s->part_nch.size()));
+  SRS_TRY(dev_upload(s, (int32_t**)&a.n_int, s->part_nint.data(), s->part_nint.size()));
+  a.ch_interior = s->ch_interior;
   std::vector<uint16_t> rc(s->NR), rj(s->NR), lc(s->NL);
   std::vector<float> lrest(s->NL);
   for (int i = 0; i < s->NR; ++i) {
@@ -860,11 +917,15 @@ int plain_steps(srs_sim* s, int64_t n) {
   return SRS_OK;
 }
 
-int resident_launch(srs_sim* s, int steps, int prestep_first = 0) {
+// speculate: no realization can finish inside this launch (the kernel then
+// updates the interior elements of a step before the cluster barrier of the
+// previous one completes).
+int resident_launch(srs_sim* s, int steps, int prestep_first = 0, int speculate = 1) {
   ResidentArgs a = s->ar;
   a.steps = steps;
   a.prestep_first = prestep_first;
   a.initial_row = prestep_first;
+  a.speculate = s->P.run_protocol ? speculate : 1;
   int rc = launch_resident(a, s->C, s->n_clusters, s->threads, s->smem, s->st);
   s->launches++;
   if (rc) return fail(SRS_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -1362,8 +1423,13 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
     // the first launch writes the t = 0 row and runs the protocol of step 0
     const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
     int first = 1;
+    int64_t launched = 0;
     while (true) {
-      SRS_TRY(resident_launch(s, S, first));
+      // without the fidelity criterion every realization finishes at step
+      // n_steps, so launches that end before it cannot see a termination
+      const int spec = !s->P.flag_fidelity && launched + S <= sc.n_steps;
+      SRS_TRY(resident_launch(s, S, first, spec));
+      launched += S;
       first = 0;
       SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
       bool all = true;
@@ -1787,6 +1853,8 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   aa.aT = s->d_aT;
   aa.n_local = s->ar.n_local;
   aa.n_chtet = s->ar.n_chtet;
+  aa.n_int = s->ar.n_int;
+  aa.ch_interior = s->ar.ch_interior;
   aa.ch_ptr = s->ar.ch_ptr;
   aa.ch_list = s->ar.ch_list;
   aa.ryr_cleft_code = s->ar.ryr_cleft_code;

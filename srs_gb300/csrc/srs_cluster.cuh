@@ -37,6 +37,17 @@ __device__ __forceinline__ void cluster_arrive_wait() {
                "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// Split cluster barrier: arrive (release) and wait (acquire) of one phase.
+// With C == 1 the CTA barrier of the caller orders everything.
+template <int C>
+__device__ __forceinline__ void cl_arrive() {
+  if constexpr (C > 1) asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+template <int C>
+__device__ __forceinline__ void cl_wait() {
+  if constexpr (C > 1) asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 template <int C>
 __device__ __forceinline__ void step_barrier() {
   if constexpr (C == 1) {

@@ -96,6 +96,10 @@ struct ResidentArgs {
   int32_t initial_row;    // ... and write the t = 0 states row
   const int32_t* n_local; // [C] elements in each partition
   const int32_t* n_chtet; // [1] channel elements (partition 0, offsets 0..n-1)
+  const int32_t* n_int;   // [C] interior elements (all neighbours in the same
+                          // partition), right after the channel elements
+  int32_t ch_interior;    // every channel element is interior to partition 0
+  int32_t speculate;      // no realization can finish inside this launch
   const int32_t* ch_ptr;  // [n_chtet+1] CSR of channel entries per channel element
   const ChanEntry32* ch_list;
   const uint16_t* ryr_cleft_code;
@@ -173,6 +177,8 @@ struct AdjArgs {
   const float4* aT;  // [C*P] coefficient of this element in each neighbour's row
   const int32_t* n_local;
   const int32_t* n_chtet;
+  const int32_t* n_int;    // [C] interior elements after the channel elements
+  int32_t ch_interior;     // every channel element is interior to partition 0
   const int32_t* ch_ptr;
   const ChanEntry32* ch_list;
   const uint16_t* ryr_cleft_code;
