@@ -288,15 +288,26 @@ struct ResidentCa {
 // Gating of every channel after time step ctl.step by one warp
 // (UpdateChannelGating, cpu/RunSimulation.cpp:656-674).  `src` holds the
 // state after that step; every channel element is local (partition 0).
+// Named barrier of the channel group (the first `n` threads of the CTA).
+__device__ __forceinline__ void group_sync(int n) {
+  if (n > 32) asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory");
+  else __syncwarp();
+}
+
+// Gating of every channel after time step ctl.step by the channel group of
+// partition 0 (UpdateChannelGating, cpu/RunSimulation.cpp:656-674): group
+// lane gl takes RyR gl, then LCC gl - NR, so with 64 lanes every channel of
+// a dyad is gated in one round.  `src` holds the state after that step;
+// every channel element is local (partition 0).
 __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const float4* src,
                               int32_t* s_ryr, int32_t* s_lcc, int32_t* s_lccv, double* s_res,
-                              int32_t* s_nb, int lane) {
+                              int32_t* s_nb, int gl, int ng) {
   const int NR = a.C.NR, NL = a.C.NL;
   const uint32_t mask = (1u << a.off_bits) - 1u;
   const srs_gate_consts* g = &a.P_.gc[ctl.vsel];
   const bool coupled = g->ryr_astar_half != 0.0f;
   if (coupled) {
-    for (int i = lane; i < NR; i += 32) {
+    for (int i = gl; i < NR; i += ng) {
       int no = 0, nc = 0;
       for (int q = 0; q < 4; ++q) {
         int j = a.C.ryr_nb[4 * i + q];
@@ -307,31 +318,34 @@ __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const float4*
       }
       s_nb[i] = no | (nc << 16);
     }
-    __syncwarp();
+    group_sync(ng);
   }
-  for (int i = lane; i < NR; i += 32) {
-    int no = 0, nc = 0;
-    if (coupled) {
-      no = s_nb[i] & 0xffff;
-      nc = s_nb[i] >> 16;
+  for (int q = gl; q < NR + NL; q += ng) {
+    if (q < NR) {
+      const int i = q;
+      int no = 0, nc = 0;
+      if (coupled) {
+        no = s_nb[i] & 0xffff;
+        nc = s_nb[i] >> 16;
+      }
+      float cs = src[a.ryr_cleft_code[i] & mask].x + a.k.c0;
+      float cj = src[a.ryr_jsr_code[i] & mask].x + a.k.c0j;
+      double rr = s_res[i];
+      s_ryr[i] = srs_gate_ryr(g, s_ryr[i], cs, cj, no, nc, &rr, ctl.seed, (uint32_t)i,
+                              (uint64_t)ctl.step);
+      s_res[i] = rr;
+    } else {
+      const int i = q - NR;
+      float cs = src[a.lcc_code[i] & mask].x + a.lcc_rest[i];
+      double rr = s_res[NR + i];
+      int st = s_lcc[i], vs = s_lccv[i];
+      srs_gate_lcc(g, &st, &vs, cs, &rr, ctl.seed, (uint32_t)(NR + i), (uint64_t)ctl.step);
+      s_lcc[i] = st;
+      s_lccv[i] = vs;
+      s_res[NR + i] = rr;
     }
-    float cs = src[a.ryr_cleft_code[i] & mask].x + a.k.c0;
-    float cj = src[a.ryr_jsr_code[i] & mask].x + a.k.c0j;
-    double rr = s_res[i];
-    s_ryr[i] = srs_gate_ryr(g, s_ryr[i], cs, cj, no, nc, &rr, ctl.seed, (uint32_t)i,
-                            (uint64_t)ctl.step);
-    s_res[i] = rr;
   }
-  for (int i = lane; i < NL; i += 32) {
-    float cs = src[a.lcc_code[i] & mask].x + a.lcc_rest[i];
-    double rr = s_res[NR + i];
-    int st = s_lcc[i], vs = s_lccv[i];
-    srs_gate_lcc(g, &st, &vs, cs, &rr, ctl.seed, (uint32_t)(NR + i), (uint64_t)ctl.step);
-    s_lcc[i] = st;
-    s_lccv[i] = vs;
-    s_res[NR + i] = rr;
-  }
-  __syncwarp();
+  group_sync(ng);
 }
 
 // Protocol of step ctl.step (rank 0, warp 0; lane 0 does the work).
@@ -388,11 +402,14 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
   const int nthr = blockDim.x;
   const int n_loc = a.n_local[rank];
   const int n_ch = (rank == 0) ? a.n_chtet[0] : 0;  // channel elements: rank 0 only
+  // In partition 0 the channel group (the first ng threads: two warps when
+  // the CTA has at least four) owns the channel elements, gates the channels
+  // right after updating them and runs the protocol; the other warps share
+  // the rest.  Elsewhere every thread strides over the whole partition.
+  const int ng = nthr >= 128 ? 64 : 32;
+  const bool split = (rank == 0) && (n_ch > 0) && (nthr > ng);
+  const bool chan_group = split && tid < ng;
   const bool chan_warp = (rank == 0) && (warp == 0);
-  // Element ranges: in partition 0, warp 0 owns the channel elements (which
-  // it gates right after updating them) and the other warps share the rest;
-  // elsewhere every thread strides over the whole partition.
-  const bool split = (rank == 0) && (n_ch > 0) && (nthr > 32);
   const int n_int = a.n_int[rank];  // interior elements follow the channel elements
   const TetRec* geo = a.geo + (size_t)rank * P;
   const uint32_t off_mask = (1u << a.off_bits) - 1u;
@@ -445,6 +462,11 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
     step_barrier<C>();
     const bool skip = ((C > 1) ? ld_dsmem_s32(done_addr0 + 12u) : tail->done_flag[3]) != 0;
     int cur = 0;
+    // Speculation is safe when no termination can be decided inside this
+    // launch: without the protocol nothing terminates, and without the
+    // fidelity criterion a run ends exactly at step n_steps.
+    const bool spec = a.speculate && (!P_.run_protocol ||
+                                      (!P_.flag_fidelity && tail->ctl.step + a.steps <= P_.n_steps));
     if (!skip) {
       // Barrier phases: the arrive that ends step s is waited on at the top of
       // step s + 1 -- after the step's interior elements when speculating
@@ -546,17 +568,19 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         // next, by warp 0 of partition 0 (split) or after the whole CTA
         auto channels = [&]() {
           if (split) {
-            if (chan_warp) {
-              update(lane, n_ch, 32);
-              __syncwarp();  // warp 0 wrote the channel elements itself
+            if (chan_group) {
+              update(tid, n_ch, ng);
+              group_sync(ng);  // the group wrote the channel elements itself
+              if (!P_.nogating) resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, tid, ng);
             }
           } else {
             update(tid, n_ch, nthr);
             __syncthreads();
+            if (chan_warp && !P_.nogating)
+              resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane, 32);
           }
           if (chan_warp) {
             RealCtl& ctl = tail->ctl;
-            if (!P_.nogating) resident_gate(a, ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane);
             if (lane == 0) {
               ctl.step += 1;
               ctl.t += P_.dt;
@@ -572,9 +596,9 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
           const uint32_t slot = (uint32_t)((s - 1) & 3);
           return ((C > 1) ? ld_dsmem_s32(done_addr0 + 4u * slot) : tail->done_flag[slot]) != 0;
         };
-        const bool worker = !(split && chan_warp);  // not the channel warp
-        const int wt = split ? tid - 32 : tid, wn = split ? nthr - 32 : nthr;
-        if (!a.speculate) {
+        const bool worker = !chan_group;  // not the channel group
+        const int wt = split ? tid - ng : tid, wn = split ? nthr - ng : nthr;
+        if (!spec) {
           cl_wait<C>();
           pending = false;
           if (finished()) break;
@@ -582,7 +606,7 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         // interior elements: neighbours all in this partition
         if (worker) update(n_ch + wt, n_ch + n_int, wn);
         if (a.ch_interior && rank == 0 && n_ch > 0) channels();
-        if (a.speculate) {
+        if (spec) {
           cl_wait<C>();
           pending = false;
           if (finished()) {  // cannot happen when the host allows speculation

@@ -457,11 +457,14 @@ int setup_plain32(srs_sim* s) {
 }
 
 // ---- FP32 resident engine ----------------------------------------------------
-int resident_partition(srs_sim* s, int C) {
+int resident_partition(srs_sim* s, int C, int threads) {
   // Order: the elements that carry channels, then breadth-first layers
   // outward from them over the diffusion faces (so partition 0 holds the
   // channels' neighbourhood and partitions are cut between layers); the
-  // sequence is cut into C contiguous partitions of equal size.  Inside each
+  // sequence is cut into C contiguous partitions that give every element
+  // thread the same number of elements (in partition 0 the channel group of
+  // 64 threads -- 32 in small CTAs -- takes the channel elements and the
+  // gating instead).  Inside each
   // partition: channel elements (partition 0 only), then interior elements
   // (every neighbour in the same partition), then boundary elements.
   const int N = s->N;
@@ -507,11 +510,24 @@ int resident_partition(srs_sim* s, int C) {
   s->part_nch.assign(C, 0);
   s->part_nint.assign(C, 0);
   int Pmax = 0;
-  for (int q = 0; q < C; ++q) {
-    int b0 = (int)((int64_t)N * q / C), e0 = (int)((int64_t)N * (q + 1) / C);
-    s->part_start[q] = b0;
-    s->part_len[q] = e0 - b0;
-    Pmax = std::max(Pmax, e0 - b0);
+  {
+    const int ng = threads >= 128 ? 64 : 32;
+    const bool split = C > 1 && n_ch > 0 && threads > ng;
+    int len0 = (int)((int64_t)N / C);
+    if (split) {
+      const double lam = (double)(N - n_ch) / ((double)C * threads - ng);
+      len0 = std::min(N, std::max(n_ch, n_ch + (int)std::lround(lam * (threads - ng))));
+    }
+    if (C == 1) len0 = N;
+    s->part_start[0] = 0;
+    s->part_len[0] = len0;
+    for (int q = 1; q < C; ++q) {
+      const int b0 = len0 + (int)((int64_t)(N - len0) * (q - 1) / (C - 1));
+      const int e0 = len0 + (int)((int64_t)(N - len0) * q / (C - 1));
+      s->part_start[q] = b0;
+      s->part_len[q] = e0 - b0;
+    }
+    for (int q = 0; q < C; ++q) Pmax = std::max(Pmax, s->part_len[q]);
   }
   if (n_ch > s->part_len[0])
     return fail(SRS_ERR_UNSUPPORTED, "channel elements do not fit in one partition");
@@ -565,7 +581,7 @@ uint16_t code_of(const srs_sim* s, int eng) {
 
 int setup_resident(srs_sim* s, int C, int threads) {
   SRS_TRY(check_fp32_supported(s, true));
-  SRS_TRY(resident_partition(s, C));
+  SRS_TRY(resident_partition(s, C, threads));
   const int N = s->N;
   const int NE = C * s->P_stride;
   // rest arrays over the padded engine numbering
@@ -917,15 +933,12 @@ int plain_steps(srs_sim* s, int64_t n) {
   return SRS_OK;
 }
 
-// speculate: no realization can finish inside this launch (the kernel then
-// updates the interior elements of a step before the cluster barrier of the
-// previous one completes).
-int resident_launch(srs_sim* s, int steps, int prestep_first = 0, int speculate = 1) {
+int resident_launch(srs_sim* s, int steps, int prestep_first = 0) {
   ResidentArgs a = s->ar;
   a.steps = steps;
   a.prestep_first = prestep_first;
   a.initial_row = prestep_first;
-  a.speculate = s->P.run_protocol ? speculate : 1;
+  a.speculate = 1;
   int rc = launch_resident(a, s->C, s->n_clusters, s->threads, s->smem, s->st);
   s->launches++;
   if (rc) return fail(SRS_ERR_CUDA, std::string("resident launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -1423,13 +1436,8 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
     // the first launch writes the t = 0 row and runs the protocol of step 0
     const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
     int first = 1;
-    int64_t launched = 0;
     while (true) {
-      // without the fidelity criterion every realization finishes at step
-      // n_steps, so launches that end before it cannot see a termination
-      const int spec = !s->P.flag_fidelity && launched + S <= sc.n_steps;
-      SRS_TRY(resident_launch(s, S, first, spec));
-      launched += S;
+      SRS_TRY(resident_launch(s, S, first));
       first = 0;
       SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
       bool all = true;
@@ -1810,6 +1818,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     ra.steps = len;
     ra.prestep_first = 0;
     ra.initial_row = 0;
+    ra.speculate = 1;
     ra.traj_u = traj_u;
     ra.traj_im = traj_im;
     ra.traj_g = traj_g;

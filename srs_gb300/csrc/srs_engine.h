@@ -99,7 +99,9 @@ struct ResidentArgs {
   const int32_t* n_int;   // [C] interior elements (all neighbours in the same
                           // partition), right after the channel elements
   int32_t ch_interior;    // every channel element is interior to partition 0
-  int32_t speculate;      // no realization can finish inside this launch
+  int32_t speculate;      // allow updating interior elements before the
+                          // barrier completes where no realization can
+                          // finish inside the launch (decided per realization)
   const int32_t* ch_ptr;  // [n_chtet+1] CSR of channel entries per channel element
   const ChanEntry32* ch_list;
   const uint16_t* ryr_cleft_code;
