@@ -64,6 +64,7 @@ __device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& a
 // ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16]; then, when
 // `own_in_smem`, the owner state float4 c4[P], float lc[P], lim[P], cim[P].
 size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem) {
+  // P: element slots of one CTA
   size_t b = (size_t)2 * P * sizeof(float4);
   b += (size_t)32 * NA * sizeof(double);
   b += (size_t)(n_chtet + 1) * sizeof(int32_t);
@@ -112,10 +113,12 @@ __device__ __forceinline__ float sl_inv_factor(const Consts32& k, float bsl, flo
 template <int C>
 __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int P = a.P;
+  const int P = a.P;           // stride of the forward engine's partitions
+  const int msub = a.m_sub;    // forward partitions per CTA
+  const int Pc = msub * P;     // this CTA's element slots
   float4* pub0 = reinterpret_cast<float4*>(smem);
-  float4* pub1 = pub0 + P;
-  double* red = reinterpret_cast<double*>(pub1 + P);
+  float4* pub1 = pub0 + Pc;
+  double* red = reinterpret_cast<double*>(pub1 + Pc);
   int32_t* s_cptr = reinterpret_cast<int32_t*>(red + 32 * NA);
   const int n_ch0 = a.n_chtet[0];
   ChanEntry32* s_clist = reinterpret_cast<ChanEntry32*>(
@@ -123,20 +126,28 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   const int n_ent = a.ch_ptr[n_ch0];
   uint32_t* s_base = reinterpret_cast<uint32_t*>(s_clist + n_ent);  // [2][16]
   float4* sm_c4 = reinterpret_cast<float4*>(s_base + 32);
-  float* sm_lc = reinterpret_cast<float*>(sm_c4 + P);
-  float* sm_lim = sm_lc + P;
-  float* sm_cim = sm_lim + P;
+  float* sm_lc = reinterpret_cast<float*>(sm_c4 + Pc);
+  float* sm_lim = sm_lc + Pc;
+  float* sm_cim = sm_lim + Pc;
 
   uint32_t rank = 0;
   if constexpr (C > 1) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
   const int cid = blockIdx.x / C, ncl = gridDim.x / C;
   const int tid = threadIdx.x, nthr = blockDim.x;
-  const int n_loc = a.n_local[rank];
-  const int n_ch = rank == 0 ? n_ch0 : 0;
-  const size_t NE = (size_t)C * P;
-  const TetRec* geo = a.geo + (size_t)rank * P;
-  const float4* aT = a.aT + (size_t)rank * P;
+  const int n_ch = rank == 0 ? n_ch0 : 0;  // channel elements: forward partition 0
+  const size_t NE = (size_t)C * Pc;
+  const TetRec* geo = a.geo + (size_t)rank * Pc;
+  const float4* aT = a.aT + (size_t)rank * Pc;
   const uint32_t mask = (1u << a.off_bits) - 1u;
+  const uint32_t ch_mask = (1u << a.ch_off_bits) - 1u;  // channel codes: forward layout
+  // element ranges of this CTA: forward partitions rank*msub .. + msub - 1,
+  // each [channel | interior | boundary] at offset j*P
+  auto for_range = [&](int lo, int hi, auto&& f) {
+    for (int i = lo + tid; i < hi; i += nthr) f(i);
+  };
+  auto for_all = [&](auto&& f) {
+    for (int j = 0; j < msub; ++j) for_range(j * P, j * P + a.n_local[rank * msub + j], f);
+  };
   const Consts32& k = a.k;
   const AdjConsts& ak = a.ak;
   const int NR = a.NR, NL = a.NL, W = NR + 2 * NL + 1;
@@ -152,7 +163,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   step_barrier<C>();
 
   for (int r = cid; r < a.R; r += ncl) {
-    const size_t roff = (size_t)r * NE + (size_t)rank * P;  // lambda, this partition
+    const size_t roff = (size_t)r * NE + (size_t)rank * Pc;  // lambda, this CTA
     // owner state: on chip when it fits, else the global arrays themselves
     float* lc = a.own_in_smem ? sm_lc : a.lam_c + roff;
     float* lim = a.own_in_smem ? sm_lim : a.lam_im + roff;
@@ -161,14 +172,14 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     const int len = a.n_steps;
     // ---- publish lambda_{s1} (with the tick injection of step s1) ----------
     {
-      const size_t xo = ((size_t)(len - 1) * a.R + r) * NE + (size_t)rank * P;
+      const size_t xo = ((size_t)(len - 1) * a.R + r) * NE + (size_t)rank * Pc;
       const double* coef = tick_coef(a, a.s0 + len, r);
-      for (int i = tid; i < n_loc; i += nthr) {
+      for_all([&](int i) {
         const float4 L = a.lam[roff + i];
         const float4 gb = __ldg(reinterpret_cast<const float4*>(geo + i) + 1);
         const uint32_t fl = __float_as_uint(gb.w);
         const float c = ((fl & 1u) ? k.c0j : k.c0) + a.traj_u[xo + i].x;
-        const float inj = tick_injection(a, coef, (int)(rank * P + i));
+        const float inj = tick_injection(a, coef, (int)(rank * Pc + i));
         pub0[i] = make_float4(L.x * sl_inv_factor(k, gb.z, c), L.y, L.z, L.w + inj);
         lc[i] = L.x;
         if (a.own_in_smem) {
@@ -176,7 +187,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           cim[i] = a.lam_cim[roff + i];
           c4[i] = a.lam_c4[roff + i];
         }
-      }
+      });
     }
     const int warp = tid >> 5, lane = tid & 31, nw = nthr >> 5;
     // per-warp FP64 accumulators of this realization's gradient
@@ -192,11 +203,11 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       const float4* pub = cur ? pub1 : pub0;
       float4* nxt = cur ? pub0 : pub1;
       const uint32_t* bs = s_base + 16 * cur;
-      const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * P;
+      const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * Pc;
       const float4* __restrict__ tu = a.traj_u + xoff;
       const float* __restrict__ tim = a.traj_im + xoff;
       const float* __restrict__ tg = a.traj_g + xoff;
-      const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * P;
+      const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
       float gstep[NA];  // this thread's contributions of this step
@@ -293,12 +304,12 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
             if (e.kind < 2) {
               if (rec[e.ch]) {
                 const uint32_t oc_code = e.kind == 0 ? a.ryr_jsr_code[e.ch] : a.ryr_cleft_code[e.ch];
-                const float wo = pub[oc_code & mask].x;
+                const float wo = pub[oc_code & ch_mask].x;
                 const float so = e.kind == 0 ? a.ryr_s_js[e.ch] : a.ryr_s_cl[e.ch];
                 const float qv = fmaf(w, e.s, wo * so);
                 if (e.kind == 0) {
                   oc = fmaf(-k.jr_scale, qv, oc);
-                  const float cj = k.c0j + a.traj_u[xoff + (oc_code & mask)].x;
+                  const float cj = k.c0j + a.traj_u[xoff + (oc_code & ch_mask)].x;
                   g[SRS_ADJ_V_RYR] = fmaf(qv * ak.v_cell, cj - c, g[SRS_ADJ_V_RYR]);
                 } else {
                   oc = fmaf(k.jr_scale, qv, oc);
@@ -334,7 +345,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         kadd(lnew, ci, k.dt * oi);
         if (t > 1) {
           const float cprev = (jsr ? k.c0j : k.c0) + a.traj_u[xprev + i].x;
-          const float inj = tick_injection(a, coef_next, (int)(rank * P + i));
+          const float inj = tick_injection(a, coef_next, (int)(rank * Pc + i));
           nxt[i] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
           lc[i] = L.x;
           lim[i] = lnew;
@@ -349,13 +360,18 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 #pragma unroll
         for (int p = 0; p < NA; ++p) gstep[p] += g[p];
       };
-      // interior elements (and the channel elements when they are interior)
-      const int i0 = n_ch + a.n_int[rank];
-      for (int i = (a.ch_interior ? 0 : n_ch) + tid; i < i0; i += nthr) element(i);
+      // interior elements (and the channel elements when they are interior):
+      // interior to their forward partition, hence to this CTA
+      for (int j = 0; j < msub; ++j) {
+        const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
+        for_range(j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
+      }
       cl_wait<C>();
-      if (!a.ch_interior)
-        for (int i = tid; i < n_ch; i += nthr) element(i);
-      for (int i = i0 + tid; i < n_loc; i += nthr) element(i);
+      for (int j = 0; j < msub; ++j) {
+        const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
+        if (!a.ch_interior) for_range(j * P, j * P + nc, element);
+        for_range(j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
+      }
       __syncthreads();
       cl_arrive<C>();
       // step sums of the warp (FP32 over its ~hundred terms) into its FP64

@@ -101,6 +101,8 @@ struct srs_sim {
   int32_t* d_wt_idx = nullptr;
   double* d_wt_w = nullptr;
   int adj_ls_version = -1;
+  TetRec* d_adj_geo = nullptr;  // geometry with the adjoint's CTA grouping
+  int adj_geo_m = 0;
   // total Ca (built on first use)
   MassArgs mass{};
   // adjoint work buffers, kept between calls (name -> allocation)
@@ -1702,6 +1704,41 @@ struct StateSnap {
   RealCtl* ctl;
 };
 
+// Geometry records with neighbour codes for CTAs that each hold m
+// consecutive partitions of the forward layout (same element order, so every
+// per-element array keeps its index).
+int adjoint_geometry(srs_sim* s, int m, int bits) {
+  if (s->d_adj_geo && s->adj_geo_m == m) return SRS_OK;
+  const int Pf = s->P_stride, NE = (int)eng_count(s);
+  auto mcode = [&](int e) -> uint16_t {
+    const int q = e / Pf, off = e % Pf;
+    return (uint16_t)(((q / m) << bits) | ((q % m) * Pf + off));
+  };
+  std::vector<TetRec> geo(NE);
+  std::memset(geo.data(), 0, geo.size() * sizeof(TetRec));
+  for (int e = 0; e < NE; ++e) {
+    const int j = s->ref_of_eng[e];
+    if (j < 0) {
+      for (int k = 0; k < 4; ++k) geo[e].nb[k] = mcode(e);
+      continue;
+    }
+    for (int k = 0; k < 4; ++k) {
+      geo[e].a[k] = (float)s->op.aij[5 * (size_t)j + 1 + k];
+      geo[e].nb[k] = mcode(s->eng_of_ref[s->op.nij[4 * (size_t)j + k]]);
+    }
+    geo[e].bsl = bsl_of(s, j);
+    geo[e].flags = (s->m.domain[j] == DOMAIN_JSR ? 1u : 0u) | (s->m.tropc[j] ? 2u : 0u) |
+                   (e < s->part_nch[0] ? 4u : 0u);
+  }
+  if (s->d_adj_geo) {
+    SRS_CUDA(cudaMemcpy(s->d_adj_geo, geo.data(), geo.size() * sizeof(TetRec), cudaMemcpyHostToDevice));
+  } else {
+    SRS_TRY(dev_upload(s, &s->d_adj_geo, geo.data(), geo.size()));
+  }
+  s->adj_geo_m = m;
+  return SRS_OK;
+}
+
 int snap_alloc(srs_sim* s, Scratch& sc, StateSnap* o) {
   const size_t n = (size_t)s->R * eng_count(s);
   SRS_TRY(sc.get(&o->M, n));
@@ -1857,8 +1894,6 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   AdjArgs aa{};
   aa.R = R;
   aa.P = s->P_stride;
-  aa.off_bits = s->off_bits;
-  aa.geo = s->ar.geo;
   aa.aT = s->d_aT;
   aa.n_local = s->ar.n_local;
   aa.n_chtet = s->ar.n_chtet;
@@ -1901,16 +1936,46 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   }
   const int n_ent = 2 * NR + NL;
   const int adj_threads = 512;
-  // owner state of lambda on chip when it fits next to the published slots
-  size_t adj_smem = adjoint_smem_bytes(s->P_stride, s->part_nch[0], n_ent, true);
-  int adj_ncl = (d->flags & SRS_ADJ_LAMBDA_GLOBAL) ? 0 : adjoint_max_clusters(s->C, adj_threads, adj_smem);
-  aa.own_in_smem = adj_ncl > 0;
-  if (!aa.own_in_smem) {
-    adj_smem = adjoint_smem_bytes(s->P_stride, s->part_nch[0], n_ent, false);
-    adj_ncl = adjoint_max_clusters(s->C, adj_threads, adj_smem);
+  // CTA grouping: m forward partitions per CTA (clusters of C/m CTAs), the
+  // owner state of lambda on chip when it fits next to the published slots.
+  // Chosen by the estimated time: rounds of clusters x slots per thread.
+  int best_m = 0, best_C = 0, adj_ncl = 0, best_bits = 0;
+  size_t adj_smem = 0;
+  bool best_own = false;
+  double best_cost = 1e300;
+  for (int m = 1; m <= s->C; ++m) {
+    if (s->C % m) continue;
+    const int Ca = s->C / m, Pc = m * s->P_stride;
+    int bits = 1, rbits = 0;
+    while ((1 << bits) < Pc) ++bits;
+    while ((1 << rbits) < Ca) ++rbits;
+    if (bits + rbits > 16) continue;
+    for (int own = 1; own >= 0; --own) {
+      if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
+      const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0);
+      const int ncl = std::min(adjoint_max_clusters(Ca, adj_threads, sm), R);
+      if (ncl <= 0) continue;
+      const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / adj_threads) *
+                          (own ? 1.0 : 1.15);
+      if (cost < best_cost) {
+        best_cost = cost;
+        best_m = m;
+        best_C = Ca;
+        adj_ncl = ncl;
+        adj_smem = sm;
+        best_own = own != 0;
+        best_bits = bits;
+      }
+      break;  // the on-chip variant when it fits
+    }
   }
-  adj_ncl = std::min(adj_ncl, R);
   if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
+  SRS_TRY(adjoint_geometry(s, best_m, best_bits));
+  aa.own_in_smem = best_own;
+  aa.m_sub = best_m;
+  aa.off_bits = best_bits;
+  aa.ch_off_bits = s->off_bits;
+  aa.geo = s->d_adj_geo;
   AdjTickArgs ta{};
   ta.n_samples = ns;
   ta.n_state = (int32_t)NE;
@@ -1939,7 +2004,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     }
     aa.n_steps = len;
     aa.s0 = s0;
-    if (launch_adjoint(aa, s->C, adj_ncl, adj_threads, adj_smem, s->st))
+    if (launch_adjoint(aa, best_C, adj_ncl, adj_threads, adj_smem, s->st))
       return fail(SRS_ERR_CUDA, std::string("adjoint launch: ") + cudaGetErrorString(cudaGetLastError()));
     s->launches++;
   }

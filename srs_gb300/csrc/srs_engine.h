@@ -172,10 +172,12 @@ struct AdjConsts {
 };
 
 struct AdjArgs {
-  int32_t R, P, off_bits;
+  int32_t R, P, off_bits;  // P: forward partition stride; off_bits of the codes in geo
+  int32_t m_sub;           // forward partitions per CTA (CTA slots m_sub * P)
+  int32_t ch_off_bits;     // off_bits of the forward layout (channel codes)
   int32_t n_steps;  // steps of the segment; the kernel runs t = n_steps .. 1
   int64_t s0;       // global index of the state the segment starts from
-  const TetRec* geo;
+  const TetRec* geo;  // geometry with neighbour codes of the CTA grouping
   const float4* aT;  // [C*P] coefficient of this element in each neighbour's row
   const int32_t* n_local;
   const int32_t* n_chtet;
