@@ -20,9 +20,10 @@
 // the forward engine recorded for the segment.  Lambda lives in HBM/L2 in
 // owner-only arrays with Kahan compensation, like the forward state.
 //
-// Parameter gradients: each step, every warp sums its elements' terms in FP32
-// (a warp-shuffle reduction) and adds that step sum to a per-warp FP64
-// accumulator in shared memory; at the end of a realization the warps' sums
+// Parameter gradients: every thread sums its elements' terms in FP32 over up
+// to 16 steps; then each warp reduces those sums (warp shuffles) and adds
+// them to a per-warp FP64 accumulator in shared memory; at the end of a
+// realization the warps' sums
 // are added in FP64 to the per-realization gradient, which therefore
 // accumulates over all steps and segments (the long reverse sweep) in double
 // precision.
@@ -142,11 +143,16 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   const uint32_t ch_mask = (1u << a.ch_off_bits) - 1u;  // channel codes: forward layout
   // element ranges of this CTA: forward partitions rank*msub .. + msub - 1,
   // each [channel | interior | boundary] at offset j*P
-  auto for_range = [&](int lo, int hi, auto&& f) {
-    for (int i = lo + tid; i < hi; i += nthr) f(i);
+  // Ranges are walked as one concatenated sequence: element k of the
+  // sequence goes to thread k % nthr, so every thread gets the same count.
+  auto for_range = [&](int& idx, int lo, int hi, auto&& f) {
+    const int n = hi - lo;
+    for (; idx < n; idx += nthr) f(lo + idx);
+    idx -= n;
   };
   auto for_all = [&](auto&& f) {
-    for (int j = 0; j < msub; ++j) for_range(j * P, j * P + a.n_local[rank * msub + j], f);
+    int idx = tid;
+    for (int j = 0; j < msub; ++j) for_range(idx, j * P, j * P + a.n_local[rank * msub + j], f);
   };
   const Consts32& k = a.k;
   const AdjConsts& ak = a.ak;
@@ -193,6 +199,9 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     // per-warp FP64 accumulators of this realization's gradient
     for (int q = tid; q < nw * NA; q += nthr) red[q] = 0.0;
     int cur = 0;
+    float gstep[NA];  // this thread's contributions of the last few steps (FP32)
+#pragma unroll
+    for (int p = 0; p < NA; ++p) gstep[p] = 0.0f;
     // barrier phases: the arrive after the publication of step t's slots is
     // waited on after the interior elements of step t, whose neighbours'
     // slots all live in this CTA (the __syncthreads orders those)
@@ -210,9 +219,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
-      float gstep[NA];  // this thread's contributions of this step
-#pragma unroll
-      for (int p = 0; p < NA; ++p) gstep[p] = 0.0f;
+
       auto element = [&](int i) {
         const float4 x = __ldg(tu + i);
         const float xim = __ldg(tim + i);
@@ -362,25 +369,29 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       };
       // interior elements (and the channel elements when they are interior):
       // interior to their forward partition, hence to this CTA
+      int idx = tid;
       for (int j = 0; j < msub; ++j) {
         const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-        for_range(j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
+        for_range(idx, j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
       }
       cl_wait<C>();
       for (int j = 0; j < msub; ++j) {
         const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-        if (!a.ch_interior) for_range(j * P, j * P + nc, element);
-        for_range(j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
+        if (!a.ch_interior) for_range(idx, j * P, j * P + nc, element);
+        for_range(idx, j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
       }
       __syncthreads();
       cl_arrive<C>();
-      // step sums of the warp (FP32 over its ~hundred terms) into its FP64
-      // accumulators: the sum over the steps runs in double precision
+      // every 16 steps (and at the end) the warp's FP32 sums go into its FP64
+      // accumulators: the long sum over the steps runs in double precision
+      if (((t - 1) & 15) == 0) {
 #pragma unroll
-      for (int p = 0; p < NA; ++p) {
-        float v = gstep[p];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp * NA + p] += (double)v;
+        for (int p = 0; p < NA; ++p) {
+          float v = gstep[p];
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if (lane == 0) red[warp * NA + p] += (double)v;
+          gstep[p] = 0.0f;
+        }
       }
       cur ^= 1;
     }

@@ -495,15 +495,20 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         // one range of elements of this partition; elements that carry
         // channels (head of partition 0) add the release flux of their
         // channels, computed from the state of this step
-        auto update = [&](int lo, int hi, int stride) {
+        // Elements lo + idx, lo + idx + stride, ... below hi; idx carries
+        // over to the next range, so consecutive ranges are dealt out as
+        // one sequence and every thread gets the same count.
+        auto update = [&](int& idx, int lo, int hi, int stride) {
+          const int first = lo + idx;
           // geometry of the next element is loaded one iteration ahead
           float4 ga_n = make_float4(0, 0, 0, 0), gb_n = ga_n;
-          if (lo < hi) {
-            const float4* gp = reinterpret_cast<const float4*>(geo + lo);
+          if (first < hi) {
+            const float4* gp = reinterpret_cast<const float4*>(geo + first);
             ga_n = __ldg(gp);
             gb_n = __ldg(gp + 1);
           }
-          for (int i = lo; i < hi; i += stride) {
+          int i = first;
+          for (; i < hi; i += stride) {
             const float4 ga = ga_n, gb = gb_n;
             if (i + stride < hi) {
               const float4* gp = reinterpret_cast<const float4*>(geo + i + stride);
@@ -563,18 +568,21 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             cib[i] = ci;
             bad |= !isfinite(out.x);
           }
+          idx = i - hi;
         };
         // channel elements, then gating of this step and the protocol of the
         // next, by warp 0 of partition 0 (split) or after the whole CTA
         auto channels = [&]() {
           if (split) {
             if (chan_group) {
-              update(tid, n_ch, ng);
+              int idx = tid;
+              update(idx, 0, n_ch, ng);
               group_sync(ng);  // the group wrote the channel elements itself
               if (!P_.nogating) resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, tid, ng);
             }
           } else {
-            update(tid, n_ch, nthr);
+            int idx = tid;
+            update(idx, 0, n_ch, nthr);
             __syncthreads();
             if (chan_warp && !P_.nogating)
               resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane, 32);
@@ -604,7 +612,8 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
           if (finished()) break;
         }
         // interior elements: neighbours all in this partition
-        if (worker) update(n_ch + wt, n_ch + n_int, wn);
+        int idx = wt;
+        if (worker) update(idx, n_ch, n_ch + n_int, wn);
         if (a.ch_interior && rank == 0 && n_ch > 0) channels();
         if (spec) {
           cl_wait<C>();
@@ -615,7 +624,7 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
           }
         }
         // boundary elements: some neighbour in another partition
-        if (worker) update(n_ch + n_int + wt, n_loc, wn);
+        if (worker) update(idx, n_ch + n_int, n_loc, wn);
         if (!a.ch_interior && rank == 0 && n_ch > 0) channels();
         __syncthreads();
         cl_arrive<C>();

@@ -115,7 +115,7 @@ def test_adjoint_matches_fp64_finite_differences(srs, case):
 def test_adjoint_segmentation_and_cluster_size_do_not_change_the_result(srs, case, K2, C):
     """The trajectory and lambda are bit-identical for any checkpoint interval
     and cluster size; only the grouping of the FP32 partial sums of the
-    gradient changes (1e-6)."""
+    gradient changes (1e-5)."""
     p = case["p"]
     g = srs.Grid(p, GOLDEN_MESH)
     sim = srs.Simulation(g, p, len(SEEDS), srs.FP32, srs.ENGINE_RESIDENT, seeds=SEEDS, cluster_size=C)
@@ -126,7 +126,7 @@ def test_adjoint_segmentation_and_cluster_size_do_not_change_the_result(srs, cas
                                  grad_state=True)
     assert np.array_equal(loss, case["loss"])
     assert np.array_equal(gs, case["gs"])
-    assert np.allclose(grad, case["grad"], rtol=1e-6, atol=0)
+    assert np.allclose(grad, case["grad"], rtol=1e-5, atol=0)
 
 
 def test_adjoint_state_in_global_memory_gives_the_same_result(srs, case):
