@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost leg")
     ap.add_argument("--adjoint-realizations", type=int, default=64)
     ap.add_argument("--adjoint-steps", type=int, default=4096)
+    ap.add_argument("--no-config2", action="store_true", help="skip the multi-mesh batch leg")
+    ap.add_argument("--config2-steps", type=int, default=4000)
     return ap.parse_args()
 
 
@@ -312,6 +314,44 @@ def adjoint_cost(srs, grid, p, args):
     return out
 
 
+def config2_batch(srs, args):
+    """Uneven multi-mesh batch: four box dyads (6k / 15k / 30k / 60k tets,
+    Poisson-disk clusters of 10 / 25 / 60 / 100 RyRs, one LCC per 7 RyRs) x
+    two protocols (leak: clamped at rest, no trigger; LCC-triggered: clamped
+    at 0 mV) x 32 realizations = 256 realizations, each member at its tuned
+    resident configuration, advanced by one CUDA graph per 1000 steps.
+    Reported against the same members advanced one after another."""
+    from srs_gb300 import tuner
+    from srs_gb300 import workloads as wl
+    tmp = tempfile.mkdtemp(prefix="srs_c2_")
+    sims, sim_ms = [], 0.0
+    seed0 = 1
+    for base, rep_ in wl.config2_meshes(tmp):
+        for p in wl.config2_protocols(rep_["max_a0"]):
+            g = srs.Grid(p, base)
+            seeds = list(range(seed0, seed0 + 32))
+            seed0 += 32
+            t = tuner.tune_resident(g, p, 32, seeds=seeds)
+            sim = srs.Simulation(g, p, 32, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                                 cluster_size=t["cluster_size"], threads_per_cta=t["threads_per_cta"],
+                                 steps_per_launch=1000)
+            sim.reset()
+            sims.append(sim)
+    n = args.config2_steps
+    spark_ms = sum(s.R * n * s.params.reals[srs.R["T_STEP"]] for s in sims)
+    for s in sims:  # members one after another
+        s.time_advance(1000)
+        sim_ms += s.time_advance(n)
+    b = srs.Batch(sims, steps_per_launch=1000)
+    b.time_advance(1000)
+    ms = b.time_advance(n)
+    return {"workload": "config2: 4 meshes (6000/15288/29478/60984 tets; 10/25/60/100 RyR) x "
+                        "2 protocols x 32 realizations, %d steps" % n,
+            "value": spark_ms / (ms / 1e3), "unit": UNIT, "batch_ms": ms,
+            "members_one_by_one_ms": sim_ms,
+            "cluster_sizes": [s.config()["cluster_size"] for s in sims]}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     dist = dist_init(ws)
@@ -401,6 +441,9 @@ def run_ours(args):
     adj = None
     if rank == 0 and not args.no_adjoint:
         adj = adjoint_cost(srs, grid, p, args)
+    c2 = None
+    if rank == 0 and not args.no_config2:
+        c2 = config2_batch(srs, args)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -428,6 +471,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "adjoint": adj,
+            "config2": c2,
         }
         print(json.dumps(line))
     if dist is not None:

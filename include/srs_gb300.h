@@ -195,6 +195,28 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples);
  * F of the equilibrium state (for dF/F0). */
 int srs_linescan(srs_sim* s, double* out, double* rest);
 
+/* ---- multi-mesh batch ----------------------------------------------------------
+ * No reference counterpart (the reference runs one mesh per process and one
+ * realization at a time).  Several FP32 resident simulations -- different
+ * grids, parameter sets, protocols, realization counts and launch
+ * configurations -- advanced as one unit: one replay of a CUDA graph runs a
+ * launch of steps_per_launch steps (0: 1000) of every member, each member on
+ * its own stream as a concurrent branch of the graph.  The members stay
+ * ordinary simulations (state exchange, line scan, adjoint ...) between batch
+ * calls; their results equal those of running them one by one. */
+typedef struct srs_batch srs_batch;
+int srs_batch_create(srs_sim* const* sims, int n, int steps_per_launch, srs_batch** out);
+void srs_batch_destroy(srs_batch* b);
+/* Every member advances n_steps (the srs_explicit_step loop); enqueued on the
+ * batch's stream and returns. */
+int srs_batch_advance(srs_batch* b, int64_t n_steps);
+int srs_batch_synchronize(srs_batch* b);
+/* srs_batch_advance bracketed by CUDA events; *ms = elapsed device time. */
+int srs_batch_time_advance(srs_batch* b, int64_t n_steps, float* ms);
+/* srs_run_simulation of every member (outs[i] for member i), replaying the
+ * graph until every realization of every member has finished. */
+int srs_batch_run_simulation(srs_batch* b, srs_run_output* outs);
+
 /* ---- total Ca per compartment ---------------------------------------------
  * No reference counterpart (the reference keeps no mass balance).  For every
  * realization, out[2r] / out[2r+1] = sum over the cytosol / JSR elements of

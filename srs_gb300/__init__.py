@@ -188,6 +188,12 @@ _SIGS = {
     "srs_linescan_setup": (C.c_int, [_P, C.POINTER(LinescanDesc), C.POINTER(C.c_int)]),
     "srs_linescan": (C.c_int, [_P, _P, _P]),
     "srs_sim_total_ca": (C.c_int, [_P, _P]),
+    "srs_batch_create": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P)]),
+    "srs_batch_destroy": (None, [_P]),
+    "srs_batch_advance": (C.c_int, [_P, C.c_int64]),
+    "srs_batch_synchronize": (C.c_int, [_P]),
+    "srs_batch_time_advance": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
+    "srs_batch_run_simulation": (C.c_int, [_P, _P]),
     "srs_adjoint_param_index": (C.c_int, [C.c_int]),
     "srs_adjoint": (C.c_int, [_P, C.POINTER(_AdjDesc), C.POINTER(_AdjOut)]),
 }
@@ -448,3 +454,53 @@ class Simulation:
 
     def write_grid_vtk(self, r, path, run=0, rank=0, n=0, t=0.0):
         _check(_lib.srs_write_grid_vtk(self._h, r, str(path).encode(), run, rank, n, float(t)))
+
+
+class Batch:
+    """Several FP32 resident simulations (uneven meshes, protocols and sizes)
+    advanced together by replaying one CUDA graph (srs_batch_*)."""
+
+    def __init__(self, sims, steps_per_launch=0):
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s._h.value for s in self.sims])
+        h = C.c_void_p()
+        _check(_lib.srs_batch_create(arr, len(self.sims), int(steps_per_launch), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.srs_batch_destroy(self._h)
+            self._h = None
+
+    def advance_async(self, n_steps):
+        _check(_lib.srs_batch_advance(self._h, int(n_steps)))
+
+    def synchronize(self):
+        _check(_lib.srs_batch_synchronize(self._h))
+
+    def time_advance(self, n_steps):
+        ms = C.c_float()
+        _check(_lib.srs_batch_time_advance(self._h, int(n_steps), C.byref(ms)))
+        return float(ms.value)
+
+    def run_simulation(self, row_capacity=None):
+        """srs_run_simulation of every member; returns one
+        (rows, t_end, n_steps) tuple per member."""
+        outs = (_RunOutput * len(self.sims))()
+        keep = []
+        for i, sim in enumerate(self.sims):
+            p = sim.params
+            cap = row_capacity or int(p.reals[R["T_FINAL"]] / p.reals[R["OUTPUT_STATES_INTERVAL"]]) + 8
+            w = sim.row_width()
+            rows = np.zeros((sim.R, cap, w), np.float32)
+            n_rows = np.zeros(sim.R, np.int64)
+            t_end = np.zeros(sim.R)
+            n_steps = np.zeros(sim.R, np.int64)
+            outs[i] = _RunOutput(rows.ctypes.data_as(C.POINTER(C.c_float)), cap, w,
+                                 n_rows.ctypes.data_as(C.POINTER(C.c_int64)),
+                                 t_end.ctypes.data_as(C.POINTER(C.c_double)),
+                                 n_steps.ctypes.data_as(C.POINTER(C.c_int64)))
+            keep.append((rows, n_rows, t_end, n_steps))
+        _check(_lib.srs_batch_run_simulation(self._h, outs))
+        return [([rows[r, :n_rows[r]].copy() for r in range(len(n_rows))], t_end, n_steps)
+                for rows, n_rows, t_end, n_steps in keep]

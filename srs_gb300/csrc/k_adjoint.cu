@@ -219,6 +219,13 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
+      // the trajectory of the next step (slot t - 2) into L2 while this one runs
+      if (t >= 2 && tid == 0) {
+        const size_t xn = ((size_t)(t - 2) * a.R + r) * NE + (size_t)rank * Pc;
+        l2_prefetch(a.traj_u + xn, (uint32_t)(Pc * sizeof(float4)));
+        l2_prefetch(a.traj_im + xn, (uint32_t)(Pc * sizeof(float)));
+        l2_prefetch(a.traj_g + xn, (uint32_t)(Pc * sizeof(float)));
+      }
 
       auto element = [&](int i) {
         const float4 x = __ldg(tu + i);

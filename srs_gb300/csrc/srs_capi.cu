@@ -1405,48 +1405,39 @@ int srs_sim_status(srs_sim* s, int* bits) {
   return SRS_OK;
 }
 
-int srs_run_simulation(srs_sim* s, srs_run_output* out) {
-  if (!s || !out || !out->rows || out->row_capacity <= 0) return fail(SRS_ERR_INPUT, "bad output");
-  Schedule sc = make_schedule(s->p);
+}  // extern "C"
+
+namespace {
+
+// RunSimulation set-up: schedule, rows buffer, protocol mode.
+int run_prepare(srs_sim* s, const srs_run_output* out, Schedule* sc, std::vector<int64_t>* before) {
+  if (!out || !out->rows || out->row_capacity <= 0) return fail(SRS_ERR_INPUT, "bad output");
+  *sc = make_schedule(s->p);
   fill_protocol_consts(s);
   if (out->row_width != s->P.row_w)
     return fail(SRS_ERR_INPUT, "row_width must be " + std::to_string(s->P.row_w));
-  SRS_TRY(set_schedule(s, sc));
+  SRS_TRY(set_schedule(s, *sc));
   SRS_TRY(ensure_rows(s, out->row_capacity, s->P.row_w));
   s->P.row_cap = out->row_capacity;
   s->P.run_protocol = 1;
   refresh_args(s);
-  std::vector<int64_t> before = ctl_steps(s);
+  *before = ctl_steps(s);
+  return SRS_OK;
+}
+
+int all_done(srs_sim* s, bool* done) {
   std::vector<RealCtl> ctl(s->R);
-  if (s->d.engine != SRS_ENGINE_RESIDENT) {
-    SRS_TRY(plain_prestep(s, 1));
-    int64_t total = 0;
-    const int64_t chunk = 4096;
-    while (true) {
-      int64_t n = std::min<int64_t>(chunk, sc.n_steps + 1 - total);
-      if (n <= 0) break;
-      // plain_steps assumes buffer 0 at the start: alternate by the global count
-      if (total & 1) return fail(SRS_ERR_STATE, "internal: odd chunk");
-      SRS_TRY(plain_steps(s, n + (n & 1)));
-      total += n + (n & 1);
-      SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
-      bool all = true;
-      for (auto& c : ctl) all &= c.done != 0;
-      if (all) break;
-    }
-  } else {
-    // the first launch writes the t = 0 row and runs the protocol of step 0
-    const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
-    int first = 1;
-    while (true) {
-      SRS_TRY(resident_launch(s, S, first));
-      first = 0;
-      SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
-      bool all = true;
-      for (auto& c : ctl) all &= c.done != 0;
-      if (all) break;
-    }
-  }
+  SRS_CUDA(cudaMemcpyAsync(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost, s->st));
+  SRS_CUDA(cudaStreamSynchronize(s->st));
+  bool all = true;
+  for (auto& c : ctl) all &= c.done != 0;
+  *done = all;
+  return SRS_OK;
+}
+
+// RunSimulation results: rows and per-realization summary to the host.
+int run_finish(srs_sim* s, srs_run_output* out, const std::vector<int64_t>& before) {
+  std::vector<RealCtl> ctl(s->R);
   SRS_CUDA(cudaStreamSynchronize(s->st));
   SRS_TRY(normalize_buffers(s, before));
   SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
@@ -1465,8 +1456,217 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
   refresh_args(s);
   if (st_bits & 1) return fail(SRS_ERR_NONFINITE, "a realization produced a non-finite Ca value");
   if (st_bits & 4) return fail(SRS_ERR_INPUT, "row_capacity too small for the run");
+  if (st_bits & 8) return fail(SRS_ERR_STATE, "internal: termination inside a speculating launch");
   return SRS_OK;
 }
+
+}  // namespace
+
+extern "C" {
+
+int srs_run_simulation(srs_sim* s, srs_run_output* out) {
+  if (!s) return fail(SRS_ERR_INPUT, "bad output");
+  Schedule sc;
+  std::vector<int64_t> before;
+  SRS_TRY(run_prepare(s, out, &sc, &before));
+  bool done = false;
+  if (s->d.engine != SRS_ENGINE_RESIDENT) {
+    SRS_TRY(plain_prestep(s, 1));
+    int64_t total = 0;
+    const int64_t chunk = 4096;
+    while (true) {
+      int64_t n = std::min<int64_t>(chunk, sc.n_steps + 1 - total);
+      if (n <= 0) break;
+      // plain_steps assumes buffer 0 at the start: alternate by the global count
+      if (total & 1) return fail(SRS_ERR_STATE, "internal: odd chunk");
+      SRS_TRY(plain_steps(s, n + (n & 1)));
+      total += n + (n & 1);
+      SRS_TRY(all_done(s, &done));
+      if (done) break;
+    }
+  } else {
+    // the first launch writes the t = 0 row and runs the protocol of step 0
+    const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
+    int first = 1;
+    while (!done) {
+      SRS_TRY(resident_launch(s, S, first));
+      first = 0;
+      SRS_TRY(all_done(s, &done));
+    }
+  }
+  return run_finish(s, out, before);
+}
+
+}  // extern "C"
+
+// ---- multi-mesh batch ----------------------------------------------------------
+struct srs_batch {
+  std::vector<srs_sim*> sims;
+  int S = 1000;  // steps per member launch in one graph replay
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t graph = nullptr;
+  int graph_mode = -1;  // run_protocol the graph was captured with
+  int64_t replays = 0;
+};
+
+namespace {
+
+void batch_drop_graph(srs_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_mode = -1;
+}
+
+// One replay: every member advances S steps on its own stream; the members'
+// launches are branches of one graph forked from and joined into b->st.
+int batch_enqueue(srs_batch* b, int steps, int first) {
+  SRS_CUDA(cudaEventRecord(b->fork, b->st));
+  for (size_t i = 0; i < b->sims.size(); ++i) {
+    srs_sim* s = b->sims[i];
+    SRS_CUDA(cudaStreamWaitEvent(s->st, b->fork, 0));
+    SRS_TRY(resident_launch(s, steps, first));
+    SRS_CUDA(cudaEventRecord(b->join[i], s->st));
+    SRS_CUDA(cudaStreamWaitEvent(b->st, b->join[i], 0));
+  }
+  return SRS_OK;
+}
+
+int batch_graph(srs_batch* b) {
+  const int mode = b->sims[0]->P.run_protocol;
+  if (b->graph && b->graph_mode == mode) return SRS_OK;
+  batch_drop_graph(b);
+  cudaGraph_t g;
+  SRS_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  int rc = batch_enqueue(b, b->S, 0);
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(SRS_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(SRS_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+  for (srs_sim* s : b->sims) s->launches--;  // counted per replay instead
+  b->graph_mode = mode;
+  return SRS_OK;
+}
+
+int batch_replay(srs_batch* b) {
+  SRS_CUDA(cudaGraphLaunch(b->graph, b->st));
+  for (srs_sim* s : b->sims) s->launches++;
+  b->replays++;
+  return SRS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int srs_batch_create(srs_sim* const* sims, int n, int steps_per_launch, srs_batch** out) {
+  if (!sims || n <= 0 || !out) return fail(SRS_ERR_INPUT, "bad argument");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!sims[i]) return fail(SRS_ERR_INPUT, "null simulation");
+    if (sims[i]->d.precision != SRS_FP32 || sims[i]->d.engine != SRS_ENGINE_RESIDENT)
+      return fail(SRS_ERR_UNSUPPORTED, "batch members are FP32 resident simulations");
+    for (int j = 0; j < i; ++j)
+      if (sims[j] == sims[i]) return fail(SRS_ERR_INPUT, "a simulation appears twice in the batch");
+  }
+  srs_batch* b = new srs_batch();
+  b->sims.assign(sims, sims + n);
+  b->S = steps_per_launch > 0 ? steps_per_launch : 1000;
+  b->join.assign(n, nullptr);
+  bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; ok && i < n; ++i)
+    ok = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    srs_batch_destroy(b);
+    return fail(SRS_ERR_CUDA, "batch stream/event creation failed");
+  }
+  *out = b;
+  return SRS_OK;
+}
+
+void srs_batch_destroy(srs_batch* b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  batch_drop_graph(b);
+  for (auto e : b->join)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+int srs_batch_advance(srs_batch* b, int64_t n_steps) {
+  if (!b || n_steps < 0) return fail(SRS_ERR_INPUT, "bad argument");
+  for (srs_sim* s : b->sims)
+    if (s->P.run_protocol) {
+      s->P.run_protocol = 0;
+      refresh_args(s);
+    }
+  if (n_steps >= b->S) SRS_TRY(batch_graph(b));
+  int64_t done = 0;
+  for (; n_steps - done >= b->S; done += b->S) SRS_TRY(batch_replay(b));
+  if (n_steps > done) SRS_TRY(batch_enqueue(b, (int)(n_steps - done), 0));
+  return SRS_OK;
+}
+
+int srs_batch_synchronize(srs_batch* b) {
+  if (!b) return fail(SRS_ERR_INPUT, "null argument");
+  SRS_CUDA(cudaStreamSynchronize(b->st));
+  return SRS_OK;
+}
+
+int srs_batch_time_advance(srs_batch* b, int64_t n_steps, float* ms) {
+  if (!b || !ms) return fail(SRS_ERR_INPUT, "null argument");
+  cudaEvent_t e0, e1;
+  SRS_CUDA(cudaEventCreate(&e0));
+  SRS_CUDA(cudaEventCreate(&e1));
+  for (srs_sim* s : b->sims) SRS_CUDA(cudaStreamSynchronize(s->st));
+  SRS_CUDA(cudaStreamSynchronize(b->st));
+  SRS_CUDA(cudaEventRecord(e0, b->st));
+  int rc = srs_batch_advance(b, n_steps);
+  SRS_CUDA(cudaEventRecord(e1, b->st));
+  SRS_CUDA(cudaEventSynchronize(e1));
+  SRS_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int srs_batch_run_simulation(srs_batch* b, srs_run_output* outs) {
+  if (!b || !outs) return fail(SRS_ERR_INPUT, "null argument");
+  const size_t n = b->sims.size();
+  std::vector<Schedule> sc(n);
+  std::vector<std::vector<int64_t>> before(n);
+  for (size_t i = 0; i < n; ++i) SRS_TRY(run_prepare(b->sims[i], &outs[i], &sc[i], &before[i]));
+  batch_drop_graph(b);  // run-mode arguments (rows, schedule) are captured afresh
+  // the first launch of every member writes its t = 0 row
+  SRS_TRY(batch_enqueue(b, b->S, 1));
+  SRS_TRY(batch_graph(b));
+  while (true) {
+    SRS_CUDA(cudaStreamSynchronize(b->st));
+    bool all = true;
+    for (srs_sim* s : b->sims) {
+      bool d = false;
+      SRS_TRY(all_done(s, &d));
+      all &= d;
+    }
+    if (all) break;
+    SRS_TRY(batch_replay(b));
+  }
+  SRS_CUDA(cudaStreamSynchronize(b->st));
+  batch_drop_graph(b);
+  int rc = SRS_OK;
+  for (size_t i = 0; i < n; ++i) {
+    int r = run_finish(b->sims[i], &outs[i], before[i]);
+    if (r && !rc) rc = r;
+  }
+  return rc;
+}
+
 
 int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
   if (!s || !d || d->res <= 0 || d->r_thresh <= 0) return fail(SRS_ERR_INPUT, "bad line-scan description");

@@ -37,6 +37,12 @@ __device__ __forceinline__ void cluster_arrive_wait() {
                "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// Bulk prefetch of a global range into L2 (address 16-byte aligned, size a
+// multiple of 16 bytes).
+__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Split cluster barrier: arrive (release) and wait (acquire) of one phase.
 // With C == 1 the CTA barrier of the caller orders everything.
 template <int C>

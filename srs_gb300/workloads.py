@@ -34,3 +34,56 @@ def config_mesh(directory):
     base = os.path.join(directory, "dyad12")
     rep = srs.write_box_mesh(base, **CONFIG_DYAD)
     return base, rep
+
+
+# Uneven multi-mesh batch: four box dyads of 6k / 15k / 30k / 60k tets in
+# 1.5 / 2 / 2.5 / 3 um boxes, Poisson-disk RyR clusters (minimum spacing
+# 30 nm) of 10 / 25 / 60 / 100 RyRs, one LCC per 7 RyRs.
+CONFIG2_MESHES = [
+    # box, n_foot, n_out, n_above, n_ryr, cluster radius (um): about a third of
+    # the disc covered by the 15 nm exclusion discs
+    (1.5, 6, 2, 8, 10, 0.085),
+    (2.0, 8, 3, 11, 25, 0.13),
+    (2.5, 9, 4, 15, 60, 0.20),
+    (3.0, 10, 6, 19, 100, 0.26),
+]
+
+
+def config2_mesh_specs():
+    out = []
+    for k, (box, nf, no, na, nr, rad) in enumerate(CONFIG2_MESHES):
+        half = rad + 0.05
+        out.append(dict(box_x=box, box_y=box, box_z=box, foot_half_x=half, foot_half_y=half,
+                        n_foot_x=nf, n_foot_y=nf, n_out_x=no, n_out_y=no, n_above_z=na,
+                        ryr_mode=1, ryr_count=nr, ryr_radius=rad, ryr_pitch=0.030,
+                        n_lcc=max(1, round(nr / 7)),
+                        lcc_half=half, seed=11 + k, lcc_seed=21 + k))
+    return out
+
+
+def config2_meshes(directory):
+    """Writes the four meshes; returns [(base, report)]."""
+    res = []
+    for k, spec in enumerate(config2_mesh_specs()):
+        base = os.path.join(directory, "c2_mesh%d" % k)
+        res.append((base, srs.write_box_mesh(base, **spec)))
+    return res
+
+
+def stable_dt(params, max_a0, dt=9e-6, margin=0.9):
+    """dt, reduced below D_max * dt * max|a0| = margin when that bound needs it."""
+    d = max(params.reals[srs.R[n]] for n in ("D_CA", "D_ATP", "D_CMDN", "D_DYE"))
+    return min(dt, margin / (d * max_a0))
+
+
+def config2_protocols(max_a0):
+    """The two protocols of the batch: leak (voltage clamped at rest, no
+    trigger, no forced RyR, 100 ms) and LCC-triggered (clamped at 0 mV,
+    30 ms, as param/Gain_0mV.xml)."""
+    leak = default_spark_params(INIT_RYR=-1, INIT_RYR_HOLD=0.0, FLAG_V_CLAMP=1, V_CLAMP=-80.0,
+                                T_CLAMP=200.0, T_FINAL=100.0)
+    trig = default_spark_params(INIT_RYR=-1, INIT_RYR_HOLD=0.0, FLAG_V_CLAMP=1, V_CLAMP=0.0,
+                                T_CLAMP=200.0, T_FINAL=30.0)
+    for p in (leak, trig):
+        p.set(T_STEP=stable_dt(p, max_a0))
+    return leak, trig

@@ -166,3 +166,20 @@ def test_capi_exports_every_declared_symbol(srs):
         assert hasattr(lib, n), n
     # and the Python mirror binds each of them
     assert names <= set(srs._SIGS)
+
+
+def test_config2_meshes_have_the_specified_sizes(srs, tmp_path):
+    """Uneven multi-mesh workload: 6k / 15k / 30k / 60k tets, Poisson-disk
+    clusters of 10 / 25 / 60 / 100 RyRs, one LCC per 7 RyRs, all stable at
+    dt = 9 ns."""
+    from srs_gb300 import workloads as wl
+    reps = wl.config2_meshes(str(tmp_path))
+    tets = [r["n_tets"] for _, r in reps]
+    assert tets == [6000, 15288, 29478, 60984]
+    assert [r["n_ryr"] for _, r in reps] == [10, 25, 60, 100]
+    assert [r["n_lcc"] for _, r in reps] == [1, 4, 9, 14]
+    for base, r in reps:
+        leak, trig = wl.config2_protocols(r["max_a0"])
+        assert leak.reals[srs.R["T_STEP"]] == 9e-6 and trig.reals[srs.R["T_STEP"]] == 9e-6
+        g = srs.Grid(leak, base)
+        assert g.n_ele == r["n_tets"]
