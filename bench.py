@@ -438,12 +438,19 @@ def run_ours(args):
                "d2h_bytes_per_step": d2h,
                "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)" % (S, rows_bytes)}
 
+    # secondary legs: a failure is reported in the line, not fatal to it
     adj = None
     if rank == 0 and not args.no_adjoint:
-        adj = adjoint_cost(srs, grid, p, args)
+        try:
+            adj = adjoint_cost(srs, grid, p, args)
+        except Exception as e:  # noqa: BLE001
+            adj = {"error": "%s: %s" % (type(e).__name__, e)}
     c2 = None
     if rank == 0 and not args.no_config2:
-        c2 = config2_batch(srs, args)
+        try:
+            c2 = config2_batch(srs, args)
+        except Exception as e:  # noqa: BLE001
+            c2 = {"error": "%s: %s" % (type(e).__name__, e)}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

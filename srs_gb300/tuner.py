@@ -55,6 +55,11 @@ def tune_resident(grid, params, R, seeds=None, clusters=(1, 2, 3, 4, 5, 6, 8),
             if verbose:
                 print("tuner: C=%d T=%d %.4f ms/step" % (C, T, ms / trial_steps))
             del sim
+    if not trials and 16 not in clusters:
+        # large grids: non-portable 16-CTA clusters
+        return tune_resident(grid, params, R, seeds, clusters=(16,), threads=threads,
+                             trial_steps=trial_steps, repeats=repeats, use_cache=use_cache,
+                             verbose=verbose)
     if not trials:
         raise RuntimeError("no resident configuration fits this grid")
     best = min(trials, key=lambda d: d["ms_per_step"])

@@ -15,7 +15,7 @@ def _members(srs, tmp_path):
     srs.write_box_mesh(tiny, **wl.TINY_DYAD)
     p1, _ = params_from_golden(srs, "spark")
     p2, _ = params_from_golden(srs, "spark_nogating")
-    p3 = wl.default_spark_params(T_FINAL=0.5, OUTPUT_STATES_INTERVAL=0.05)
+    p3 = wl.default_spark_params(T_FINAL=0.5, OUTPUT_STATES_INTERVAL=0.05, INIT_RYR=4)
     return [(GOLDEN_MESH, p1, [1, 2, 3, 4], 2), (GOLDEN_MESH, p2, [5, 6, 7], 1), (tiny, p3, [8, 9], 1)]
 
 
