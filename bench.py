@@ -63,10 +63,16 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-tune", action="store_true", help="use the default configuration")
+    ap.add_argument("--cluster-size", type=int, default=0, help="with --no-tune: this cluster size")
+    ap.add_argument("--threads", type=int, default=0, help="with --no-tune: threads per CTA")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost leg")
     ap.add_argument("--adjoint-realizations", type=int, default=64)
     ap.add_argument("--adjoint-steps", type=int, default=4096)
     ap.add_argument("--no-config2", action="store_true", help="skip the multi-mesh batch leg")
+    ap.add_argument("--only", choices=["adjoint", "config2"], default=None,
+                    help="run one secondary leg alone and print its JSON (profiling)")
+    ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
+                    help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
     ap.add_argument("--config2-steps", type=int, default=4000)
     return ap.parse_args()
 
@@ -279,7 +285,10 @@ def adjoint_cost(srs, grid, p, args):
     import torch
     Ra, n, te = args.adjoint_realizations, args.adjoint_steps, 128
     from srs_gb300 import tuner
-    t = tuner.tune_resident(grid, p, Ra, seeds=list(range(1, Ra + 1)))
+    if args.no_tune:
+        t = dict(cluster_size=args.cluster_size, threads_per_cta=args.threads)
+    else:
+        t = tuner.tune_resident(grid, p, Ra, seeds=list(range(1, Ra + 1)))
     sim = srs.Simulation(grid, p, Ra, srs.FP32, srs.ENGINE_RESIDENT, seeds=list(range(1, Ra + 1)),
                          cluster_size=t["cluster_size"], threads_per_cta=t["threads_per_cta"],
                          steps_per_launch=256)
@@ -301,7 +310,11 @@ def adjoint_cost(srs, grid, p, args):
                        "every %d steps" % (Ra, n, ns, te),
            "cluster_size": sim.config()["cluster_size"], "forward_s": fwd}
     # K = 256: checkpoint + recompute; K = n: the forward pass keeps the trajectory
-    for K, key in ((256, "checkpoint_256"), (n, "whole_trajectory")):
+    modes = ((256, "checkpoint_256"), (n, "whole_trajectory"))
+    if args.adjoint_checkpoint >= 0:
+        K1 = args.adjoint_checkpoint or n
+        modes = ((K1, "checkpoint_%d" % K1),)
+    for K, key in modes:
         sim.reset()
         sim.adjoint(n, te, f0, checkpoint_every=K)  # warm: work buffers of this mode
         sim.reset()
@@ -368,11 +381,17 @@ def run_ours(args):
     base, rep = wl.config_mesh(tmp)
     p = wl.default_spark_params()
     grid = srs.Grid(p, base)
+    if args.only:
+        if rank == 0:
+            leg = adjoint_cost(srs, grid, p, args) if args.only == "adjoint" else config2_batch(srs, args)
+            print(json.dumps(dict(leg, leg=args.only)))
+        return 0
     R, S = args.realizations, args.launch_steps
     seeds = [1 + rank * R + i for i in range(R)]
     from srs_gb300 import tuner
     if args.no_tune:
-        tuned = dict(cluster_size=0, threads_per_cta=0, ms_per_step=None, trials=[])
+        tuned = dict(cluster_size=args.cluster_size, threads_per_cta=args.threads, ms_per_step=None,
+                     trials=[])
     else:
         tuned = tuner.tune_resident(grid, p, R, seeds=seeds)
     sim = srs.Simulation(grid, p, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
