@@ -96,6 +96,11 @@ def dist_init(ws):
     return dist
 
 
+def replica_seeds(rank, R):
+    """Philox keys of rank `rank`'s replica: disjoint across ranks."""
+    return [1 + rank * R + i for i in range(R)]
+
+
 def barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -387,7 +392,7 @@ def run_ours(args):
             print(json.dumps(dict(leg, leg=args.only)))
         return 0
     R, S = args.realizations, args.launch_steps
-    seeds = [1 + rank * R + i for i in range(R)]
+    seeds = replica_seeds(rank, R)
     from srs_gb300 import tuner
     if args.no_tune:
         tuned = dict(cluster_size=args.cluster_size, threads_per_cta=args.threads, ms_per_step=None,
