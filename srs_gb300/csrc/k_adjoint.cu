@@ -27,6 +27,8 @@
 // are added in FP64 to the per-realization gradient, which therefore
 // accumulates over all steps and segments (the long reverse sweep) in double
 // precision.
+#include <type_traits>
+
 #include "srs_cluster.cuh"
 #include "srs_engine.h"
 
@@ -227,7 +229,13 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         l2_prefetch(a.traj_g + xn, (uint32_t)(Pc * sizeof(float)));
       }
 
-      auto element = [&](int i) {
+      // OWN: the owner state of lambda is in shared memory (else global)
+      auto element = [&](int i, auto own) {
+        constexpr bool OWN = decltype(own)::value;
+        float* lc = OWN ? sm_lc : a.lam_c + roff;
+        float* lim = OWN ? sm_lim : a.lam_im + roff;
+        float* cim = OWN ? sm_cim : a.lam_cim + roff;
+        float4* c4 = OWN ? sm_c4 : a.lam_c4 + roff;
         const float4 x = __ldg(tu + i);
         const float xim = __ldg(tim + i);
         const float G = __ldg(tg + i);
@@ -274,14 +282,12 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         Sy = fmaf(at.z, n2.w, Sy);
         Sy = fmaf(at.w, n3.w, Sy);
         Sy = fmaf(-sa, me.w, Sy);
-        float g[NA];
-#pragma unroll
-        for (int p = 0; p < NA; ++p) g[p] = 0.0f;
+        float* g = gstep;  // this element's terms go straight into the thread's sums
         // D gradients: sum_j lambda_j (L u)_j = sum_j u_j (L^T lambda)_j
-        g[SRS_ADJ_D_CA] = x.x * Sc;
-        g[SRS_ADJ_D_ATP] = x.y * Sa;
-        g[SRS_ADJ_D_CMDN] = x.z * Sm;
-        g[SRS_ADJ_D_DYE] = x.w * Sy;
+        g[SRS_ADJ_D_CA] = fmaf(x.x, Sc, g[SRS_ADJ_D_CA]);
+        g[SRS_ADJ_D_ATP] = fmaf(x.y, Sa, g[SRS_ADJ_D_ATP]);
+        g[SRS_ADJ_D_CMDN] = fmaf(x.z, Sm, g[SRS_ADJ_D_CMDN]);
+        g[SRS_ADJ_D_DYE] = fmaf(x.w, Sy, g[SRS_ADJ_D_DYE]);
         float oc = k.D[0] * Sc, oa = k.D[1] * Sa, om = k.D[2] * Sm, oy = k.D[3] * Sy, oi = 0.0f;
         const float w = me.x;
         const float li = lim[i];
@@ -305,7 +311,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
             const float dden = fmaf(2.0f * Ki, k.sd2, k.sd1);
             const float dv = (dnum - v * dden) * iden * (2.0f * c * k.inv_kdi * k.inv_kdi);
             dG = fmaf(-k.serca_scale, dv, dG);
-            g[SRS_ADJ_A_P] = -w * ak.serca_per_ap * v;
+            g[SRS_ADJ_A_P] -= w * ak.serca_per_ap * v;
           }
         } else {
           adj_buffer(k, ak, 4, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_CSQN);
@@ -344,8 +350,8 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           const float GB = G / (1.0f + bk2);           // G / B
           const float t3 = GB * bk2 * ikc;             // G bsl / (B kc^3)
           oc = fmaf(2.0f * t3, w, oc);
-          g[SRS_ADJ_B_TOT_SL] = -w * GB * bk2 * ak.inv_btot_sl;
-          g[SRS_ADJ_K_D_SL] = -w * t3 * (c - k.khi) * ak.inv_khi;
+          g[SRS_ADJ_B_TOT_SL] -= w * GB * bk2 * ak.inv_btot_sl;
+          g[SRS_ADJ_K_D_SL] -= w * t3 * (c - k.khi) * ak.inv_khi;
         }
         // compensated update of lambda
         float4 L = make_float4(lc[i], me.y, me.z, me.w);
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         kadd(L.w, cm.w, k.dt * oy);
         kadd(lnew, ci, k.dt * oi);
         if (t > 1) {
-          const float cprev = (jsr ? k.c0j : k.c0) + a.traj_u[xprev + i].x;
+          const float cprev = (jsr ? k.c0j : k.c0) + __ldg(a.traj_u + xprev + i).x;
           const float inj = tick_injection(a, coef_next, (int)(rank * Pc + i));
           nxt[i] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
           lc[i] = L.x;
@@ -371,22 +377,26 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           a.lam_c4[roff + i] = cm;
           a.lam_cim[roff + i] = ci;
         }
-#pragma unroll
-        for (int p = 0; p < NA; ++p) gstep[p] += g[p];
       };
+      auto element_s = [&](int i) { element(i, std::true_type{}); };
+      auto element_g = [&](int i) { element(i, std::false_type{}); };
       // interior elements (and the channel elements when they are interior):
       // interior to their forward partition, hence to this CTA
-      int idx = tid;
-      for (int j = 0; j < msub; ++j) {
-        const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-        for_range(idx, j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
-      }
-      cl_wait<C>();
-      for (int j = 0; j < msub; ++j) {
-        const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-        if (!a.ch_interior) for_range(idx, j * P, j * P + nc, element);
-        for_range(idx, j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
-      }
+      auto sweep = [&](auto&& element) {
+        int idx = tid;
+        for (int j = 0; j < msub; ++j) {
+          const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
+          for_range(idx, j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
+        }
+        cl_wait<C>();
+        for (int j = 0; j < msub; ++j) {
+          const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
+          if (!a.ch_interior) for_range(idx, j * P, j * P + nc, element);
+          for_range(idx, j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
+        }
+      };
+      if (a.own_in_smem) sweep(element_s);
+      else sweep(element_g);
       __syncthreads();
       cl_arrive<C>();
       // every 16 steps (and at the end) the warp's FP32 sums go into its FP64
