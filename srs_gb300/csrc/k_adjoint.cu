@@ -216,8 +216,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       const uint32_t* bs = s_base + 16 * cur;
       const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * Pc;
       const float4* __restrict__ tu = a.traj_u + xoff;
-      const float* __restrict__ tim = a.traj_im + xoff;
-      const float* __restrict__ tg = a.traj_g + xoff;
+      const float2* __restrict__ tig = a.traj_ig + xoff;
       const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
@@ -225,8 +224,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       if (t >= 2 && tid == 0) {
         const size_t xn = ((size_t)(t - 2) * a.R + r) * NE + (size_t)rank * Pc;
         l2_prefetch(a.traj_u + xn, (uint32_t)(Pc * sizeof(float4)));
-        l2_prefetch(a.traj_im + xn, (uint32_t)(Pc * sizeof(float)));
-        l2_prefetch(a.traj_g + xn, (uint32_t)(Pc * sizeof(float)));
+        l2_prefetch(a.traj_ig + xn, (uint32_t)(Pc * sizeof(float2)));
       }
 
       // OWN: the owner state of lambda is in shared memory (else global)
@@ -236,9 +234,15 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         float* lim = OWN ? sm_lim : a.lam_im + roff;
         float* cim = OWN ? sm_cim : a.lam_cim + roff;
         float4* c4 = OWN ? sm_c4 : a.lam_c4 + roff;
+        if (i + nthr < Pc) {  // the element this thread takes next, into L1
+          l1_prefetch(tu + i + nthr);
+          l1_prefetch(tig + i + nthr);
+          l1_prefetch(geo + i + nthr);
+          l1_prefetch(aT + i + nthr);
+        }
         const float4 x = __ldg(tu + i);
-        const float xim = __ldg(tim + i);
-        const float G = __ldg(tg + i);
+        const float2 ig = __ldg(tig + i);
+        const float xim = ig.x, G = ig.y;
         const float4* gp = reinterpret_cast<const float4*>(geo + i);
         const float4 ga = __ldg(gp);
         const float4 gb = __ldg(gp + 1);

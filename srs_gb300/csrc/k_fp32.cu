@@ -554,10 +554,10 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
               const size_t o = ((size_t)s * a.R + r) * ((size_t)C * P) + (size_t)rank * P + i;
               float g;
               a.traj_u[o] = src[i];
-              a.traj_im[o] = immb[i];
-              tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
+              const float im0 = immb[i];
+              tet_update(k, src[i], im0, n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
                          &out, &imo, &g);
-              a.traj_g[o] = g;
+              a.traj_ig[o] = make_float2(im0, g);
             } else {
               tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
                          &out, &imo);
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         if constexpr (TRAJ) {
           const size_t o = ((size_t)a.steps * a.R + r) * ((size_t)C * P) + (size_t)rank * P + i;
           a.traj_u[o] = fin[i];
-          a.traj_im[o] = immb[i];
+          a.traj_ig[o] = make_float2(immb[i], 0.0f);
         }
       }
       if (rank == 0) {

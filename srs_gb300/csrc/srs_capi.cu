@@ -2001,7 +2001,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   // memory: checkpoints (nseg + 1), one segment of trajectory, lambda
   const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
                         (size_t)R * sizeof(RealCtl);
-  const size_t traj_b = (size_t)(K + 1) * R * NE * 20 + (size_t)K * R * NE * 4 + (size_t)K * R * W * 4;
+  const size_t traj_b = (size_t)(K + 1) * R * NE * 24 + (size_t)K * R * W * 4;
   const size_t need = snap_b * (size_t)(nseg + 1) + traj_b + (size_t)R * NE * 44 +
                       (size_t)(K / te + 2) * R * ns * 8 + (size_t)R * n_ticks * ns * 8;
   size_t free_b = 0, total_b = 0, held = 0;
@@ -2016,11 +2016,10 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   std::vector<StateSnap> ck(nseg + 1);
   for (auto& c : ck) SRS_TRY(snap_alloc(s, sc, &c));
   float4* traj_u;
-  float *traj_im, *traj_g;
+  float2* traj_ig;
   int32_t* traj_ch;
   SRS_TRY(sc.get(&traj_u, (size_t)(K + 1) * R * NE));
-  SRS_TRY(sc.get(&traj_im, (size_t)(K + 1) * R * NE));
-  SRS_TRY(sc.get(&traj_g, (size_t)K * R * NE));
+  SRS_TRY(sc.get(&traj_ig, (size_t)(K + 1) * R * NE));
   SRS_TRY(sc.get(&traj_ch, (size_t)K * R * W));
   float4 *lam, *lam_c4;
   float *lam_im, *lam_cim;
@@ -2057,8 +2056,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     ra.initial_row = 0;
     ra.speculate = 1;
     ra.traj_u = traj_u;
-    ra.traj_im = traj_im;
-    ra.traj_g = traj_g;
+    ra.traj_ig = traj_ig;
     ra.traj_ch = traj_ch;
     if (launch_resident(ra, s->C, s->n_clusters, s->threads, s->smem, s->st))
       return fail(SRS_ERR_CUDA, std::string("trajectory launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -2108,8 +2106,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   aa.NR = NR;
   aa.NL = NL;
   aa.traj_u = traj_u;
-  aa.traj_im = traj_im;
-  aa.traj_g = traj_g;
+  aa.traj_ig = traj_ig;
   aa.traj_ch = traj_ch;
   aa.tick_every = te;
   aa.n_samples = ns;

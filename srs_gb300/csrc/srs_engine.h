@@ -117,13 +117,12 @@ struct ResidentArgs {
   Channels C;
   ChanState CS;
   // Trajectory recording (null: off).  Step s of the launch stores the state
-  // it starts from (traj_u/traj_im slot s), its Ca rate before the rapid-buffer
-  // factor (traj_g slot s) and the channel states it uses (traj_ch slot s:
-  // RyR[NR], LCC[NL], LCC V-gate[NL], voltage selector); slot `steps` of
-  // traj_u/traj_im holds the final state.  Layout [slot][R][C*P].
+  // it starts from (traj_u slot s and traj_ig.x), its Ca rate before the
+  // rapid-buffer factor (traj_ig.y) and the channel states it uses (traj_ch
+  // slot s: RyR[NR], LCC[NL], LCC V-gate[NL], voltage selector); slot
+  // `steps` of traj_u/traj_ig holds the final state.  Layout [slot][R][C*P].
   float4* traj_u;
-  float* traj_im;
-  float* traj_g;
+  float2* traj_ig;
   int32_t* traj_ch;
 };
 // Line scan: F[r][i] = pad[i] + sum_q w[q] * dye(col[q]) over ptr[i]..ptr[i+1].
@@ -191,8 +190,7 @@ struct AdjArgs {
   const float* ryr_s_js;  // -1/V0 of each RyR's JSR element
   int32_t NR, NL;
   const float4* traj_u;    // trajectory of the segment (ResidentArgs layout)
-  const float* traj_im;
-  const float* traj_g;
+  const float2* traj_ig;  // (immobile buffer, Ca rate before the rapid-buffer factor)
   const int32_t* traj_ch;
   int32_t tick_every;      // loss ticks at global steps that are multiples
   int32_t n_samples;
