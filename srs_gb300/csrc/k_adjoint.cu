@@ -234,12 +234,6 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         float* lim = OWN ? sm_lim : a.lam_im + roff;
         float* cim = OWN ? sm_cim : a.lam_cim + roff;
         float4* c4 = OWN ? sm_c4 : a.lam_c4 + roff;
-        if (i + nthr < Pc) {  // the element this thread takes next, into L1
-          l1_prefetch(tu + i + nthr);
-          l1_prefetch(tig + i + nthr);
-          l1_prefetch(geo + i + nthr);
-          l1_prefetch(aT + i + nthr);
-        }
         const float4 x = __ldg(tu + i);
         const float2 ig = __ldg(tig + i);
         const float xim = ig.x, G = ig.y;

@@ -43,11 +43,6 @@ __device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Prefetch of the cache line holding p into L1.
-__device__ __forceinline__ void l1_prefetch(const void* p) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
 // Split cluster barrier: arrive (release) and wait (acquire) of one phase.
 // With C == 1 the CTA barrier of the caller orders everything.
 template <int C>
