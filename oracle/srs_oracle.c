@@ -1192,8 +1192,8 @@ static void fp32_element(const or_k32* k, const float* o, float im, const float*
   }
   rca += flux;
   if (bsl != 0.0f) {
-    float kc = k->khi + c;
-    rca = rca / fmaf(bsl, 1.0f / (kc * kc), 1.0f);
+    float kc = k->khi + c, kc2 = kc * kc;
+    rca = (rca * kc2) / (kc2 + bsl);
   }
   /* compensated (Kahan) Euler update: y = dt*r - comp; t = u + y;
    * comp = (t - u) - y */

@@ -96,9 +96,10 @@ __device__ __forceinline__ void tet_update(const Consts32& k, float4 o, float im
   }
   rca += flux;
   if (g_out) *g_out = rca;  // Ca rate before the rapid-buffer factor
-  if (bsl != 0.0f) {  // rapid SL buffer (cpu/RunSimulation.cpp:15-22)
-    float kc = k.khi + c;
-    rca = rca / fmaf(bsl, 1.0f / (kc * kc), 1.0f);
+  if (bsl != 0.0f) {  // rapid SL buffer (cpu/RunSimulation.cpp:15-22): r / (1 + bsl / kc^2)
+    const float kc = k.khi + c;
+    const float kc2 = kc * kc;
+    rca = (rca * kc2) / (kc2 + bsl);
   }
   // compensated Euler: y = dt*r - comp; t = u + y; comp = (t - u) - y
   float y, t;
