@@ -466,8 +466,10 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
     // Speculation is safe when no termination can be decided inside this
     // launch: without the protocol nothing terminates, and without the
     // fidelity criterion a run ends exactly at step n_steps.
+    // (every CTA reads the step count from global memory: only partition 0
+    // keeps the control block in shared memory)
     const bool spec = a.speculate && (!P_.run_protocol ||
-                                      (!P_.flag_fidelity && tail->ctl.step + a.steps <= P_.n_steps));
+                                      (!P_.flag_fidelity && a.CS.ctl[r].step + a.steps <= P_.n_steps));
     if (!skip) {
       // Barrier phases: the arrive that ends step s is waited on at the top of
       // step s + 1 -- after the step's interior elements when speculating
