@@ -332,6 +332,19 @@ def adjoint_cost(srs, grid, p, args):
     return out
 
 
+def plain_one_realization(srs, grid, p, n=4000):
+    """The plain form the batched engine is measured against: one realization,
+    one fused step kernel per time step (graph-replayed), FP32 and FP64."""
+    out = {}
+    for name, prec in (("fp32", srs.FP32), ("fp64", srs.FP64)):
+        sim = srs.Simulation(grid, p, 1, prec, srs.ENGINE_PLAIN, seeds=[1])
+        sim.reset()
+        sim.time_advance(256)
+        ms = sim.time_advance(n)
+        out[name] = {"value": n * DT_MS / (ms / 1e3), "unit": UNIT, "us_per_step": 1e3 * ms / n}
+    return out
+
+
 def config2_batch(srs, args):
     """Uneven multi-mesh batch: four box dyads (6k / 15k / 30k / 60k tets,
     Poisson-disk clusters of 10 / 25 / 60 / 100 RyRs, one LCC per 7 RyRs) x
@@ -469,6 +482,13 @@ def run_ours(args):
             adj = adjoint_cost(srs, grid, p, args)
         except Exception as e:  # noqa: BLE001
             adj = {"error": "%s: %s" % (type(e).__name__, e)}
+    plain1 = None
+    if rank == 0:
+        try:
+            plain1 = plain_one_realization(srs, grid, p)
+            plain1["batched_over_plain_fp32"] = value / ws / plain1["fp32"]["value"]
+        except Exception as e:  # noqa: BLE001
+            plain1 = {"error": "%s: %s" % (type(e).__name__, e)}
     c2 = None
     if rank == 0 and not args.no_config2:
         try:
@@ -502,6 +522,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "adjoint": adj,
+            "plain_one_realization": plain1,
             "config2": c2,
         }
         print(json.dumps(line))

@@ -157,20 +157,26 @@ def test_fp32_resident_bit_exact_with_plain(srs, cluster):
             assert np.array_equal(a[k], b[k]), (cluster, r, k)
 
 
-def test_fp32_resident_run_simulation_matches_plain(srs):
-    p = golden_params(srs, "fidelity")
+@pytest.mark.parametrize("proto,cluster,launch", [("fidelity", 2, 500), ("spark", 3, 700),
+                                                  ("lcc_trigger", 2, 333)])
+def test_fp32_resident_run_simulation_matches_plain(srs, proto, cluster, launch):
+    """Rows and final states, with the run ending inside a later launch (the
+    launches before it speculate; the fidelity run never does)."""
+    p = golden_params(srs, proto)
     g = srs.Grid(p, GOLDEN_MESH)
     seeds = [41, 42, 43]
     pl = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
     rs = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
-                        cluster_size=2, steps_per_launch=500)
+                        cluster_size=cluster, steps_per_launch=launch)
     ra, ta, na = pl.run_simulation()
     rb, tb, nb = rs.run_simulation()
     for r in range(len(seeds)):
         assert ra[r].shape == rb[r].shape
         assert np.array_equal(ra[r], rb[r])
         assert ta[r] == tb[r] and na[r] == nb[r]
-        assert np.array_equal(pl.get_state(r)["states"], rs.get_state(r)["states"])
+        a, b = pl.get_state(r), rs.get_state(r)
+        for k in ("states", "ryr", "lcc", "lccv", "residuals"):
+            assert np.array_equal(a[k], b[k]), (proto, r, k)
 
 
 def test_resident_on_config_mesh_matches_plain(srs, box_mesh):
