@@ -39,6 +39,10 @@ def _units():
     return [
         ("k_plain64.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_plain64.cu")]),
         ("k_fp32.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_fp32.cu")]),
+        ("k_res_a.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_res_a.cu")]),
+        ("k_res_b.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_res_b.cu")]),
+        ("k_res_c.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_res_c.cu")]),
+        ("k_res_d.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_res_d.cu")]),
         ("srs_capi.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "srs_capi.cu")]),
         ("k_noalloc.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_noalloc.cu")]),
         ("k_linescan.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_linescan.cu")]),

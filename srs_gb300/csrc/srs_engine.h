@@ -236,6 +236,20 @@ void lcc_flux_consts(const srs_params& p, double V, double* A, double* E, double
                      double* Vg);
 
 size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries);
+// per cluster size (k_res_*.cu)
+#define SRS_RESIDENT_DECLARE(CC)                                                            \
+  int launch_resident_c##CC(const ResidentArgs& a, int n_clusters, int threads, size_t smem, \
+                            cudaStream_t st);                                              \
+  int resident_max_clusters_c##CC(int threads, size_t smem);
+SRS_RESIDENT_DECLARE(1)
+SRS_RESIDENT_DECLARE(2)
+SRS_RESIDENT_DECLARE(3)
+SRS_RESIDENT_DECLARE(4)
+SRS_RESIDENT_DECLARE(5)
+SRS_RESIDENT_DECLARE(6)
+SRS_RESIDENT_DECLARE(8)
+SRS_RESIDENT_DECLARE(16)
+#undef SRS_RESIDENT_DECLARE
 int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
                     cudaStream_t st);
 int resident_max_clusters(int C, int threads, size_t smem);
