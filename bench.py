@@ -74,6 +74,9 @@ def parse():
     ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
     ap.add_argument("--config2-steps", type=int, default=4000)
+    ap.add_argument("--adjoint-threads", type=int, default=0, help="reverse-sweep threads per CTA")
+    ap.add_argument("--adjoint-partitions", type=int, default=0,
+                    help="forward partitions per reverse-sweep CTA")
     return ap.parse_args()
 
 
@@ -321,10 +324,12 @@ def adjoint_cost(srs, grid, p, args):
         modes = ((K1, "checkpoint_%d" % K1),)
     for K, key in modes:
         sim.reset()
-        sim.adjoint(n, te, f0, checkpoint_every=K)  # warm: work buffers of this mode
+        kw = dict(checkpoint_every=K, threads_per_cta=args.adjoint_threads,
+                  cta_partitions=args.adjoint_partitions)
+        sim.adjoint(n, te, f0, **kw)  # warm: work buffers of this mode
         sim.reset()
         t0 = time.perf_counter()
-        loss, grad, _ = sim.adjoint(n, te, f0, checkpoint_every=K)
+        loss, grad, _ = sim.adjoint(n, te, f0, **kw)
         adj = time.perf_counter() - t0
         if not np.isfinite(grad).all():
             raise SystemExit("non-finite adjoint gradient")

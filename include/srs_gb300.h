@@ -281,6 +281,9 @@ typedef struct srs_adjoint_desc {
   const double* f0;      /* [n_samples] reference fluorescence F0 */
   const double* target;  /* [R][n_steps/tick_every][n_samples], or NULL (zero) */
   int flags;
+  int threads_per_cta;   /* reverse-sweep kernel: 256 or 512 (0: chosen by the library) */
+  int cta_partitions;    /* forward partitions per reverse-sweep CTA, a divisor of the
+                            cluster size (0: chosen by the library) */
 } srs_adjoint_desc;
 typedef struct srs_adjoint_out {
   double* loss;        /* [R] */

@@ -133,7 +133,8 @@ ADJ_LAMBDA_GLOBAL = 1
 
 class _AdjDesc(C.Structure):
     _fields_ = [("n_steps", C.c_int64), ("tick_every", C.c_int), ("checkpoint_every", C.c_int),
-                ("f0", C.c_void_p), ("target", C.c_void_p), ("flags", C.c_int)]
+                ("f0", C.c_void_p), ("target", C.c_void_p), ("flags", C.c_int),
+                ("threads_per_cta", C.c_int), ("cta_partitions", C.c_int)]
 
 
 class _AdjOut(C.Structure):
@@ -430,7 +431,7 @@ class Simulation:
         return out
 
     def adjoint(self, n_steps, tick_every, f0, target=None, checkpoint_every=0, grad_state=False,
-                flags=0):
+                flags=0, threads_per_cta=0, cta_partitions=0):
         """srs_adjoint: pathwise gradient of the line-scan dF/F0 loss.
 
         Returns (loss[R], grad[R][N_ADJ] in ADJ_PARAMS order, and
@@ -447,7 +448,8 @@ class Simulation:
         grad = np.zeros((self.R, N_ADJ))
         gs = np.zeros((self.R, 6, self.grid.n_ele)) if grad_state else None
         d = _AdjDesc(int(n_steps), int(tick_every), int(checkpoint_every), f0.ctypes.data,
-                     tg.ctypes.data if tg is not None else None, int(flags))
+                     tg.ctypes.data if tg is not None else None, int(flags), int(threads_per_cta),
+                     int(cta_partitions))
         o = _AdjOut(loss.ctypes.data, grad.ctypes.data, gs.ctypes.data if gs is not None else None)
         _check(_lib.srs_adjoint(self._h, C.byref(d), C.byref(o)))
         return loss, grad, gs

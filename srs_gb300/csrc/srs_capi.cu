@@ -2132,7 +2132,11 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     aa.ak.inv_khi = (float)(1.0 / s->p.reals[R_K_D_SL_HI]);
   }
   const int n_ent = 2 * NR + NL;
-  const int adj_threads = 512;
+  if (d->threads_per_cta != 0 && d->threads_per_cta != 256 && d->threads_per_cta != 512)
+    return fail(SRS_ERR_INPUT, "threads_per_cta must be 256 or 512");
+  if (d->cta_partitions < 0 || (d->cta_partitions > 0 && s->C % d->cta_partitions))
+    return fail(SRS_ERR_INPUT, "cta_partitions must divide the cluster size");
+  const int adj_threads = d->threads_per_cta ? d->threads_per_cta : 512;
   // CTA grouping: m forward partitions per CTA (clusters of C/m CTAs), the
   // owner state of lambda on chip when it fits next to the published slots.
   // Chosen by the estimated time: rounds of clusters x slots per thread.
@@ -2141,7 +2145,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   bool best_own = false;
   double best_cost = 1e300;
   for (int m = 1; m <= s->C; ++m) {
-    if (s->C % m) continue;
+    if (s->C % m || (d->cta_partitions && m != d->cta_partitions)) continue;
     const int Ca = s->C / m, Pc = m * s->P_stride;
     int bits = 1, rbits = 0;
     while ((1 << bits) < Pc) ++bits;
