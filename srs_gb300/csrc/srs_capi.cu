@@ -2136,38 +2136,43 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     return fail(SRS_ERR_INPUT, "threads_per_cta must be 256 or 512");
   if (d->cta_partitions < 0 || (d->cta_partitions > 0 && s->C % d->cta_partitions))
     return fail(SRS_ERR_INPUT, "cta_partitions must divide the cluster size");
-  const int adj_threads = d->threads_per_cta ? d->threads_per_cta : 512;
   // CTA grouping: m forward partitions per CTA (clusters of C/m CTAs), the
-  // owner state of lambda on chip when it fits next to the published slots.
-  // Chosen by the estimated time: rounds of clusters x slots per thread.
-  int best_m = 0, best_C = 0, adj_ncl = 0, best_bits = 0;
+  // owner state of lambda on chip when it fits next to the published slots,
+  // 256 or 512 threads.  Chosen by the estimated time, rounds of clusters x
+  // slots per thread; at equal estimate the 256-thread CTA wins (two CTAs per
+  // SM overlap each other's barrier waits).
+  int best_m = 0, best_C = 0, adj_ncl = 0, best_bits = 0, adj_threads = 0;
   size_t adj_smem = 0;
   bool best_own = false;
   double best_cost = 1e300;
-  for (int m = 1; m <= s->C; ++m) {
-    if (s->C % m || (d->cta_partitions && m != d->cta_partitions)) continue;
-    const int Ca = s->C / m, Pc = m * s->P_stride;
-    int bits = 1, rbits = 0;
-    while ((1 << bits) < Pc) ++bits;
-    while ((1 << rbits) < Ca) ++rbits;
-    if (bits + rbits > 16) continue;
-    for (int own = 1; own >= 0; --own) {
-      if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
-      const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0);
-      const int ncl = std::min(adjoint_max_clusters(Ca, adj_threads, sm), R);
-      if (ncl <= 0) continue;
-      const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / adj_threads) *
-                          (own ? 1.0 : 1.15);
-      if (cost < best_cost) {
-        best_cost = cost;
-        best_m = m;
-        best_C = Ca;
-        adj_ncl = ncl;
-        adj_smem = sm;
-        best_own = own != 0;
-        best_bits = bits;
+  for (int thr : {256, 512}) {
+    if (d->threads_per_cta && thr != d->threads_per_cta) continue;
+    for (int m = 1; m <= s->C; ++m) {
+      if (s->C % m || (d->cta_partitions && m != d->cta_partitions)) continue;
+      const int Ca = s->C / m, Pc = m * s->P_stride;
+      int bits = 1, rbits = 0;
+      while ((1 << bits) < Pc) ++bits;
+      while ((1 << rbits) < Ca) ++rbits;
+      if (bits + rbits > 16) continue;
+      for (int own = 1; own >= 0; --own) {
+        if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
+        const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0);
+        const int ncl = std::min(adjoint_max_clusters(Ca, thr, sm), R);
+        if (ncl <= 0) continue;
+        const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / thr) *
+                            (own ? 1.0 : 1.15) * (thr == 512 ? 1.02 : 1.0);
+        if (cost < best_cost) {
+          best_cost = cost;
+          best_m = m;
+          best_C = Ca;
+          adj_ncl = ncl;
+          adj_smem = sm;
+          best_own = own != 0;
+          best_bits = bits;
+          adj_threads = thr;
+        }
+        break;  // the on-chip variant when it fits
       }
-      break;  // the on-chip variant when it fits
     }
   }
   if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
