@@ -75,6 +75,7 @@ def parse():
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
     ap.add_argument("--config2-steps", type=int, default=4000)
     ap.add_argument("--adjoint-threads", type=int, default=0, help="reverse-sweep threads per CTA")
+    ap.add_argument("--adjoint-flags", type=int, default=0, help="srs_adjoint_desc flags")
     ap.add_argument("--adjoint-partitions", type=int, default=0,
                     help="forward partitions per reverse-sweep CTA")
     return ap.parse_args()
@@ -325,7 +326,7 @@ def adjoint_cost(srs, grid, p, args):
     for K, key in modes:
         sim.reset()
         kw = dict(checkpoint_every=K, threads_per_cta=args.adjoint_threads,
-                  cta_partitions=args.adjoint_partitions)
+                  cta_partitions=args.adjoint_partitions, flags=args.adjoint_flags)
         sim.adjoint(n, te, f0, **kw)  # warm: work buffers of this mode
         sim.reset()
         t0 = time.perf_counter()

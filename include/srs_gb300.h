@@ -274,6 +274,9 @@ enum {
 /* flags: SRS_ADJ_LAMBDA_GLOBAL keeps the adjoint state in global memory even
  * where it fits on chip (the path taken for partitions too large for it). */
 #define SRS_ADJ_LAMBDA_GLOBAL 1
+/* SRS_ADJ_NO_STAGE reads the recorded trajectory straight from global memory
+ * instead of staging each step's slice in shared memory by bulk copies. */
+#define SRS_ADJ_NO_STAGE 2
 typedef struct srs_adjoint_desc {
   int64_t n_steps;
   int tick_every;

@@ -129,6 +129,7 @@ NOALLOC_MAX_REALIZATIONS = 256
 
 
 ADJ_LAMBDA_GLOBAL = 1
+ADJ_NO_STAGE = 2
 
 
 class _AdjDesc(C.Structure):

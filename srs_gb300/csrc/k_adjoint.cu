@@ -65,8 +65,10 @@ __device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& a
 
 // Shared memory: float4 pub[2][P]; double red[32][NA]; int32 cptr[n_ch+1];
 // ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16]; then, when
-// `own_in_smem`, the owner state float4 c4[P], float lc[P], lim[P], cim[P].
-size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem) {
+// `own_in_smem`, the owner state float4 c4[P], float lc[P], lim[P], cim[P];
+// then, when `stage`, three trajectory buffers float4 u[3][P], float2
+// ig[3][P] and their mbarriers uint64 bar[3].
+size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, bool stage) {
   // P: element slots of one CTA
   size_t b = (size_t)2 * P * sizeof(float4);
   b += (size_t)32 * NA * sizeof(double);
@@ -75,6 +77,7 @@ size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem) {
   b += (size_t)n_entries * sizeof(ChanEntry32);
   b += 2 * 16 * sizeof(uint32_t);
   if (own_in_smem) b += (size_t)P * (3 * sizeof(float) + sizeof(float4));
+  if (stage) b += (size_t)3 * P * (sizeof(float4) + sizeof(float2)) + 3 * sizeof(uint64_t);
   return b;
 }
 
@@ -132,6 +135,11 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   float* sm_lc = reinterpret_cast<float*>(sm_c4 + Pc);
   float* sm_lim = sm_lc + Pc;
   float* sm_cim = sm_lim + Pc;
+  // trajectory staging (a.stage): slot k of the segment in buffer k % 3
+  float4* st_u = reinterpret_cast<float4*>(a.own_in_smem ? reinterpret_cast<unsigned char*>(sm_cim + Pc)
+                                                         : reinterpret_cast<unsigned char*>(s_base + 32));
+  float2* st_ig = reinterpret_cast<float2*>(st_u + 3 * Pc);
+  uint64_t* st_bar = reinterpret_cast<uint64_t*>(st_ig + 3 * Pc);
 
   uint32_t rank = 0;
   if constexpr (C > 1) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
@@ -164,11 +172,41 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     for (int i = tid; i <= n_ch; i += nthr) s_cptr[i] = a.ch_ptr[i];
     for (int i = tid; i < n_ent; i += nthr) s_clist[i] = a.ch_list[i];
   }
+  if (a.stage && tid == 0) {
+    for (int b = 0; b < 3; ++b) mbar_init(&st_bar[b], 1);
+    fence_proxy_async();
+  }
   if (tid < C) {
     s_base[tid] = (C > 1) ? map_rank(smem_addr(pub0), tid) : smem_addr(pub0);
     s_base[16 + tid] = (C > 1) ? map_rank(smem_addr(pub1), tid) : smem_addr(pub1);
   }
   step_barrier<C>();
+
+  // Staging: thread 0 copies slot k of the trajectory (this CTA's slice) into
+  // buffer k % 3 with two bulk copies completing on that buffer's mbarrier;
+  // every thread waits on the mbarrier's phase before reading.  A buffer
+  // receives a new slot only after the __syncthreads that ends the last step
+  // reading its old one.  Uses of each buffer are counted so that all
+  // threads know the phase parity of every wait.
+  uint32_t use_par = 0;  // bit b: parity of the uses of buffer b so far
+  uint32_t stall = 0;  // a wait that gave up (reported in the status word)
+  auto slot_off = [&](int kslot, int r) {
+    return ((size_t)kslot * a.R + r) * NE + (size_t)rank * Pc;
+  };
+  auto stage_issue = [&](int kslot, int r) {
+    const int b = kslot % 3;
+    const size_t o = slot_off(kslot, r);
+    mbar_expect_tx(&st_bar[b], (uint32_t)(Pc * (sizeof(float4) + sizeof(float2))));
+    bulk_g2s(st_u + (size_t)b * Pc, a.traj_u + o, (uint32_t)(Pc * sizeof(float4)), &st_bar[b]);
+    bulk_g2s(st_ig + (size_t)b * Pc, a.traj_ig + o, (uint32_t)(Pc * sizeof(float2)), &st_bar[b]);
+  };
+  auto stage_wait = [&](int kslot, int len) {
+    const int b = kslot % 3;
+    const uint32_t parity = ((use_par >> b) ^ (uint32_t)((len - 1 - kslot) / 3)) & 1u;
+    for (int it = 0; it < (1 << 22); ++it)
+      if (mbar_try_wait(&st_bar[b], parity)) return;
+    stall = 1;
+  };
 
   for (int r = cid; r < a.R; r += ncl) {
     const size_t roff = (size_t)r * NE + (size_t)rank * Pc;  // lambda, this CTA
@@ -178,15 +216,24 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     float* cim = a.own_in_smem ? sm_cim : a.lam_cim + roff;
     float4* c4 = a.own_in_smem ? sm_c4 : a.lam_c4 + roff;
     const int len = a.n_steps;
+    if (a.stage) {
+      if (tid == 0) {
+        fence_proxy_async();
+        stage_issue(len - 1, r);
+        if (len >= 2) stage_issue(len - 2, r);
+      }
+      stage_wait(len - 1, len);
+    }
     // ---- publish lambda_{s1} (with the tick injection of step s1) ----------
     {
       const size_t xo = ((size_t)(len - 1) * a.R + r) * NE + (size_t)rank * Pc;
+      const float4* xu = a.stage ? st_u + (size_t)((len - 1) % 3) * Pc : a.traj_u + xo;
       const double* coef = tick_coef(a, a.s0 + len, r);
       for_all([&](int i) {
         const float4 L = a.lam[roff + i];
         const float4 gb = __ldg(reinterpret_cast<const float4*>(geo + i) + 1);
         const uint32_t fl = __float_as_uint(gb.w);
-        const float c = ((fl & 1u) ? k.c0j : k.c0) + a.traj_u[xo + i].x;
+        const float c = ((fl & 1u) ? k.c0j : k.c0) + xu[i].x;
         const float inj = tick_injection(a, coef, (int)(rank * Pc + i));
         pub0[i] = make_float4(L.x * sl_inv_factor(k, gb.z, c), L.y, L.z, L.w + inj);
         lc[i] = L.x;
@@ -215,13 +262,25 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       float4* nxt = cur ? pub0 : pub1;
       const uint32_t* bs = s_base + 16 * cur;
       const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * Pc;
-      const float4* __restrict__ tu = a.traj_u + xoff;
-      const float2* __restrict__ tig = a.traj_ig + xoff;
+      const float4* tu = a.traj_u + xoff;
+      const float2* tig = a.traj_ig + xoff;
       const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
-      // the trajectory of the next step (slot t - 2) into L2 while this one runs
-      if (t >= 2 && tid == 0) {
+      const float4* cprev_src = a.traj_u + xprev;
+      if (a.stage) {
+        // slot t - 3 into the buffer slot t left (read at steps t + 1, t + 2)
+        if (t >= 3 && tid == 0) {
+          fence_proxy_async();
+          stage_issue(t - 3, r);
+        }
+        stage_wait(t - 1, len);
+        if (t >= 2) stage_wait(t - 2, len);
+        tu = st_u + (size_t)((t - 1) % 3) * Pc;
+        tig = st_ig + (size_t)((t - 1) % 3) * Pc;
+        cprev_src = st_u + (size_t)((t >= 2 ? t - 2 : 0) % 3) * Pc;
+      } else if (t >= 2 && tid == 0) {
+        // the trajectory of the next step (slot t - 2) into L2 while this one runs
         const size_t xn = ((size_t)(t - 2) * a.R + r) * NE + (size_t)rank * Pc;
         l2_prefetch(a.traj_u + xn, (uint32_t)(Pc * sizeof(float4)));
         l2_prefetch(a.traj_ig + xn, (uint32_t)(Pc * sizeof(float2)));
@@ -234,8 +293,8 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         float* lim = OWN ? sm_lim : a.lam_im + roff;
         float* cim = OWN ? sm_cim : a.lam_cim + roff;
         float4* c4 = OWN ? sm_c4 : a.lam_c4 + roff;
-        const float4 x = __ldg(tu + i);
-        const float2 ig = __ldg(tig + i);
+        const float4 x = tu[i];
+        const float2 ig = tig[i];
         const float xim = ig.x, G = ig.y;
         const float4* gp = reinterpret_cast<const float4*>(geo + i);
         const float4 ga = __ldg(gp);
@@ -327,7 +386,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
                 const float qv = fmaf(w, e.s, wo * so);
                 if (e.kind == 0) {
                   oc = fmaf(-k.jr_scale, qv, oc);
-                  const float cj = k.c0j + a.traj_u[xoff + (oc_code & ch_mask)].x;
+                  const float cj = k.c0j + tu[oc_code & ch_mask].x;
                   g[SRS_ADJ_V_RYR] = fmaf(qv * ak.v_cell, cj - c, g[SRS_ADJ_V_RYR]);
                 } else {
                   oc = fmaf(k.jr_scale, qv, oc);
@@ -362,7 +421,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         kadd(L.w, cm.w, k.dt * oy);
         kadd(lnew, ci, k.dt * oi);
         if (t > 1) {
-          const float cprev = (jsr ? k.c0j : k.c0) + __ldg(a.traj_u + xprev + i).x;
+          const float cprev = (jsr ? k.c0j : k.c0) + cprev_src[i].x;
           const float inj = tick_injection(a, coef_next, (int)(rank * Pc + i));
           nxt[i] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
           lc[i] = L.x;
@@ -419,7 +478,11 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       atomicAdd(a.grad + (size_t)r * NA + tid, v * (double)k.dt);
     }
     step_barrier<C>();  // pub and red are reused by the next realization
+    if (a.stage)
+      for (int b = 0; b < 3; ++b)
+        if (a.n_steps > b) use_par ^= (((uint32_t)((a.n_steps - 1 - b) / 3 + 1)) & 1u) << b;
   }
+  if (stall) atomicOr(a.status, 1u);
 }
 
 // Line-scan loss at one tick: F_i = pad_i + sum_q w_q dye(col_q) from the

@@ -2143,7 +2143,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   // SM overlap each other's barrier waits).
   int best_m = 0, best_C = 0, adj_ncl = 0, best_bits = 0, adj_threads = 0;
   size_t adj_smem = 0;
-  bool best_own = false;
+  bool best_own = false, best_stage = false;
   double best_cost = 1e300;
   for (int thr : {256, 512}) {
     if (d->threads_per_cta && thr != d->threads_per_cta) continue;
@@ -2154,30 +2154,39 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       while ((1 << bits) < Pc) ++bits;
       while ((1 << rbits) < Ca) ++rbits;
       if (bits + rbits > 16) continue;
-      for (int own = 1; own >= 0; --own) {
-        if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
-        const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0);
-        const int ncl = std::min(adjoint_max_clusters(Ca, thr, sm), R);
-        if (ncl <= 0) continue;
-        const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / thr) *
-                            (own ? 1.0 : 1.15) * (thr == 512 ? 1.02 : 1.0);
-        if (cost < best_cost) {
-          best_cost = cost;
-          best_m = m;
-          best_C = Ca;
-          adj_ncl = ncl;
-          adj_smem = sm;
-          best_own = own != 0;
-          best_bits = bits;
-          adj_threads = thr;
+      for (int stage = 1; stage >= 0; --stage) {
+        if (stage && (d->flags & SRS_ADJ_NO_STAGE)) continue;
+        for (int own = 1; own >= 0; --own) {
+          if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
+          const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0, stage != 0);
+          const int ncl = std::min(adjoint_max_clusters(Ca, thr, sm), R);
+          if (ncl <= 0) continue;
+          const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / thr) *
+                              (own ? 1.0 : 1.15) * (stage ? 0.85 : 1.0) * (thr == 512 ? 1.02 : 1.0);
+          if (cost < best_cost) {
+            best_cost = cost;
+            best_m = m;
+            best_C = Ca;
+            adj_ncl = ncl;
+            adj_smem = sm;
+            best_own = own != 0;
+            best_stage = stage != 0;
+            best_bits = bits;
+            adj_threads = thr;
+          }
+          break;  // the on-chip variant when it fits
         }
-        break;  // the on-chip variant when it fits
       }
     }
   }
   if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
   SRS_TRY(adjoint_geometry(s, best_m, best_bits));
   aa.own_in_smem = best_own;
+  aa.stage = best_stage;
+  unsigned int* d_status;
+  SRS_TRY(sc.get(&d_status, 1));
+  SRS_CUDA(cudaMemsetAsync(d_status, 0, sizeof(unsigned int), s->st));
+  aa.status = d_status;
   aa.m_sub = best_m;
   aa.off_bits = best_bits;
   aa.ch_off_bits = s->off_bits;
@@ -2256,6 +2265,11 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
         g[SP_CSQN * (size_t)N + j] = jsr ? li : 0.0;
       }
     }
+  }
+  {
+    unsigned int st_bits = 0;
+    SRS_CUDA(cudaMemcpy(&st_bits, d_status, sizeof(st_bits), cudaMemcpyDeviceToHost));
+    if (st_bits & 1u) return fail(SRS_ERR_TIMEOUT, "adjoint: a trajectory copy did not complete");
   }
   for (int r = 0; r < R; ++r)
     for (int p = 0; p < SRS_N_ADJ; ++p)

@@ -204,6 +204,8 @@ struct AdjArgs {
   float* lam_cim;
   float* lam_c;    // [R][C*P] lambda_Ca within a segment (when not on chip)
   int32_t own_in_smem;  // owner state of lambda in shared memory
+  int32_t stage;        // trajectory staged in shared memory by bulk copies
+  unsigned int* status; // bit 0: a staging wait gave up
   double* grad;  // [R][SRS_N_ADJ]
   Consts32 k;
   AdjConsts ak;
@@ -223,7 +225,7 @@ struct AdjTickArgs {
   double* loss;          // [R][n_samples]: loss terms of this tick
 };
 
-size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem);
+size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, bool stage);
 int launch_adjoint(const AdjArgs& a, int C, int n_clusters, int threads, size_t smem,
                    cudaStream_t st);
 int adjoint_max_clusters(int C, int threads, size_t smem);

@@ -129,14 +129,23 @@ def test_adjoint_segmentation_and_cluster_size_do_not_change_the_result(srs, cas
     assert np.allclose(grad, case["grad"], rtol=1e-5, atol=0)
 
 
-def test_adjoint_state_in_global_memory_gives_the_same_result(srs, case):
+@pytest.mark.parametrize("flags,threads", [("LAMBDA_GLOBAL", 0), ("NO_STAGE", 0),
+                                          ("LAMBDA_GLOBAL|NO_STAGE", 512), ("", 256)])
+def test_adjoint_memory_placements_give_the_same_result(srs, case, flags, threads):
+    """lambda's owner state on chip or in global memory, the trajectory staged
+    in shared memory by bulk copies or read from global memory, 256 or 512
+    threads: the same arithmetic, so loss and dL/dS0 are bit-identical and the
+    gradient differs only by the grouping of its FP32 partial sums."""
     p = case["p"]
+    f = 0
+    for name in filter(None, flags.split("|")):
+        f |= getattr(srs, "ADJ_" + name)
     _, sim = _start(srs, p, srs.FP32, srs.ENGINE_RESIDENT)
     loss, grad, gs = sim.adjoint(N_STEPS, TICK, case["f0"], case["target"], checkpoint_every=K,
-                                 grad_state=True, flags=srs.ADJ_LAMBDA_GLOBAL)
+                                 grad_state=True, flags=f, threads_per_cta=threads)
     assert np.array_equal(loss, case["loss"])
     assert np.array_equal(gs, case["gs"])
-    assert np.allclose(grad, case["grad"], rtol=1e-12, atol=0)
+    assert np.allclose(grad, case["grad"], rtol=1e-5, atol=0)
 
 
 def test_adjoint_leaves_the_state_after_n_steps(srs, case):
