@@ -2162,7 +2162,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
           const int ncl = std::min(adjoint_max_clusters(Ca, thr, sm), R);
           if (ncl <= 0) continue;
           const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / thr) *
-                              (own ? 1.0 : 1.15) * (stage ? 0.85 : 1.0) * (thr == 512 ? 1.02 : 1.0);
+                              (own ? 1.0 : 1.15) * (stage ? 1.01 : 1.0) * (thr == 512 ? 1.02 : 1.0);
           if (cost < best_cost) {
             best_cost = cost;
             best_m = m;

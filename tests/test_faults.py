@@ -1,0 +1,100 @@
+"""Fault injection on the host: corrupted or missing input files and
+inconsistent channel data end in an error code and a message (the reference
+prints and exits or aborts, cpu/InitFuncs.cpp / cpu/OutputFuncs.cpp); nothing
+reaches the device."""
+import os
+import shutil
+
+import pytest
+
+from conftest import GOLDEN_MESH, params_from_golden
+
+SUFFIXES = ("_tet_properties.txt", "_face_properties.txt", ".node", ".ele", "_ryr.txt", "_lcc.txt")
+
+
+@pytest.fixture
+def mesh_copy(tmp_path):
+    base = str(tmp_path / "m")
+    for s in SUFFIXES:
+        shutil.copy(GOLDEN_MESH + s, base + s)
+    return base
+
+
+def _edit(path, fn):
+    lines = open(path).read().splitlines()
+    open(path, "w").write("\n".join(fn(lines)) + "\n")
+
+
+def _load(srs, base):
+    p, _ = params_from_golden(srs, "spark")
+    with pytest.raises(srs.SrsError) as e:
+        srs.Grid(p, base)
+    return e.value.status, str(e.value)
+
+
+def test_missing_file_is_an_io_error(srs, mesh_copy):
+    os.remove(mesh_copy + "_ryr.txt")
+    st, msg = _load(srs, mesh_copy)
+    assert st == -2 and "_ryr.txt" in msg
+
+
+def test_truncated_element_file_is_an_io_error(srs, mesh_copy):
+    _edit(mesh_copy + "_tet_properties.txt", lambda L: L[: len(L) // 2])
+    st, _ = _load(srs, mesh_copy)
+    assert st == -2
+
+
+def test_short_face_line_is_rejected(srs, mesh_copy):
+    """The files are read field by field across line breaks (as the
+    reference's fscanf does), so a short line shifts every later field: the
+    result is an inconsistent mesh or a read error, never a silent load."""
+    _edit(mesh_copy + "_face_properties.txt", lambda L: L[:5] + [" ".join(L[5].split()[:10])] + L[6:])
+    st, _ = _load(srs, mesh_copy)
+    assert st in (-2, -3)
+
+
+@pytest.mark.parametrize("which,value", [("ryr_ele", "100000"), ("ryr_jsr", "-3"), ("lcc", "384")])
+def test_channel_index_out_of_range_is_a_mesh_error(srs, mesh_copy, which, value):
+    if which == "lcc":
+        _edit(mesh_copy + "_lcc.txt", lambda L: L[:1] + [value] + L[2:])
+    else:
+        col = 0 if which == "ryr_ele" else 1
+
+        def f(L):
+            w = L[1].split()
+            w[col] = value
+            return L[:1] + [" ".join(w)] + L[2:]
+        _edit(mesh_copy + "_ryr.txt", f)
+    st, msg = _load(srs, mesh_copy)
+    assert st == -3 and "out of range" in msg
+
+
+def test_face_element_out_of_range_is_a_mesh_error(srs, mesh_copy):
+    def f(L):
+        w = L[2].split()
+        w[0] = "99999"
+        return L[:2] + [" ".join(w)] + L[3:]
+    _edit(mesh_copy + "_face_properties.txt", f)
+    st, _ = _load(srs, mesh_copy)
+    assert st == -3
+
+
+def test_non_positive_volume_is_a_mesh_error(srs, mesh_copy):
+    def f(L):
+        w = L[2].split()
+        w[3] = "0"
+        return L[:2] + [" ".join(w)] + L[3:]
+    _edit(mesh_copy + "_tet_properties.txt", f)
+    st, msg = _load(srs, mesh_copy)
+    assert st == -3 and "volume" in msg
+
+
+def test_parameter_file_errors(srs, tmp_path):
+    with pytest.raises(srs.SrsError) as e:
+        srs.read_parameters(str(tmp_path / "absent.xml"))
+    assert e.value.status == -2
+    empty = tmp_path / "empty.xml"
+    empty.write_text("<?xml version='1.0'?>\\n<simulation>\\n</simulation>\\n")
+    with pytest.raises(srs.SrsError) as e:
+        srs.read_parameters(str(empty))
+    assert e.value.status == -2
