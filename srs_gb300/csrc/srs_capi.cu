@@ -364,6 +364,11 @@ int check_fp32_supported(const srs_sim* s, bool resident) {
   const Operator& op = s->op;
   if (s->p.reals[R_B_TOT_SL_LO] != 0.0)
     return fail(SRS_ERR_UNSUPPORTED, "FP32 engines model only the high-affinity SL buffer");
+  for (int i = 0; i < m.NR; ++i)
+    if (m.domain[m.ryr_ele[i]] != DOMAIN_CYTO || m.domain[m.ryr_jsr[i]] != DOMAIN_JSR)
+      return fail(SRS_ERR_MESH, "RyR " + std::to_string(i) +
+                                    ": the FP32 engines need its cleft element in the cytosol and "
+                                    "its JSR element in the JSR");
   for (int j = 0; j < m.N; ++j) {
     for (int k = 0; k < 4; ++k) {
       int n = op.nij[4 * (size_t)j + k];

@@ -98,3 +98,22 @@ def test_parameter_file_errors(srs, tmp_path):
     with pytest.raises(srs.SrsError) as e:
         srs.read_parameters(str(empty))
     assert e.value.status == -2
+
+
+@pytest.mark.gpu
+def test_ryr_with_swapped_domains_is_rejected_by_fp32_engines(srs, mesh_copy):
+    """The FP32 engines store Ca relative to each domain's rest and take a
+    RyR's flux from its JSR element to its cleft element; a RyR whose two
+    elements are swapped is refused instead of giving wrong fluxes."""
+    def f(L):
+        w = L[1].split()
+        w[0], w[1] = w[1], w[0]
+        return L[:1] + [" ".join(w)] + L[2:]
+    _edit(mesh_copy + "_ryr.txt", f)
+    p, _ = params_from_golden(srs, "spark")
+    g = srs.Grid(p, mesh_copy)
+    srs.Simulation(g, p, 1, srs.FP64, srs.ENGINE_PLAIN)  # absolute FP64 state: fine
+    for eng in (srs.ENGINE_PLAIN, srs.ENGINE_RESIDENT):
+        with pytest.raises(srs.SrsError) as e:
+            srs.Simulation(g, p, 1, srs.FP32, eng)
+        assert e.value.status == -3
