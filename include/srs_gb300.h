@@ -277,6 +277,9 @@ enum {
 /* SRS_ADJ_NO_STAGE reads the recorded trajectory straight from global memory
  * instead of staging each step's slice in shared memory by bulk copies. */
 #define SRS_ADJ_NO_STAGE 2
+/* SRS_ADJ_STAGE always stages the slices (the library does not choose it by
+ * itself: on the measured meshes it is not faster). */
+#define SRS_ADJ_STAGE 4
 typedef struct srs_adjoint_desc {
   int64_t n_steps;
   int tick_every;

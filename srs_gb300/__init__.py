@@ -130,6 +130,7 @@ NOALLOC_MAX_REALIZATIONS = 256
 
 ADJ_LAMBDA_GLOBAL = 1
 ADJ_NO_STAGE = 2
+ADJ_STAGE = 4
 
 
 class _AdjDesc(C.Structure):

@@ -2161,6 +2161,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       if (bits + rbits > 16) continue;
       for (int stage = 1; stage >= 0; --stage) {
         if (stage && (d->flags & SRS_ADJ_NO_STAGE)) continue;
+        if (!stage && (d->flags & SRS_ADJ_STAGE)) continue;
         for (int own = 1; own >= 0; --own) {
           if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
           const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0, stage != 0);

@@ -130,7 +130,8 @@ def test_adjoint_segmentation_and_cluster_size_do_not_change_the_result(srs, cas
 
 
 @pytest.mark.parametrize("flags,threads", [("LAMBDA_GLOBAL", 0), ("NO_STAGE", 0),
-                                          ("LAMBDA_GLOBAL|NO_STAGE", 512), ("", 256)])
+                                          ("LAMBDA_GLOBAL|NO_STAGE", 512), ("", 256),
+                                          ("STAGE", 256), ("STAGE|LAMBDA_GLOBAL", 512)])
 def test_adjoint_memory_placements_give_the_same_result(srs, case, flags, threads):
     """lambda's owner state on chip or in global memory, the trajectory staged
     in shared memory by bulk copies or read from global memory, 256 or 512
