@@ -104,7 +104,7 @@ __device__ __forceinline__ float sl_inv_factor(const Consts32& k, float bsl, flo
   if (bsl == 0.0f) return 1.0f;
   const float kc = k.khi + c;
   const float kc2 = kc * kc;
-  return kc2 / (kc2 + bsl);
+  return __fdividef(kc2, kc2 + bsl);
 }
 
 }  // namespace
@@ -147,8 +147,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int n_ch = rank == 0 ? n_ch0 : 0;  // channel elements: forward partition 0
   const size_t NE = (size_t)C * Pc;
-  const TetRec* geo = a.geo + (size_t)rank * Pc;
-  const float4* aT = a.aT + (size_t)rank * Pc;
+  const AdjRec* geo = a.geo + (size_t)rank * Pc;
   const uint32_t mask = (1u << a.off_bits) - 1u;
   const uint32_t ch_mask = (1u << a.ch_off_bits) - 1u;  // channel codes: forward layout
   // element ranges of this CTA: forward partitions rank*msub .. + msub - 1,
@@ -232,10 +231,10 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       for_all([&](int i) {
         const float4 L = a.lam[roff + i];
         const float4 gb = __ldg(reinterpret_cast<const float4*>(geo + i) + 1);
-        const uint32_t fl = __float_as_uint(gb.w);
-        const float c = ((fl & 1u) ? k.c0j : k.c0) + xu[i].x;
+        const bool jsr = (__float_as_uint(gb.w) >> 31) != 0;
+        const float c = (jsr ? k.c0j : k.c0) + xu[i].x;
         const float inj = tick_injection(a, coef, (int)(rank * Pc + i));
-        pub0[i] = make_float4(L.x * sl_inv_factor(k, gb.z, c), L.y, L.z, L.w + inj);
+        pub0[i] = make_float4(L.x * sl_inv_factor(k, fabsf(gb.z), c), L.y, L.z, L.w + inj);
         lc[i] = L.x;
         if (a.own_in_smem) {
           lim[i] = a.lam_im[roff + i];
@@ -287,23 +286,36 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       }
 
       // OWN: the owner state of lambda is in shared memory (else global)
-      auto element = [&](int i, auto own) {
+      // the element's record and trajectory slice, loaded one element ahead
+      struct Pre {
+        float4 at, gb, x;
+        float2 ig;
+      };
+      auto preload = [&](int i) {
+        const float4* gp = reinterpret_cast<const float4*>(geo + i);
+        Pre q;
+        q.at = __ldg(gp);
+        q.gb = __ldg(gp + 1);
+        q.x = tu[i];
+        q.ig = tig[i];
+        return q;
+      };
+      auto element = [&](int i, const Pre& pre, auto own) {
         constexpr bool OWN = decltype(own)::value;
         float* lc = OWN ? sm_lc : a.lam_c + roff;
         float* lim = OWN ? sm_lim : a.lam_im + roff;
         float* cim = OWN ? sm_cim : a.lam_cim + roff;
         float4* c4 = OWN ? sm_c4 : a.lam_c4 + roff;
-        const float4 x = tu[i];
-        const float2 ig = tig[i];
-        const float xim = ig.x, G = ig.y;
-        const float4* gp = reinterpret_cast<const float4*>(geo + i);
-        const float4 ga = __ldg(gp);
-        const float4 gb = __ldg(gp + 1);
-        const float4 at = __ldg(aT + i);
+        const float4 x = pre.x;
+        const float xim = pre.ig.x, G = pre.ig.y;
+        const float4 at = pre.at;
+        const float4 gb = pre.gb;
         const uint32_t w0 = __float_as_uint(gb.x), w1 = __float_as_uint(gb.y);
         const uint32_t c0 = w0 & 0xffffu, c1 = w0 >> 16, c2 = w1 & 0xffffu, c3 = w1 >> 16;
-        const float bsl = gb.z;
-        const uint32_t fl = __float_as_uint(gb.w);
+        const float bsl = fabsf(gb.z);
+        const bool trpn = (__float_as_uint(gb.z) >> 31) != 0;
+        const float sa = fabsf(gb.w);
+        const bool jsr = (__float_as_uint(gb.w) >> 31) != 0;
         const float4 me = pub[i];
         float4 n0, n1, n2, n3;
         if constexpr (C == 1) {
@@ -317,7 +329,6 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & mask) * 16u);
           n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & mask) * 16u);
         }
-        const float sa = (ga.x + ga.y) + (ga.z + ga.w);
         // transposed diffusion: S = sum_k aT_k lambda(nb_k) - (sum_k a_k) lambda(self)
         float Sc = at.x * n0.x;
         Sc = fmaf(at.y, n1.x, Sc);
@@ -349,20 +360,19 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         const float w = me.x;
         const float li = lim[i];
         float dG = 0.0f;
-        const bool jsr = (fl & 1u) != 0;
         const float c = (jsr ? k.c0j : k.c0) + x.x;
         if (!jsr) {
           adj_buffer(k, ak, 0, c, x.w, me.w, w, oy, oc, dG, g, SRS_ADJ_K_ON_DYE);
           adj_buffer(k, ak, 1, c, x.y, me.y, w, oa, oc, dG, g, SRS_ADJ_K_ON_ATP);
           adj_buffer(k, ak, 2, c, x.z, me.z, w, om, oc, dG, g, SRS_ADJ_K_ON_CMDN);
-          if (fl & 2u) {
+          if (trpn) {
             adj_buffer(k, ak, 3, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_TRPN);
             // SERCA v(Ki), Ki = (c / K_D_i)^2 (cpu/RunSimulation.cpp:83-91)
             float Ki = c * k.inv_kdi;
             Ki = Ki * Ki;
             const float den = fmaf(Ki * Ki, k.sd2, fmaf(Ki, k.sd1, k.sd0));
             const float num = fmaf(Ki * Ki, 3.24873e12f, fmaf(Ki, k.sn1, -k.sn0));
-            const float iden = 1.0f / den;
+            const float iden = __fdividef(1.0f, den);
             const float v = num * iden;
             const float dnum = fmaf(2.0f * Ki, 3.24873e12f, k.sn1);
             const float dden = fmaf(2.0f * Ki, k.sd2, k.sd1);
@@ -402,9 +412,9 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         if (bsl != 0.0f) {
           // F_Ca = G / B(c):  -G B'(c) / B^2 lambda_Ca = 2 bsl G w / (B kc^3)
           const float kc = k.khi + c;
-          const float ikc = 1.0f / kc;
+          const float ikc = __fdividef(1.0f, kc);
           const float bk2 = bsl * ikc * ikc;           // B - 1
-          const float GB = G / (1.0f + bk2);           // G / B
+          const float GB = __fdividef(G, 1.0f + bk2);  // G / B
           const float t3 = GB * bk2 * ikc;             // G bsl / (B kc^3)
           oc = fmaf(2.0f * t3, w, oc);
           g[SRS_ADJ_B_TOT_SL] -= w * GB * bk2 * ak.inv_btot_sl;
@@ -435,21 +445,36 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           a.lam_cim[roff + i] = ci;
         }
       };
-      auto element_s = [&](int i) { element(i, std::true_type{}); };
-      auto element_g = [&](int i) { element(i, std::false_type{}); };
+      auto element_s = [&](int i, const Pre& q) { element(i, q, std::true_type{}); };
+      auto element_g = [&](int i, const Pre& q) { element(i, q, std::false_type{}); };
+      // for_range with the loads of the next element issued before the
+      // current one is computed
+      auto pipe_range = [&](int& idx, int lo, int hi, auto&& f) {
+        const int n = hi - lo;
+        if (idx < n) {
+          Pre cur_p = preload(lo + idx);
+          for (; idx < n; idx += nthr) {
+            Pre nxt_p = cur_p;
+            if (idx + nthr < n) nxt_p = preload(lo + idx + nthr);
+            f(lo + idx, cur_p);
+            cur_p = nxt_p;
+          }
+        }
+        idx -= n;
+      };
       // interior elements (and the channel elements when they are interior):
       // interior to their forward partition, hence to this CTA
       auto sweep = [&](auto&& element) {
         int idx = tid;
         for (int j = 0; j < msub; ++j) {
           const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-          for_range(idx, j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
+          pipe_range(idx, j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
         }
         cl_wait<C>();
         for (int j = 0; j < msub; ++j) {
           const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-          if (!a.ch_interior) for_range(idx, j * P, j * P + nc, element);
-          for_range(idx, j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
+          if (!a.ch_interior) pipe_range(idx, j * P, j * P + nc, element);
+          pipe_range(idx, j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
         }
       };
       if (a.own_in_smem) sweep(element_s);

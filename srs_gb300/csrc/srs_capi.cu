@@ -94,14 +94,14 @@ struct srs_sim {
   std::vector<double> ls_w_h;
   int ls_version = 0;
   // adjoint (built on first use)
-  float4* d_aT = nullptr;
+  std::vector<float4> aT_h;  // transposed coefficients, engine order (host)
   float* d_ryr_s_cl = nullptr;
   float* d_ryr_s_js = nullptr;
   int32_t* d_wt_ptr = nullptr;
   int32_t* d_wt_idx = nullptr;
   double* d_wt_w = nullptr;
   int adj_ls_version = -1;
-  TetRec* d_adj_geo = nullptr;  // geometry with the adjoint's CTA grouping
+  AdjRec* d_adj_geo = nullptr;  // reverse-sweep records of the CTA grouping
   int adj_geo_m = 0;
   // total Ca (built on first use)
   MassArgs mass{};
@@ -1849,10 +1849,11 @@ struct Scratch {
 // Transposed coefficients, RyR volume factors and the element -> sample map
 // of the line scan, in the resident engine layout.
 int adjoint_setup(srs_sim* s) {
-  if (s->d_aT && s->adj_ls_version == s->ls_version) return SRS_OK;
+  if (!s->aT_h.empty() && s->adj_ls_version == s->ls_version) return SRS_OK;
   const int NE = (int)eng_count(s);
-  if (!s->d_aT) {
-    std::vector<float4> aT(NE, make_float4(0, 0, 0, 0));
+  if (s->aT_h.empty()) {
+    std::vector<float4>& aT = s->aT_h;
+    aT.assign(NE, make_float4(0, 0, 0, 0));
     for (int e = 0; e < NE; ++e) {
       const int j = s->ref_of_eng[e];
       if (j < 0) continue;
@@ -1873,7 +1874,6 @@ int adjoint_setup(srs_sim* s) {
       scl[i] = (float)(1.0 / s->m.V0[s->m.ryr_ele[i]]);
       sjs[i] = (float)(-(1.0 / s->m.V0[s->m.ryr_jsr[i]]));
     }
-    SRS_TRY(dev_upload(s, &s->d_aT, aT.data(), aT.size()));
     SRS_TRY(dev_upload(s, &s->d_ryr_s_cl, scl.data(), scl.size()));
     SRS_TRY(dev_upload(s, &s->d_ryr_s_js, sjs.data(), sjs.size()));
   }
@@ -1909,9 +1909,10 @@ struct StateSnap {
   RealCtl* ctl;
 };
 
-// Geometry records with neighbour codes for CTAs that each hold m
+// Reverse-sweep records with neighbour codes for CTAs that each hold m
 // consecutive partitions of the forward layout (same element order, so every
-// per-element array keeps its index).
+// per-element array keeps its index).  The two domain flags ride in sign
+// bits: bsl and sa are never negative.
 int adjoint_geometry(srs_sim* s, int m, int bits) {
   if (s->d_adj_geo && s->adj_geo_m == m) return SRS_OK;
   const int Pf = s->P_stride, NE = (int)eng_count(s);
@@ -1919,24 +1920,33 @@ int adjoint_geometry(srs_sim* s, int m, int bits) {
     const int q = e / Pf, off = e % Pf;
     return (uint16_t)(((q / m) << bits) | ((q % m) * Pf + off));
   };
-  std::vector<TetRec> geo(NE);
-  std::memset(geo.data(), 0, geo.size() * sizeof(TetRec));
+  std::vector<AdjRec> geo(NE);
+  std::memset(geo.data(), 0, geo.size() * sizeof(AdjRec));
   for (int e = 0; e < NE; ++e) {
     const int j = s->ref_of_eng[e];
     if (j < 0) {
       for (int k = 0; k < 4; ++k) geo[e].nb[k] = mcode(e);
       continue;
     }
+    float a[4];
     for (int k = 0; k < 4; ++k) {
-      geo[e].a[k] = (float)s->op.aij[5 * (size_t)j + 1 + k];
+      a[k] = (float)s->op.aij[5 * (size_t)j + 1 + k];
       geo[e].nb[k] = mcode(s->eng_of_ref[s->op.nij[4 * (size_t)j + k]]);
     }
-    geo[e].bsl = bsl_of(s, j);
-    geo[e].flags = (s->m.domain[j] == DOMAIN_JSR ? 1u : 0u) | (s->m.tropc[j] ? 2u : 0u) |
-                   (e < s->part_nch[0] ? 4u : 0u);
+    const float4 t = s->aT_h[e];
+    geo[e].aT[0] = t.x;
+    geo[e].aT[1] = t.y;
+    geo[e].aT[2] = t.z;
+    geo[e].aT[3] = t.w;
+    const float sa = (a[0] + a[1]) + (a[2] + a[3]);
+    const float bsl = bsl_of(s, j);
+    geo[e].bsl = s->m.tropc[j] ? -bsl : bsl;
+    geo[e].sa = s->m.domain[j] == DOMAIN_JSR ? -sa : sa;
+    if (bsl < 0.0f || sa < 0.0f || std::signbit(bsl) || std::signbit(sa))
+      return fail(SRS_ERR_MESH, "negative SL capacity or coupling coefficient");
   }
   if (s->d_adj_geo) {
-    SRS_CUDA(cudaMemcpy(s->d_adj_geo, geo.data(), geo.size() * sizeof(TetRec), cudaMemcpyHostToDevice));
+    SRS_CUDA(cudaMemcpy(s->d_adj_geo, geo.data(), geo.size() * sizeof(AdjRec), cudaMemcpyHostToDevice));
   } else {
     SRS_TRY(dev_upload(s, &s->d_adj_geo, geo.data(), geo.size()));
   }
@@ -2097,7 +2107,6 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   AdjArgs aa{};
   aa.R = R;
   aa.P = s->P_stride;
-  aa.aT = s->d_aT;
   aa.n_local = s->ar.n_local;
   aa.n_chtet = s->ar.n_chtet;
   aa.n_int = s->ar.n_int;

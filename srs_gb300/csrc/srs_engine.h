@@ -86,6 +86,15 @@ struct __align__(16) TetRec {
   uint32_t flags;
 };
 
+// Per-element record of the reverse sweep (32 bytes, two vector loads).
+struct __align__(16) AdjRec {
+  float aT[4];     // coefficient of this element in each neighbour's row
+  uint16_t nb[4];  // neighbour codes of the adjoint's CTA grouping
+  float bsl;       // SL capacity x K_D; sign bit set: the element has troponin C
+  float sa;        // sum of the element's own off-diagonal coefficients; sign bit
+                   // set: JSR element
+};
+
 struct ResidentArgs {
   int32_t R;
   int32_t P;
@@ -176,8 +185,7 @@ struct AdjArgs {
   int32_t ch_off_bits;     // off_bits of the forward layout (channel codes)
   int32_t n_steps;  // steps of the segment; the kernel runs t = n_steps .. 1
   int64_t s0;       // global index of the state the segment starts from
-  const TetRec* geo;  // geometry with neighbour codes of the CTA grouping
-  const float4* aT;  // [C*P] coefficient of this element in each neighbour's row
+  const AdjRec* geo;  // [C*P] per-element records of the CTA grouping
   const int32_t* n_local;
   const int32_t* n_chtet;
   const int32_t* n_int;    // [C] interior elements after the channel elements
