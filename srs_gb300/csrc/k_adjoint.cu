@@ -54,18 +54,19 @@ __device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& a
   const float alpha = k.kon[q] * free;
   const float beta = fmaf(k.kon[q], c, k.koff[q]);
   dG -= alpha;            // dF_Ca/dCa (times B)
-  ob += beta * (w - lb);  // dF_Ca/db * lambda_Ca + dF_b/db * lambda_b
-  oc += alpha * lb;       // dF_b/dCa * lambda_b
+  ob = fmaf(beta, w - lb, ob);  // dF_Ca/db * lambda_Ca + dF_b/db * lambda_b
+  oc = fmaf(alpha, lb, oc);      // dF_b/dCa * lambda_b
   const float d = lb - w;
-  g[gi] += d * free * c;              // dr/dkon = (B - b) c
-  g[gi + 1] -= d * (ak.brest[q] + ub);  // dr/dkoff = -b
+  g[gi] = fmaf(d * free, c, g[gi]);                  // dr/dkon = (B - b) c
+  g[gi + 1] = fmaf(-d, ak.brest[q] + ub, g[gi + 1]);  // dr/dkoff = -b
 }
 
 }  // namespace
 
 // Shared memory: float4 pub[2][P]; double red[32][NA]; int32 cptr[n_ch+1];
 // ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16]; then, when
-// `own_in_smem`, the owner state float4 c4[P], float lc[P], lim[P], cim[P];
+// `own_in_smem`, the owner state float4 c4[P], o[P] (lambda_Ca, lambda_imm,
+// its compensation, unused);
 // then, when `stage`, three trajectory buffers float4 u[3][P], float2
 // ig[3][P] and their mbarriers uint64 bar[3].
 size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, bool stage) {
@@ -76,7 +77,7 @@ size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, b
   b = (b + 15) & ~(size_t)15;
   b += (size_t)n_entries * sizeof(ChanEntry32);
   b += 2 * 16 * sizeof(uint32_t);
-  if (own_in_smem) b += (size_t)P * (3 * sizeof(float) + sizeof(float4));
+  if (own_in_smem) b += (size_t)P * 2 * sizeof(float4);
   if (stage) b += (size_t)3 * P * (sizeof(float4) + sizeof(float2)) + 3 * sizeof(uint64_t);
   return b;
 }
@@ -131,12 +132,12 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       (reinterpret_cast<uintptr_t>(s_cptr + n_ch0 + 1) + 15) & ~(uintptr_t)15);
   const int n_ent = a.ch_ptr[n_ch0];
   uint32_t* s_base = reinterpret_cast<uint32_t*>(s_clist + n_ent);  // [2][16]
+  // owner state on chip: compensation terms c4, then (lambda_Ca, lambda_imm,
+  // compensation of lambda_imm, unused) in one float4 per element
   float4* sm_c4 = reinterpret_cast<float4*>(s_base + 32);
-  float* sm_lc = reinterpret_cast<float*>(sm_c4 + Pc);
-  float* sm_lim = sm_lc + Pc;
-  float* sm_cim = sm_lim + Pc;
+  float4* sm_o = sm_c4 + Pc;
   // trajectory staging (a.stage): slot k of the segment in buffer k % 3
-  float4* st_u = reinterpret_cast<float4*>(a.own_in_smem ? reinterpret_cast<unsigned char*>(sm_cim + Pc)
+  float4* st_u = reinterpret_cast<float4*>(a.own_in_smem ? reinterpret_cast<unsigned char*>(sm_o + Pc)
                                                          : reinterpret_cast<unsigned char*>(s_base + 32));
   float2* st_ig = reinterpret_cast<float2*>(st_u + 3 * Pc);
   uint64_t* st_bar = reinterpret_cast<uint64_t*>(st_ig + 3 * Pc);
@@ -209,11 +210,6 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
 
   for (int r = cid; r < a.R; r += ncl) {
     const size_t roff = (size_t)r * NE + (size_t)rank * Pc;  // lambda, this CTA
-    // owner state: on chip when it fits, else the global arrays themselves
-    float* lc = a.own_in_smem ? sm_lc : a.lam_c + roff;
-    float* lim = a.own_in_smem ? sm_lim : a.lam_im + roff;
-    float* cim = a.own_in_smem ? sm_cim : a.lam_cim + roff;
-    float4* c4 = a.own_in_smem ? sm_c4 : a.lam_c4 + roff;
     const int len = a.n_steps;
     if (a.stage) {
       if (tid == 0) {
@@ -235,11 +231,12 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         const float c = (jsr ? k.c0j : k.c0) + xu[i].x;
         const float inj = tick_injection(a, coef, (int)(rank * Pc + i));
         pub0[i] = make_float4(L.x * sl_inv_factor(k, fabsf(gb.z), c), L.y, L.z, L.w + inj);
-        lc[i] = L.x;
+        // owner state: on chip when it fits, else the global arrays themselves
         if (a.own_in_smem) {
-          lim[i] = a.lam_im[roff + i];
-          cim[i] = a.lam_cim[roff + i];
-          c4[i] = a.lam_c4[roff + i];
+          sm_o[i] = make_float4(L.x, a.lam_im[roff + i], a.lam_cim[roff + i], 0.0f);
+          sm_c4[i] = a.lam_c4[roff + i];
+        } else {
+          a.lam_c[roff + i] = L.x;
         }
       });
     }
@@ -302,10 +299,18 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       };
       auto element = [&](int i, const Pre& pre, auto own) {
         constexpr bool OWN = decltype(own)::value;
-        float* lc = OWN ? sm_lc : a.lam_c + roff;
-        float* lim = OWN ? sm_lim : a.lam_im + roff;
-        float* cim = OWN ? sm_cim : a.lam_cim + roff;
-        float4* c4 = OWN ? sm_c4 : a.lam_c4 + roff;
+        float lx, li, ci;
+        if constexpr (OWN) {
+          const float4 o = sm_o[i];
+          lx = o.x;
+          li = o.y;
+          ci = o.z;
+        } else {
+          lx = a.lam_c[roff + i];
+          li = a.lam_im[roff + i];
+          ci = a.lam_cim[roff + i];
+        }
+        float4 cm = OWN ? sm_c4[i] : a.lam_c4[roff + i];
         const float4 x = pre.x;
         const float xim = pre.ig.x, G = pre.ig.y;
         const float4 at = pre.at;
@@ -358,7 +363,6 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         g[SRS_ADJ_D_DYE] = fmaf(x.w, Sy, g[SRS_ADJ_D_DYE]);
         float oc = k.D[0] * Sc, oa = k.D[1] * Sa, om = k.D[2] * Sm, oy = k.D[3] * Sy, oi = 0.0f;
         const float w = me.x;
-        const float li = lim[i];
         float dG = 0.0f;
         const float c = (jsr ? k.c0j : k.c0) + x.x;
         if (!jsr) {
@@ -378,7 +382,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
             const float dden = fmaf(2.0f * Ki, k.sd2, k.sd1);
             const float dv = (dnum - v * dden) * iden * (2.0f * c * k.inv_kdi * k.inv_kdi);
             dG = fmaf(-k.serca_scale, dv, dG);
-            g[SRS_ADJ_A_P] -= w * ak.serca_per_ap * v;
+            g[SRS_ADJ_A_P] = fmaf(-w * ak.serca_per_ap, v, g[SRS_ADJ_A_P]);
           }
         } else {
           adj_buffer(k, ak, 4, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_CSQN);
@@ -417,13 +421,11 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           const float GB = __fdividef(G, 1.0f + bk2);  // G / B
           const float t3 = GB * bk2 * ikc;             // G bsl / (B kc^3)
           oc = fmaf(2.0f * t3, w, oc);
-          g[SRS_ADJ_B_TOT_SL] -= w * GB * bk2 * ak.inv_btot_sl;
-          g[SRS_ADJ_K_D_SL] -= w * t3 * (c - k.khi) * ak.inv_khi;
+          g[SRS_ADJ_B_TOT_SL] = fmaf(-w * GB, bk2 * ak.inv_btot_sl, g[SRS_ADJ_B_TOT_SL]);
+          g[SRS_ADJ_K_D_SL] = fmaf(-w * t3, (c - k.khi) * ak.inv_khi, g[SRS_ADJ_K_D_SL]);
         }
         // compensated update of lambda
-        float4 L = make_float4(lc[i], me.y, me.z, me.w);
-        float4 cm = c4[i];
-        float ci = cim[i];
+        float4 L = make_float4(lx, me.y, me.z, me.w);
         float lnew = li;
         kadd(L.x, cm.x, k.dt * oc);
         kadd(L.y, cm.y, k.dt * oa);
@@ -434,10 +436,15 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
           const float cprev = (jsr ? k.c0j : k.c0) + cprev_src[i].x;
           const float inj = tick_injection(a, coef_next, (int)(rank * Pc + i));
           nxt[i] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
-          lc[i] = L.x;
-          lim[i] = lnew;
-          c4[i] = cm;
-          cim[i] = ci;
+          if constexpr (OWN) {
+            sm_o[i] = make_float4(L.x, lnew, ci, 0.0f);
+            sm_c4[i] = cm;
+          } else {
+            a.lam_c[roff + i] = L.x;
+            a.lam_im[roff + i] = lnew;
+            a.lam_c4[roff + i] = cm;
+            a.lam_cim[roff + i] = ci;
+          }
         } else {
           a.lam[roff + i] = L;
           a.lam_im[roff + i] = lnew;
