@@ -64,7 +64,8 @@ __device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& a
 }  // namespace
 
 // Shared memory: float4 pub[2][P]; double red[32][NA]; int32 cptr[n_ch+1];
-// ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16]; then, when
+// ChanEntry32 clist[] (16-byte aligned); uint32 base[2][16]; uint16
+// sched[P] (16-byte aligned end); then, when
 // `own_in_smem`, the owner state float4 c4[P], o[P] (lambda_Ca, lambda_imm,
 // its compensation, unused);
 // then, when `stage`, three trajectory buffers float4 u[3][P], float2
@@ -77,6 +78,8 @@ size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, b
   b = (b + 15) & ~(size_t)15;
   b += (size_t)n_entries * sizeof(ChanEntry32);
   b += 2 * 16 * sizeof(uint32_t);
+  b += (size_t)P * sizeof(uint16_t);
+  b = (b + 15) & ~(size_t)15;
   if (own_in_smem) b += (size_t)P * 2 * sizeof(float4);
   if (stage) b += (size_t)3 * P * (sizeof(float4) + sizeof(float2)) + 3 * sizeof(uint64_t);
   return b;
@@ -132,13 +135,15 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       (reinterpret_cast<uintptr_t>(s_cptr + n_ch0 + 1) + 15) & ~(uintptr_t)15);
   const int n_ent = a.ch_ptr[n_ch0];
   uint32_t* s_base = reinterpret_cast<uint32_t*>(s_clist + n_ent);  // [2][16]
+  uint16_t* sched = reinterpret_cast<uint16_t*>(s_base + 32);         // [Pc]
   // owner state on chip: compensation terms c4, then (lambda_Ca, lambda_imm,
   // compensation of lambda_imm, unused) in one float4 per element
-  float4* sm_c4 = reinterpret_cast<float4*>(s_base + 32);
+  float4* sm_c4 = reinterpret_cast<float4*>(
+      (reinterpret_cast<uintptr_t>(sched + Pc) + 15) & ~(uintptr_t)15);
   float4* sm_o = sm_c4 + Pc;
   // trajectory staging (a.stage): slot k of the segment in buffer k % 3
   float4* st_u = reinterpret_cast<float4*>(a.own_in_smem ? reinterpret_cast<unsigned char*>(sm_o + Pc)
-                                                         : reinterpret_cast<unsigned char*>(s_base + 32));
+                                                         : reinterpret_cast<unsigned char*>(sm_c4));
   float2* st_ig = reinterpret_cast<float2*>(st_u + 3 * Pc);
   uint64_t* st_bar = reinterpret_cast<uint64_t*>(st_ig + 3 * Pc);
 
@@ -179,6 +184,27 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   if (tid < C) {
     s_base[tid] = (C > 1) ? map_rank(smem_addr(pub0), tid) : smem_addr(pub0);
     s_base[16 + tid] = (C > 1) ? map_rank(smem_addr(pub1), tid) : smem_addr(pub1);
+  }
+  // Element schedule of a step: the interior ranges of this CTA's
+  // partitions, then (after the cluster wait) the channel range when it is
+  // not interior and the boundary ranges.  Position q of the schedule goes
+  // to thread q % nthr, so every thread gets the same count.
+  int n_pre = 0, n_sched = 0;
+  {
+    auto put = [&](int lo, int hi) {
+      for (int i = tid; i < hi - lo; i += nthr) sched[n_sched + i] = (uint16_t)(lo + i);
+      n_sched += hi - lo;
+    };
+    for (int j = 0; j < msub; ++j) {
+      const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
+      put(j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q]);
+    }
+    n_pre = n_sched;
+    for (int j = 0; j < msub; ++j) {
+      const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
+      if (!a.ch_interior) put(j * P, j * P + nc);
+      put(j * P + nc + a.n_int[q], j * P + a.n_local[q]);
+    }
   }
   step_barrier<C>();
 
@@ -252,18 +278,53 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
     // slots all live in this CTA (the __syncthreads orders those)
     __syncthreads();
     cl_arrive<C>();
+    // trajectory of step t (x_{t-1}, its immobile buffer and Ca rate) and
+    // the Ca of x_{t-2} (for lambda_Ca / B of the next step's slot)
+    struct StepPtr {
+      const float4* tu;
+      const float2* tig;
+      const float4* cprev;
+    };
+    auto step_ptrs = [&](int t) {
+      StepPtr sp;
+      if (a.stage) {
+        sp.tu = st_u + (size_t)((t - 1) % 3) * Pc;
+        sp.tig = st_ig + (size_t)((t - 1) % 3) * Pc;
+        sp.cprev = st_u + (size_t)((t >= 2 ? t - 2 : 0) % 3) * Pc;
+      } else {
+        const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * Pc;
+        sp.tu = a.traj_u + xoff;
+        sp.tig = a.traj_ig + xoff;
+        sp.cprev = a.traj_u + ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
+      }
+      return sp;
+    };
+    // the element's record and trajectory, loaded one element ahead (and,
+    // for a thread's first element, during the previous step)
+    struct Pre {
+      float4 at, gb, x;
+      float2 ig;
+      float cp;
+    };
+    auto preload = [&](int i, const StepPtr& sp, int t) {
+      const float4* gp = reinterpret_cast<const float4*>(geo + i);
+      Pre q;
+      q.at = __ldg(gp);
+      q.gb = __ldg(gp + 1);
+      q.x = sp.tu[i];
+      q.ig = sp.tig[i];
+      q.cp = t > 1 ? sp.cprev[i].x : 0.0f;
+      return q;
+    };
+    Pre first = {};
+    bool have_first = false;
     for (int t = len; t >= 1; --t) {
       const int64_t n = a.s0 + t;  // this step maps x_{n-1} to x_n
       const float4* pub = cur ? pub1 : pub0;
       float4* nxt = cur ? pub0 : pub1;
       const uint32_t* bs = s_base + 16 * cur;
-      const size_t xoff = ((size_t)(t - 1) * a.R + r) * NE + (size_t)rank * Pc;
-      const float4* tu = a.traj_u + xoff;
-      const float2* tig = a.traj_ig + xoff;
-      const size_t xprev = ((size_t)(t >= 2 ? t - 2 : 0) * a.R + r) * NE + (size_t)rank * Pc;
       const int32_t* rec = a.traj_ch + ((size_t)(t - 1) * a.R + r) * W;
       const double* coef_next = t > 1 ? tick_coef(a, n - 1, r) : nullptr;
-      const float4* cprev_src = a.traj_u + xprev;
       if (a.stage) {
         // slot t - 3 into the buffer slot t left (read at steps t + 1, t + 2)
         if (t >= 3 && tid == 0) {
@@ -272,31 +333,15 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         }
         stage_wait(t - 1, len);
         if (t >= 2) stage_wait(t - 2, len);
-        tu = st_u + (size_t)((t - 1) % 3) * Pc;
-        tig = st_ig + (size_t)((t - 1) % 3) * Pc;
-        cprev_src = st_u + (size_t)((t >= 2 ? t - 2 : 0) % 3) * Pc;
       } else if (t >= 2 && tid == 0) {
         // the trajectory of the next step (slot t - 2) into L2 while this one runs
         const size_t xn = ((size_t)(t - 2) * a.R + r) * NE + (size_t)rank * Pc;
         l2_prefetch(a.traj_u + xn, (uint32_t)(Pc * sizeof(float4)));
         l2_prefetch(a.traj_ig + xn, (uint32_t)(Pc * sizeof(float2)));
       }
+      const StepPtr sp = step_ptrs(t);
 
       // OWN: the owner state of lambda is in shared memory (else global)
-      // the element's record and trajectory slice, loaded one element ahead
-      struct Pre {
-        float4 at, gb, x;
-        float2 ig;
-      };
-      auto preload = [&](int i) {
-        const float4* gp = reinterpret_cast<const float4*>(geo + i);
-        Pre q;
-        q.at = __ldg(gp);
-        q.gb = __ldg(gp + 1);
-        q.x = tu[i];
-        q.ig = tig[i];
-        return q;
-      };
       auto element = [&](int i, const Pre& pre, auto own) {
         constexpr bool OWN = decltype(own)::value;
         float lx, li, ci;
@@ -400,7 +445,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
                 const float qv = fmaf(w, e.s, wo * so);
                 if (e.kind == 0) {
                   oc = fmaf(-k.jr_scale, qv, oc);
-                  const float cj = k.c0j + tu[oc_code & ch_mask].x;
+                  const float cj = k.c0j + sp.tu[oc_code & ch_mask].x;
                   g[SRS_ADJ_V_RYR] = fmaf(qv * ak.v_cell, cj - c, g[SRS_ADJ_V_RYR]);
                 } else {
                   oc = fmaf(k.jr_scale, qv, oc);
@@ -433,7 +478,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         kadd(L.w, cm.w, k.dt * oy);
         kadd(lnew, ci, k.dt * oi);
         if (t > 1) {
-          const float cprev = (jsr ? k.c0j : k.c0) + cprev_src[i].x;
+          const float cprev = (jsr ? k.c0j : k.c0) + pre.cp;
           const float inj = tick_injection(a, coef_next, (int)(rank * Pc + i));
           nxt[i] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
           if constexpr (OWN) {
@@ -454,38 +499,33 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
       };
       auto element_s = [&](int i, const Pre& q) { element(i, q, std::true_type{}); };
       auto element_g = [&](int i, const Pre& q) { element(i, q, std::false_type{}); };
-      // for_range with the loads of the next element issued before the
-      // current one is computed
-      auto pipe_range = [&](int& idx, int lo, int hi, auto&& f) {
-        const int n = hi - lo;
-        if (idx < n) {
-          Pre cur_p = preload(lo + idx);
-          for (; idx < n; idx += nthr) {
-            Pre nxt_p = cur_p;
-            if (idx + nthr < n) nxt_p = preload(lo + idx + nthr);
-            f(lo + idx, cur_p);
-            cur_p = nxt_p;
+      // the schedule in two phases around the cluster wait; the loads of a
+      // thread's next element are issued before its current one is computed
+      auto sweep = [&](auto&& f) {
+        int q = tid;
+        Pre p = first;
+        if (!have_first && q < n_sched) p = preload(sched[q], sp, t);
+        auto run = [&](int end) {
+          for (; q < end; q += nthr) {
+            Pre nx = p;
+            if (q + nthr < n_sched) nx = preload(sched[q + nthr], sp, t);
+            f((int)sched[q], p);
+            p = nx;
           }
-        }
-        idx -= n;
-      };
-      // interior elements (and the channel elements when they are interior):
-      // interior to their forward partition, hence to this CTA
-      auto sweep = [&](auto&& element) {
-        int idx = tid;
-        for (int j = 0; j < msub; ++j) {
-          const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-          pipe_range(idx, j * P + (a.ch_interior ? 0 : nc), j * P + nc + a.n_int[q], element);
-        }
+        };
+        run(n_pre);
         cl_wait<C>();
-        for (int j = 0; j < msub; ++j) {
-          const int q = rank * msub + j, nc = q == 0 ? n_ch0 : 0;
-          if (!a.ch_interior) pipe_range(idx, j * P, j * P + nc, element);
-          pipe_range(idx, j * P + nc + a.n_int[q], j * P + a.n_local[q], element);
-        }
+        run(n_sched);
       };
       if (a.own_in_smem) sweep(element_s);
       else sweep(element_g);
+      // the first element of the next step (its trajectory slot is resident
+      // without staging; staged slots are waited on at the step's start)
+      have_first = false;
+      if (!a.stage && t > 1 && tid < n_sched) {
+        first = preload(sched[tid], step_ptrs(t - 1), t - 1);
+        have_first = true;
+      }
       __syncthreads();
       cl_arrive<C>();
       // every 16 steps (and at the end) the warp's FP32 sums go into its FP64
