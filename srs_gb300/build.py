@@ -36,6 +36,8 @@ def _units():
     common_cu = [nvcc(), *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
                  "-Xcompiler", "-ffp-contract=off", "-I", CSRC, "-I", INC]
     common_cc = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I", CSRC, "-I", INC]
+    # Every engine that must match the oracle bit for bit is compiled without
+    # FMA contraction; the adjoint (checked to tolerances) contracts.
     return [
         ("k_plain64.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_plain64.cu")]),
         ("k_fp32.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_fp32.cu")]),
@@ -46,7 +48,7 @@ def _units():
         ("srs_capi.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "srs_capi.cu")]),
         ("k_noalloc.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_noalloc.cu")]),
         ("k_linescan.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_linescan.cu")]),
-        ("k_adjoint.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_adjoint.cu")]),
+        ("k_adjoint.o", common_cu + ["-c", os.path.join(CSRC, "k_adjoint.cu")]),
         ("k_mass.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_mass.cu")]),
         ("srs_host.o", common_cc + ["-c", os.path.join(CSRC, "srs_host.cpp")]),
         ("meshgen.o", common_cc + ["-c", os.path.join(CSRC, "meshgen.cpp")]),
