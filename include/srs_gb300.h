@@ -93,6 +93,9 @@ int srs_initial_states(const srs_grid* g, const srs_params* ps, double* states);
 
 /* ---- simulation ---------------------------------------------------------- */
 typedef struct srs_sim srs_sim;
+/* Realizations per simulation: kernels put them on a grid dimension limited
+ * to 65535 blocks. */
+#define SRS_MAX_REALIZATIONS 65535
 typedef struct srs_sim_desc {
   int n_realizations;   /* independent realizations sharing the grid */
   int precision;        /* SRS_FP64 or SRS_FP32 */
@@ -287,7 +290,8 @@ typedef struct srs_adjoint_desc {
   const double* f0;      /* [n_samples] reference fluorescence F0 */
   const double* target;  /* [R][n_steps/tick_every][n_samples], or NULL (zero) */
   int flags;
-  int threads_per_cta;   /* reverse-sweep kernel: 256 or 512 (0: chosen by the library) */
+  int threads_per_cta;   /* reverse-sweep kernel: a multiple of 32 in [64, 512] (0: chosen
+                            by the library) */
   int cta_partitions;    /* forward partitions per reverse-sweep CTA, a divisor of the
                             cluster size (0: chosen by the library) */
 } srs_adjoint_desc;

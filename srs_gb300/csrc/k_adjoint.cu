@@ -557,30 +557,33 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
   if (stall) atomicOr(a.status, 1u);
 }
 
-// Line-scan loss at one tick: F_i = pad_i + sum_q w_q dye(col_q) from the
-// trajectory slot, e_i = F_i / F0_i - 1 - target_i, coef_i = e_i / F0_i
+// Line-scan loss at the ticks of a segment: F_i = base_i + sum_q w_q
+// dye(col_q) with the dye deviation of the trajectory slot (base_i: pad plus
+// the resting dye), e_i = F_i / F0_i - 1 - target_i, coef_i = e_i / F0_i
 // (= dL/dF_i) and the loss term e_i^2 / 2, kept per sample so the host sums
-// them in a fixed order.  One block per (sample, realization).
+// them in a fixed order.  One block per (sample, realization, tick).
 __global__ void k_adj_tick(AdjTickArgs a) {
-  const int i = blockIdx.x, r = blockIdx.y;
-  const float4* U = a.traj_u + (size_t)r * a.n_state;
+  const int i = blockIdx.x, r = blockIdx.y, z = blockIdx.z;
+  // dye deviation: the fourth float of each element's state
+  const float* U = reinterpret_cast<const float*>(a.traj_u + (size_t)z * a.slot_stride +
+                                                  (size_t)r * a.n_state);
   double acc = 0.0;
-  for (int q = a.ptr[i] + threadIdx.x; q < a.ptr[i + 1]; q += blockDim.x) {
-    const int e = a.col[q];
-    acc += a.w[q] * (a.rest_dye[e] + (double)U[e].w);
-  }
+  for (int q = a.ptr[i] + threadIdx.x; q < a.ptr[i + 1]; q += blockDim.x)
+    acc += a.w[q] * (double)__ldg(U + 4 * (size_t)a.col[q] + 3);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ double red[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) red[warp] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double F = a.pad[i];
+    double F = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) F += red[q];
-    const double tg = a.target ? a.target[((size_t)r * a.n_ticks + a.tick) * a.n_samples + i] : 0.0;
+    F += a.base[i];
+    const int tick = a.tick0 + z;
+    const double tg = a.target ? a.target[((size_t)r * a.n_ticks + tick) * a.n_samples + i] : 0.0;
     const double e = F / a.f0[i] - 1.0 - tg;
-    a.coef[(size_t)r * a.n_samples + i] = e / a.f0[i];
-    a.loss[(size_t)r * a.n_samples + i] = 0.5 * e * e;
+    a.coef[((size_t)z * a.R + r) * a.n_samples + i] = e / a.f0[i];
+    a.loss[((size_t)tick * a.R + r) * a.n_samples + i] = 0.5 * e * e;
   }
 }
 
@@ -660,8 +663,16 @@ int adjoint_max_clusters(int C, int threads, size_t smem) {
   }
 }
 
-int launch_adj_tick(const AdjTickArgs& a, int R, cudaStream_t st) {
-  k_adj_tick<<<dim3(a.n_samples, R), 128, 0, st>>>(a);
+int launch_adj_tick(const AdjTickArgs& a, cudaStream_t st) {
+  constexpr int ZMAX = 65535;  // grid z limit: long segments in several launches
+  for (int z0 = 0; z0 < a.n_seg_ticks; z0 += ZMAX) {
+    AdjTickArgs c = a;
+    c.n_seg_ticks = a.n_seg_ticks - z0 < ZMAX ? a.n_seg_ticks - z0 : ZMAX;
+    c.tick0 = a.tick0 + z0;
+    c.traj_u = a.traj_u + (size_t)z0 * a.slot_stride;
+    c.coef = a.coef + (size_t)z0 * a.R * a.n_samples;
+    k_adj_tick<<<dim3(a.n_samples, a.R, c.n_seg_ticks), 128, 0, st>>>(c);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

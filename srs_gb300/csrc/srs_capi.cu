@@ -92,12 +92,14 @@ struct srs_sim {
   double* d_ls_out = nullptr;
   std::vector<int32_t> ls_ptr_h, ls_col_h;  // host copy of the line-scan CSR
   std::vector<double> ls_w_h;
+  std::vector<double> ls_pad_h;
   int ls_version = 0;
   // adjoint (built on first use)
   std::vector<float4> aT_h;  // transposed coefficients, engine order (host)
   float* d_ryr_s_cl = nullptr;
   float* d_ryr_s_js = nullptr;
   int32_t* d_wt_ptr = nullptr;
+  double* d_ls_base = nullptr;  // resting part of each line-scan sample
   int32_t* d_wt_idx = nullptr;
   double* d_wt_w = nullptr;
   int adj_ls_version = -1;
@@ -1121,7 +1123,9 @@ int srs_initial_states(const srs_grid* g, const srs_params* ps, double* states) 
 
 int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* d, srs_sim** out) {
   if (!g || !ps || !d || !out) return fail(SRS_ERR_INPUT, "null argument");
-  if (d->n_realizations <= 0) return fail(SRS_ERR_INPUT, "n_realizations must be positive");
+  if (d->n_realizations <= 0 || d->n_realizations > SRS_MAX_REALIZATIONS)
+    return fail(SRS_ERR_INPUT, "n_realizations must be in [1, " +
+                                   std::to_string(SRS_MAX_REALIZATIONS) + "]");
   if (d->precision != SRS_FP64 && d->precision != SRS_FP32)
     return fail(SRS_ERR_INPUT, "precision must be 64 or 32");
   if (d->engine != SRS_ENGINE_PLAIN && d->engine != SRS_ENGINE_RESIDENT)
@@ -1770,6 +1774,7 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
   s->ls_ptr_h = ptr;
   s->ls_col_h = col;
   s->ls_w_h = w;
+  s->ls_pad_h = pad;
   s->ls_version++;
   LinescanArgs& a = s->ls;
   a.n_samples = ns;
@@ -1894,6 +1899,18 @@ int adjoint_setup(srs_sim* s) {
   SRS_TRY(dev_upload(s, &s->d_wt_ptr, cnt.data(), cnt.size()));
   SRS_TRY(dev_upload(s, &s->d_wt_idx, idx.data(), idx.size()));
   SRS_TRY(dev_upload(s, &s->d_wt_w, wv.data(), wv.size()));
+  // the resting part of every sample, pad + sum_q w_q dye_rest(col_q): the
+  // tick kernels add the trajectory's dye deviations to it
+  std::vector<double> base(ns);
+  for (int i = 0; i < ns; ++i) {
+    double acc = 0.0;
+    for (int q = s->ls_ptr_h[i]; q < s->ls_ptr_h[i + 1]; ++q) {
+      const int j = s->ref_of_eng[s->ls_col_h[q]];
+      if (j >= 0 && s->m.domain[j] == DOMAIN_CYTO) acc += s->ls_w_h[q] * s->rv.dye;
+    }
+    base[i] = s->ls_pad_h[i] + acc;
+  }
+  SRS_TRY(dev_upload(s, &s->d_ls_base, base.data(), base.size()));
   s->adj_ls_version = s->ls_version;
   return SRS_OK;
 }
@@ -2146,8 +2163,9 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     aa.ak.inv_khi = (float)(1.0 / s->p.reals[R_K_D_SL_HI]);
   }
   const int n_ent = 2 * NR + NL;
-  if (d->threads_per_cta != 0 && d->threads_per_cta != 256 && d->threads_per_cta != 512)
-    return fail(SRS_ERR_INPUT, "threads_per_cta must be 256 or 512");
+  if (d->threads_per_cta != 0 &&
+      (d->threads_per_cta % 32 || d->threads_per_cta < 64 || d->threads_per_cta > 512))
+    return fail(SRS_ERR_INPUT, "threads_per_cta must be a multiple of 32 in [64, 512]");
   if (d->cta_partitions < 0 || (d->cta_partitions > 0 && s->C % d->cta_partitions))
     return fail(SRS_ERR_INPUT, "cta_partitions must divide the cluster size");
   // CTA grouping: m forward partitions per CTA (clusters of C/m CTAs), the
@@ -2159,8 +2177,9 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   size_t adj_smem = 0;
   bool best_own = false, best_stage = false;
   double best_cost = 1e300;
-  for (int thr : {256, 512}) {
-    if (d->threads_per_cta && thr != d->threads_per_cta) continue;
+  const std::vector<int> thr_list =
+      d->threads_per_cta ? std::vector<int>{d->threads_per_cta} : std::vector<int>{256, 512};
+  for (int thr : thr_list) {
     for (int m = 1; m <= s->C; ++m) {
       if (s->C % m || (d->cta_partitions && m != d->cta_partitions)) continue;
       const int Ca = s->C / m, Pc = m * s->P_stride;
@@ -2213,10 +2232,11 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   ta.ptr = s->ls.ptr;
   ta.col = s->ls.col;
   ta.w = s->ls.w;
-  ta.pad = s->ls.pad;
   ta.f0 = f0;
   ta.target = target;
-  ta.rest_dye = s->ls.rest_dye;
+  ta.base = s->d_ls_base;
+  ta.R = R;
+  ta.loss = loss;
   for (int64_t k = nseg - 1; k >= 0; --k) {
     const int64_t s0 = k * K;
     const int len = (int)std::min<int64_t>(K, n_steps - s0);
@@ -2224,12 +2244,15 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       SRS_TRY(snap_copy(s, ck[k], false));
       SRS_TRY(traj_launch(len));
     }
-    for (int64_t n = (s0 / te + 1) * te; n <= s0 + len; n += te) {
-      ta.tick = (int32_t)(n / te - 1);
-      ta.loss = loss + (size_t)ta.tick * R * ns;
-      ta.traj_u = traj_u + (size_t)(n - s0) * R * NE;
-      ta.coef = coef + (size_t)(n / te - s0 / te - 1) * R * ns;
-      if (launch_adj_tick(ta, R, s->st)) return fail(SRS_ERR_CUDA, "tick launch failed");
+    // every tick of the segment in one launch
+    const int64_t n1 = (s0 / te + 1) * te;
+    if (n1 <= s0 + len) {
+      ta.tick0 = (int32_t)(n1 / te - 1);
+      ta.n_seg_ticks = (int32_t)((s0 + len - n1) / te + 1);
+      ta.traj_u = traj_u + (size_t)(n1 - s0) * R * NE;
+      ta.slot_stride = (int64_t)te * R * (int64_t)NE;
+      ta.coef = coef + (size_t)(n1 / te - s0 / te - 1) * R * ns;
+      if (launch_adj_tick(ta, s->st)) return fail(SRS_ERR_CUDA, "tick launch failed");
       s->launches++;
     }
     aa.n_steps = len;

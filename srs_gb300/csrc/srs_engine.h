@@ -220,24 +220,26 @@ struct AdjArgs {
 };
 
 struct AdjTickArgs {
-  int32_t n_samples, n_state, n_ticks, tick;
+  int32_t n_samples, n_state, n_ticks, R;
+  int32_t tick0;        // global index of the segment's first tick
+  int32_t n_seg_ticks;  // ticks of the segment (grid z)
+  int64_t slot_stride;  // trajectory elements between consecutive ticks
   const int32_t* ptr;
   const int32_t* col;
   const double* w;
-  const double* pad;
+  const double* base;    // [n_samples] pad + resting dye part
   const double* f0;
   const double* target;  // [R][n_ticks][n_samples] or null
-  const double* rest_dye;
-  const float4* traj_u;  // trajectory slot [R][n_state]
-  double* coef;          // [R][n_samples]
-  double* loss;          // [R][n_samples]: loss terms of this tick
+  const float4* traj_u;  // trajectory slot of the first tick [R][n_state]
+  double* coef;          // [n_seg_ticks][R][n_samples]
+  double* loss;          // [n_ticks][R][n_samples]: loss terms of every tick
 };
 
 size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, bool stage);
 int launch_adjoint(const AdjArgs& a, int C, int n_clusters, int threads, size_t smem,
                    cudaStream_t st);
 int adjoint_max_clusters(int C, int threads, size_t smem);
-int launch_adj_tick(const AdjTickArgs& a, int R, cudaStream_t st);
+int launch_adj_tick(const AdjTickArgs& a, cudaStream_t st);
 
 // Host-side constants (double precision, from the parameter set and the
 // membrane potential V): gating rates and the LCC flux terms.

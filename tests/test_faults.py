@@ -100,6 +100,27 @@ def test_parameter_file_errors(srs, tmp_path):
     assert e.value.status == -2
 
 
+@pytest.mark.parametrize("n", [0, -1, 65536])
+def test_realization_count_out_of_range_is_an_input_error(srs, n):
+    p, _ = params_from_golden(srs, "spark")
+    g = srs.Grid(p, GOLDEN_MESH)
+    with pytest.raises(srs.SrsError) as e:
+        srs.Simulation(g, p, n, srs.FP32, srs.ENGINE_PLAIN)
+    assert e.value.status == -1 and "n_realizations" in str(e.value)
+
+
+def test_unstable_time_step_is_rejected(srs):
+    """D * dt * max|a0| > 1: the explicit step would blow up, refused before
+    any device work."""
+    p, _ = params_from_golden(srs, "spark")
+    g = srs.Grid(p, GOLDEN_MESH)
+    p = p.copy().set(T_STEP=p.reals[srs.R["T_STEP"]] * 1e4)
+    for prec, eng in ((srs.FP64, srs.ENGINE_PLAIN), (srs.FP32, srs.ENGINE_RESIDENT)):
+        with pytest.raises(srs.SrsError) as e:
+            srs.Simulation(g, p, 4, prec, eng)
+        assert e.value.status == -4 and "unstable" in str(e.value)
+
+
 @pytest.mark.gpu
 def test_ryr_with_swapped_domains_is_rejected_by_fp32_engines(srs, mesh_copy):
     """The FP32 engines store Ca relative to each domain's rest and take a
