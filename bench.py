@@ -467,19 +467,24 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rows_bytes = 0
+        t_reset = 0.0
         for _ in range(args.e2e_steps):
-            sim_e.reset()
+            ta = time.perf_counter()
+            sim_e.reset()  # returns after its uploads completed
+            t_reset += time.perf_counter() - ta
             rows, t_end, n_steps = sim_e.run_simulation()
             rows_bytes = sum(r.nbytes for r in rows)
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.e2e_steps)
+        reset_ms = 1e3 * t_reset / args.e2e_steps
         e2e_val = ws * R * S * DT_MS / e2e_s
         row_cap = int(pe.reals[0] / pe.reals[2]) + 8
         d2h = R * row_cap * sim_e.row_width() * 4 + 2 * cfg_e["ctl_bytes"]
 
         e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": cfg_e["reset_h2d_bytes"],
                "d2h_bytes_per_step": d2h,
-               "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)" % (S, rows_bytes)}
+               "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)" % (S, rows_bytes),
+               "reset_ms": reset_ms, "ms_per_step": 1e3 * e2e_s}
 
     # secondary legs: a failure is reported in the line, not fatal to it
     adj = None

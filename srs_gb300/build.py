@@ -88,7 +88,7 @@ def build(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(run, _units()))
     link = [nvcc(), *ARCH, "-shared", "-o", LIB] + [os.path.join(BUILD, o) for o in objs] + [
-        "-lcudart"]
+        "-lcudart", "-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -145,8 +145,8 @@ int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStre
 size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries) {
   size_t b = (size_t)P * (3 * sizeof(float4) + 2 * sizeof(float));
   b += sizeof(ResidentSmemTail);
-  b += (size_t)(NR + 2 * NL + NR) * sizeof(int32_t);
-  b += (size_t)(NR + NL) * sizeof(float);
+  b += (size_t)(NR + 2 * NL + NR) * sizeof(int32_t);  // ryr, lcc, lccv, lattice counts
+  b += (size_t)(2 * NR + 2 * NL) * sizeof(uint32_t);  // channel element offsets, LCC rest
   b = (b + 7) & ~(size_t)7;
   b += (size_t)(NR + NL) * sizeof(double);
   b += (size_t)(n_chtet + 1) * sizeof(int32_t);

@@ -41,25 +41,35 @@ __device__ __forceinline__ float4 resident_nb(const uint32_t* bs, const float4* 
 // Channels arrays hold (kind << 28 | channel) instead of element indices:
 // kind 0 = RyR cleft element, 1 = RyR JSR element, 2 = LCC element.  All of
 // them live in partition 0 (local shared memory of rank 0).
+// Offsets in partition 0 of every channel's elements, and the LCC elements'
+// resting Ca, staged in rank 0's shared memory once per launch: the channel
+// group reads them every step.
+struct ChanSmem {
+  const uint32_t* cl;   // [NR] RyR cleft element
+  const uint32_t* js;   // [NR] RyR JSR element
+  const uint32_t* lc;   // [NL] LCC element
+  const float* lrest;   // [NL] resting Ca of the LCC element
+};
+
 struct ResidentCa {
   const ResidentArgs* a;
   const float4* src;
-  uint32_t mask;
+  ChanSmem cs;
   __device__ double operator()(int e) const {
     int kind = e >> 28, idx = e & 0x0fffffff;
-    uint32_t code;
+    uint32_t off;
     float rest;
     if (kind == 0) {
-      code = a->ryr_cleft_code[idx];
+      off = cs.cl[idx];
       rest = a->k.c0;
     } else if (kind == 1) {
-      code = a->ryr_jsr_code[idx];
+      off = cs.js[idx];
       rest = a->k.c0j;
     } else {
-      code = a->lcc_code[idx];
-      rest = a->lcc_rest[idx];
+      off = cs.lc[idx];
+      rest = cs.lrest[idx];
     }
-    return (double)(src[code & mask].x + rest);
+    return (double)(src[off].x + rest);
   }
 };
 
@@ -79,9 +89,8 @@ __device__ __forceinline__ void group_sync(int n) {
 // every channel element is local (partition 0).
 static __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const float4* src,
                               int32_t* s_ryr, int32_t* s_lcc, int32_t* s_lccv, double* s_res,
-                              int32_t* s_nb, int gl, int ng) {
+                              int32_t* s_nb, const ChanSmem& cs, int gl, int ng) {
   const int NR = a.C.NR, NL = a.C.NL;
-  const uint32_t mask = (1u << a.off_bits) - 1u;
   const srs_gate_consts* g = &a.P_.gc[ctl.vsel];
   const bool coupled = g->ryr_astar_half != 0.0f;
   if (coupled) {
@@ -106,18 +115,18 @@ static __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const 
         no = s_nb[i] & 0xffff;
         nc = s_nb[i] >> 16;
       }
-      float cs = src[a.ryr_cleft_code[i] & mask].x + a.k.c0;
-      float cj = src[a.ryr_jsr_code[i] & mask].x + a.k.c0j;
+      float ca_s = src[cs.cl[i]].x + a.k.c0;
+      float ca_j = src[cs.js[i]].x + a.k.c0j;
       double rr = s_res[i];
-      s_ryr[i] = srs_gate_ryr(g, s_ryr[i], cs, cj, no, nc, &rr, ctl.seed, (uint32_t)i,
+      s_ryr[i] = srs_gate_ryr(g, s_ryr[i], ca_s, ca_j, no, nc, &rr, ctl.seed, (uint32_t)i,
                               (uint64_t)ctl.step);
       s_res[i] = rr;
     } else {
       const int i = q - NR;
-      float cs = src[a.lcc_code[i] & mask].x + a.lcc_rest[i];
+      float ca_l = src[cs.lc[i]].x + cs.lrest[i];
       double rr = s_res[NR + i];
       int st = s_lcc[i], vs = s_lccv[i];
-      srs_gate_lcc(g, &st, &vs, cs, &rr, ctl.seed, (uint32_t)(NR + i), (uint64_t)ctl.step);
+      srs_gate_lcc(g, &st, &vs, ca_l, &rr, ctl.seed, (uint32_t)(NR + i), (uint64_t)ctl.step);
       s_lcc[i] = st;
       s_lccv[i] = vs;
       s_res[NR + i] = rr;
@@ -129,9 +138,9 @@ static __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const 
 // Protocol of step ctl.step (rank 0, warp 0; lane 0 does the work).
 static __device__ void resident_prestep(const ResidentArgs& a, RealCtl& ctl, const float4* src,
                                  int32_t* s_ryr, int32_t* s_lcc, int32_t* s_lccv, int r,
-                                 int write_row_now, int lane) {
+                                 int write_row_now, int lane, const ChanSmem& cs) {
   if (lane == 0) {
-    ResidentCa cab{&a, src, (1u << a.off_bits) - 1u};
+    ResidentCa cab{&a, src, cs};
     float* rows = a.CS.rows + (size_t)r * a.P_.row_cap * a.P_.row_w;
     if (write_row_now && a.P_.run_protocol)
       write_row(a.P_, a.C, ctl, s_ryr, s_lcc, s_lccv, rows, ctl.t, cab);
@@ -158,16 +167,17 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
   int32_t* s_lcc = s_ryr + NR;
   int32_t* s_lccv = s_lcc + NL;
   int32_t* s_nb = s_lccv + NL;
-  float* s_jr = reinterpret_cast<float*>(s_nb + NR);
-  float* s_jl = s_jr + NR;
+  uint32_t* s_ccl = reinterpret_cast<uint32_t*>(s_nb + NR);
+  uint32_t* s_cjs = s_ccl + NR;
+  uint32_t* s_clc = s_cjs + NR;
+  float* s_lrest = reinterpret_cast<float*>(s_clc + NL);
+  const ChanSmem cs{s_ccl, s_cjs, s_clc, s_lrest};
   double* s_res = reinterpret_cast<double*>(
-      (reinterpret_cast<uintptr_t>(s_jl + NL) + 7) & ~(uintptr_t)7);
+      (reinterpret_cast<uintptr_t>(s_lrest + NL) + 7) & ~(uintptr_t)7);
   // channel-entry CSR of partition 0, staged once per launch
   int32_t* s_cptr = reinterpret_cast<int32_t*>(s_res + NCH);
   ChanEntry32* s_clist = reinterpret_cast<ChanEntry32*>(
       (reinterpret_cast<uintptr_t>(s_cptr + a.n_chtet[0] + 1) + 15) & ~(uintptr_t)15);
-  (void)s_jr;
-  (void)s_jl;
 
   uint32_t rank = 0;
   if constexpr (C > 1) {
@@ -197,6 +207,14 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
     const int nnz = a.ch_ptr[n_ch];
     for (int i = tid; i <= n_ch; i += nthr) s_cptr[i] = a.ch_ptr[i];
     for (int i = tid; i < nnz; i += nthr) s_clist[i] = a.ch_list[i];
+    for (int i = tid; i < NR; i += nthr) {
+      s_ccl[i] = a.ryr_cleft_code[i] & off_mask;
+      s_cjs[i] = a.ryr_jsr_code[i] & off_mask;
+    }
+    for (int i = tid; i < NL; i += nthr) {
+      s_clc[i] = a.lcc_code[i] & off_mask;
+      s_lrest[i] = a.lcc_rest[i];
+    }
   }
 
   if (tid < 32) {
@@ -234,7 +252,7 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
     if (chan_warp) {
       // protocol work that precedes the first step of a run
       if (a.prestep_first && !tail->ctl.done)
-        resident_prestep(a, tail->ctl, buf0, s_ryr, s_lcc, s_lccv, r, a.initial_row, lane);
+        resident_prestep(a, tail->ctl, buf0, s_ryr, s_lcc, s_lccv, r, a.initial_row, lane, cs);
       if (lane == 0) tail->done_flag[3] = tail->ctl.done;
     }
     step_barrier<C>();
@@ -305,12 +323,12 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
                 float J = 0.0f;
                 if (e.kind < 2) {
                   if (s_ryr[e.ch]) {
-                    float us = src[a.ryr_cleft_code[e.ch] & off_mask].x;
-                    float uj = src[a.ryr_jsr_code[e.ch] & off_mask].x;
+                    float us = src[s_ccl[e.ch]].x;
+                    float uj = src[s_cjs[e.ch]].x;
                     J = k.jr_scale * ((k.dc0 + uj) - us);
                   }
                 } else if ((s_lcc[e.ch] == 6 || s_lcc[e.ch] == 12) && s_lccv[e.ch] == 2) {
-                  float c = a.lcc_rest[e.ch] + src[i].x;
+                  float c = s_lrest[e.ch] + src[i].x;
                   J = k.lccA[v] * fmaf(c, k.lccE[v], -k.lccB);
                 }
                 flux = fmaf(J, e.s, flux);
@@ -346,7 +364,6 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             immb[i] = imo;
             cmb[i] = cm;
             cib[i] = ci;
-            bad |= !isfinite(out.x);
           }
           idx = i - hi;
         };
@@ -358,14 +375,14 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
               int idx = tid;
               update(idx, 0, n_ch, ng);
               group_sync(ng);  // the group wrote the channel elements itself
-              if (!P_.nogating) resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, tid, ng);
+              if (!P_.nogating) resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, cs, tid, ng);
             }
           } else {
             int idx = tid;
             update(idx, 0, n_ch, nthr);
             __syncthreads();
             if (chan_warp && !P_.nogating)
-              resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, lane, 32);
+              resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, cs, lane, 32);
           }
           if (chan_warp) {
             RealCtl& ctl = tail->ctl;
@@ -374,7 +391,7 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
               ctl.t += P_.dt;
             }
             __syncwarp();
-            resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane);
+            resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane, cs);
             if (lane == 0) tail->done_flag[s & 3] = ctl.done;
           }
         };
@@ -417,7 +434,10 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
     // ---- store the realization ----------------------------------------------
     if (!skip) {
       const float4* fin = cur ? buf1 : buf0;
+      // a non-finite Ca stays non-finite through every later update, so the
+      // end of the launch is where it is looked for
       for (int i = tid; i < n_loc; i += nthr) {
+        bad |= !isfinite(fin[i].x);
         a.M[roff + i] = fin[i];
         a.I[roff + i] = immb[i];
         a.CM[roff + i] = cmb[i];

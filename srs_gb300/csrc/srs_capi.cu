@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "srs_engine.h"
@@ -65,6 +66,7 @@ struct srs_sim {
   int rows_w_alloc = 0;
   int64_t* d_ticks = nullptr;
   double* d_tick_t = nullptr;
+  size_t ticks_cap = 0;  // capacity of d_ticks / d_tick_t (reused across runs)
   unsigned int* d_counters = nullptr;
   Channels ch{};
   Protocol P{};
@@ -761,9 +763,25 @@ int upload_state_range(srs_sim* s, int r0, int r1, const double* S6) {
   if (!hM) return fail(SRS_ERR_NOMEM, "pinned staging allocation failed");
   float* hI = (float*)(hM + NE * nr);
   to_engine_fp32(s, S6, hM, hI);
-  for (int r = 1; r < nr; ++r) {
-    std::memcpy(hM + r * NE, hM, NE * sizeof(float4));
-    std::memcpy(hI + r * NE, hI, NE * sizeof(float));
+  // realization 0's state copied into the others' staging slots by up to 8
+  // host threads (the copy is memory-bound: one thread does not saturate it)
+  auto fill = [&](int ra, int rb) {
+    for (int r = ra; r < rb; ++r) {
+      std::memcpy(hM + r * NE, hM, NE * sizeof(float4));
+      std::memcpy(hI + r * NE, hI, NE * sizeof(float));
+    }
+  };
+  const int nt = std::max(1, std::min({8, (int)std::thread::hardware_concurrency(), (nr - 1) / 16}));
+  if (nt <= 1) {
+    fill(1, nr);
+  } else {
+    std::vector<std::thread> pool;
+    const int chunk = (nr - 1 + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+      const int ra = 1 + t * chunk, rb = std::min(nr, ra + chunk);
+      if (ra < rb) pool.emplace_back(fill, ra, rb);
+    }
+    for (auto& th : pool) th.join();
   }
   SRS_CUDA(cudaMemcpyAsync(s->d_M[0] + (size_t)r0 * NE, hM, NE * nr * sizeof(float4),
                            cudaMemcpyHostToDevice, s->st));
@@ -985,10 +1003,17 @@ int set_schedule(srs_sim* s, const Schedule& sc) {
     ticks.push_back(-1);
     tt.push_back(0.0);
   }
-  SRS_TRY(dev_upload(s, &s->d_ticks, ticks.data(), ticks.size()));
-  SRS_TRY(dev_upload(s, &s->d_tick_t, tt.data(), tt.size()));
+  if (ticks.size() > s->ticks_cap) {
+    SRS_TRY(dev_upload(s, &s->d_ticks, ticks.data(), ticks.size()));
+    SRS_TRY(dev_upload(s, &s->d_tick_t, tt.data(), tt.size()));
+    s->ticks_cap = ticks.size();
+  } else {
+    SRS_CUDA(cudaMemcpy(s->d_ticks, ticks.data(), ticks.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    SRS_CUDA(cudaMemcpy(s->d_tick_t, tt.data(), tt.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   s->P.ticks = s->d_ticks;
   s->P.tick_t = s->d_tick_t;
+  s->P.sched_ver = s->P.sched_ver + 1;  // invalidates the per-realization tick caches
   s->P.n_ticks = (int32_t)sc.tick_steps.size();
   s->P.n_steps = sc.n_steps;
   s->P.clamp_end = sc.clamp_end_step;

@@ -79,7 +79,15 @@ __device__ void prestep(const Protocol& P, const Channels& C, RealCtl& ctl, int3
   }
   if (P.flag_vclamp) ctl.vsel = (n < P.clamp_end) ? 1 : 0;
   if (P.init_ryr != -1 && n < P.hold_end && !ryr[P.init_ryr]) ryr[P.init_ryr] = 1;
-  if (ctl.tick_idx < P.n_ticks && P.ticks[ctl.tick_idx] == n) {
+  // the step of the next tick, read from the schedule once per tick rather
+  // than once per step (a global load on the protocol thread's path)
+  if (ctl.tick_idx < P.n_ticks &&
+      (ctl.tick_cache_ver != P.sched_ver || ctl.tick_cache_idx != ctl.tick_idx)) {
+    ctl.next_tick = P.ticks[ctl.tick_idx];
+    ctl.tick_cache_idx = ctl.tick_idx;
+    ctl.tick_cache_ver = P.sched_ver;
+  }
+  if (ctl.tick_idx < P.n_ticks && ctl.next_tick == n) {
     int n_open = 0;
     double ca_max = 0;
     for (int i = 0; i < C.NR; ++i) {

@@ -23,6 +23,9 @@ struct RealCtl {
   int32_t tick_idx;        // next entry of the tick list
   int32_t vsel;            // 0: default potential, 1: clamp potential
   uint32_t status;         // bit 0: non-finite state seen, bit 1: wait timeout
+  int64_t next_tick;       // ticks[tick_cache_idx] of schedule tick_cache_ver
+  int32_t tick_cache_idx;
+  int32_t tick_cache_ver;  // 0: nothing cached (schedule versions start at 1)
 };
 
 // Protocol and channel constants (cpu/RunSimulation.cpp:436-575, 143-400).
@@ -37,7 +40,7 @@ struct Protocol {
   int32_t flag_vclamp, flag_lcc, lcc_index, init_ryr;
   int32_t flag_fidelity, n_open_max, nogating, ryr_out;
   int32_t row_w;
-  int32_t pad0;
+  int32_t sched_ver;        // version of ticks / tick_t (incremented per upload)
   int64_t row_cap;
   double c_min;
   double dt;
