@@ -4,13 +4,17 @@
 Workload (config 1): the 10,368-element box dyad (12^3 hexahedra, 49 RyRs,
 7 LCCs), DefaultSpark parameters at dt = 9 ns, 1024 independent
 realizations (Philox seeds 1..1024) with FP32 state, run by the resident
-persistent engine.  One bench step = one persistent launch that advances all
-realizations by --launch-steps time steps.
+persistent engine under the reference's RunSimulation protocol for
+DefaultSpark (RyR 24 held open, output rows).  One bench step = one
+persistent launch that advances all realizations by --launch-steps time
+steps.
 
 Metric: simulated spark-ms per wall second (sum over realizations).
-  value      device-resident: CUDA events on the engine's stream around K
-             launches, state already in HBM (1024 x 10,368 x 20 B = 212 MB,
-             larger than the 129 MB L2, so no flush is needed).
+  value      device-resident: one run of W + K launches from the equilibrium
+             state (uploaded before the run); CUDA events on the engine's
+             stream around each launch, the last K summed.  The state
+             (1024 x 10,368 x 20 B = 212 MB) is larger than the 129 MB L2, so
+             no flush is needed.
   e2e        through the public API with host buffers: srs_sim_reset
              (initial state uploaded from pinned host memory) +
              srs_run_simulation (RunSimulation protocol, states rows read
@@ -418,26 +422,32 @@ def run_ours(args):
                      trials=[])
     else:
         tuned = tuner.tune_resident(grid, p, R, seeds=seeds)
-    sim = srs.Simulation(grid, p, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+    # One bench step = one launch of S time steps of the reference's
+    # RunSimulation under the DefaultSpark protocol (RyR 24 held open, output
+    # rows every S steps), from the equilibrium state uploaded by
+    # srs_sim_reset before the run.  The run has W + K launches: the first W
+    # are the warm-up, the last K the timed region, each launch timed on the
+    # device (CUDA events on the engine's stream, srs_run_simulation_timed).
+    W, K = args.warmup, args.steps
+    pr = wl.default_spark_params(T_FINAL=((W + K) * S - 0.5) * DT_MS, OUTPUT_STATES_INTERVAL=S * DT_MS)
+    sim = srs.Simulation(grid, pr, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
                          steps_per_launch=S, cluster_size=tuned["cluster_size"],
                          threads_per_cta=tuned["threads_per_cta"])
     cfg = sim.config()
-    # warm-up launches
-    for _ in range(args.warmup):
-        sim.advance_async(S)
-    sim.synchronize()
+    sim.reset()
     clocks = Clocks(local)
     launches0 = sim.config()["kernel_launches"]
     barrier(dist)
     torch.cuda.synchronize()
     clocks.start()
-    ms = sim.time_advance(args.steps * S)
+    _, _, n_run, launch_ms = sim.run_simulation(timed=True)
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier(dist)
-    launches = sim.config()["kernel_launches"] - launches0
-    if sim.status() & 1:
-        raise SystemExit("non-finite state during the timed region")
+    launches = sim.config()["kernel_launches"] - launches0 - W
+    ms = float(launch_ms[W:].sum())
+    if len(launch_ms) != W + K or int(n_run.min()) != (W + K) * S or int(n_run.max()) != (W + K) * S:
+        raise SystemExit("the run did not make %d launches of %d steps" % (W + K, S))
     ms_max = max_over_ranks(dist, ms)
     sec = ms_max / 1e3
     value = ws * R * args.steps * S * DT_MS / sec
@@ -518,7 +528,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {
                 "workload": "config1: batched box dyad, %d realizations x %d elements "
-                            "(12^3 hexahedra, 49 RyR, 7 LCC), DefaultSpark dt=9ns, FP32 state"
+                            "(12^3 hexahedra, 49 RyR, 7 LCC), DefaultSpark dt=9ns, FP32 state, "
+                            "RunSimulation protocol (RyR 24 held open, a states row per launch)"
                             % (R, n_el),
                 "realizations_per_gpu": R, "elements": n_el, "steps_per_launch": S,
                 "engine": "resident", "cluster_size": cfg["cluster_size"],

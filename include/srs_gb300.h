@@ -149,6 +149,13 @@ typedef struct srs_run_output {
   int64_t* n_steps;
 } srs_run_output;
 int srs_run_simulation(srs_sim* s, srs_run_output* out);
+/* srs_run_simulation that also returns the device time of each of its
+ * time-step launches (CUDA events on the engine's stream around the launch;
+ * set-up and the read-back of rows are outside): launch_ms[i] for the first
+ * max_launches launches, their count in *n_launches.  A launch advances
+ * steps_per_launch steps (resident engine) or up to 4096 (plain engines). */
+int srs_run_simulation_timed(srs_sim* s, srs_run_output* out, float* launch_ms, int max_launches,
+                             int* n_launches);
 
 /* Time-stepping without protocol, for throughput measurement: advances every
  * realization by n_steps (gating on), device-resident, stream-ordered; the

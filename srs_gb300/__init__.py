@@ -179,6 +179,8 @@ _SIGS = {
     "srs_sim_set_globals": (C.c_int, [_P, C.c_double, C.c_double]),
     "srs_explicit_step": (C.c_int, [_P, C.c_int64]),
     "srs_run_simulation": (C.c_int, [_P, C.POINTER(_RunOutput)]),
+    "srs_run_simulation_timed": (C.c_int, [_P, C.POINTER(_RunOutput), C.POINTER(C.c_float), C.c_int,
+                                           C.POINTER(C.c_int)]),
     "srs_sim_advance_async": (C.c_int, [_P, C.c_int64]),
     "srs_sim_synchronize": (C.c_int, [_P]),
     "srs_sim_time_advance": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
@@ -388,8 +390,10 @@ class Simulation:
     def row_width(self):
         return STATES_ROW_BASE + (self.grid.n_ryr if self.params.ints[I["FLAG_RYR_OUT"]] else 0)
 
-    def run_simulation(self, row_capacity=None):
-        """RunSimulation for every realization; returns per-realization rows."""
+    def run_simulation(self, row_capacity=None, timed=False):
+        """RunSimulation for every realization; returns per-realization rows,
+        final times and step counts (and, with timed=True, the device time in
+        ms of each time-step launch)."""
         p = self.params
         if row_capacity is None:
             row_capacity = int(p.reals[R["T_FINAL"]] / p.reals[R["OUTPUT_STATES_INTERVAL"]]) + 8
@@ -402,8 +406,17 @@ class Simulation:
                          n_rows.ctypes.data_as(C.POINTER(C.c_int64)),
                          t_end.ctypes.data_as(C.POINTER(C.c_double)),
                          n_steps.ctypes.data_as(C.POINTER(C.c_int64)))
-        _check(_lib.srs_run_simulation(self._h, C.byref(out)))
-        return [rows[r, :n_rows[r]].copy() for r in range(self.R)], t_end, n_steps
+        if timed:
+            cap = 1 << 16
+            ms = np.zeros(cap, np.float32)
+            n = C.c_int(0)
+            _check(_lib.srs_run_simulation_timed(self._h, C.byref(out),
+                                                 ms.ctypes.data_as(C.POINTER(C.c_float)), cap,
+                                                 C.byref(n)))
+        else:
+            _check(_lib.srs_run_simulation(self._h, C.byref(out)))
+        res = [rows[r, :n_rows[r]].copy() for r in range(self.R)], t_end, n_steps
+        return res + (ms[:min(n.value, cap)].copy(),) if timed else res
 
     def linescan_setup(self, **kw):
         """Line scan along an axis (see srs_linescan_desc); returns sample count."""

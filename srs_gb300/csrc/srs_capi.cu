@@ -1499,10 +1499,44 @@ int run_finish(srs_sim* s, srs_run_output* out, const std::vector<int64_t>& befo
 extern "C" {
 
 int srs_run_simulation(srs_sim* s, srs_run_output* out) {
+  return srs_run_simulation_timed(s, out, nullptr, 0, nullptr);
+}
+
+int srs_run_simulation_timed(srs_sim* s, srs_run_output* out, float* launch_ms, int max_launches,
+                             int* n_launches) {
+  if (launch_ms && max_launches < 0) return fail(SRS_ERR_INPUT, "max_launches must be >= 0");
   if (!s) return fail(SRS_ERR_INPUT, "bad output");
   Schedule sc;
   std::vector<int64_t> before;
   SRS_TRY(run_prepare(s, out, &sc, &before));
+  struct Events {  // destroyed on every return path
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Events() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } evs;
+  cudaEvent_t* ev = evs.e;
+  int n_timed = 0;
+  if (launch_ms) {
+    SRS_CUDA(cudaEventCreate(&ev[0]));
+    SRS_CUDA(cudaEventCreate(&ev[1]));
+  }
+  // device time of the launches between two all-done checks
+  auto t_begin = [&]() -> int {
+    if (launch_ms) SRS_CUDA(cudaEventRecord(ev[0], s->st));
+    return SRS_OK;
+  };
+  auto t_end = [&]() -> int {
+    if (!launch_ms) return SRS_OK;
+    SRS_CUDA(cudaEventRecord(ev[1], s->st));
+    SRS_CUDA(cudaEventSynchronize(ev[1]));
+    float ms = 0.0f;
+    SRS_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    if (n_timed < max_launches) launch_ms[n_timed] = ms;
+    n_timed++;
+    return SRS_OK;
+  };
   bool done = false;
   if (s->d.engine != SRS_ENGINE_RESIDENT) {
     SRS_TRY(plain_prestep(s, 1));
@@ -1513,7 +1547,9 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
       if (n <= 0) break;
       // plain_steps assumes buffer 0 at the start: alternate by the global count
       if (total & 1) return fail(SRS_ERR_STATE, "internal: odd chunk");
+      SRS_TRY(t_begin());
       SRS_TRY(plain_steps(s, n + (n & 1)));
+      SRS_TRY(t_end());
       total += n + (n & 1);
       SRS_TRY(all_done(s, &done));
       if (done) break;
@@ -1523,11 +1559,14 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out) {
     const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
     int first = 1;
     while (!done) {
+      SRS_TRY(t_begin());
       SRS_TRY(resident_launch(s, S, first));
+      SRS_TRY(t_end());
       first = 0;
       SRS_TRY(all_done(s, &done));
     }
   }
+  if (n_launches) *n_launches = n_timed;
   return run_finish(s, out, before);
 }
 

@@ -179,6 +179,24 @@ def test_fp32_resident_run_simulation_matches_plain(srs, proto, cluster, launch)
             assert np.array_equal(a[k], b[k]), (proto, r, k)
 
 
+def test_timed_run_simulation_gives_the_same_run(srs):
+    """srs_run_simulation_timed: the same rows, times and states as
+    srs_run_simulation, one positive device time per launch."""
+    p = golden_params(srs, "spark")
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [51, 52]
+    launch = 700
+    sims = [srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                           cluster_size=2, steps_per_launch=launch) for _ in range(2)]
+    ra, ta, na = sims[0].run_simulation()
+    rb, tb, nb, ms = sims[1].run_simulation(timed=True)
+    for r in range(len(seeds)):
+        assert np.array_equal(ra[r], rb[r])
+        assert ta[r] == tb[r] and na[r] == nb[r]
+        assert np.array_equal(sims[0].get_state(r)["states"], sims[1].get_state(r)["states"])
+    assert len(ms) == -(-int(na.max()) // launch) and np.all(ms > 0)
+
+
 def test_resident_on_config_mesh_matches_plain(srs, box_mesh):
     base, _ = box_mesh
     p = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24,
