@@ -73,7 +73,9 @@ def parse():
     ap.add_argument("--adjoint-realizations", type=int, default=64)
     ap.add_argument("--adjoint-steps", type=int, default=4096)
     ap.add_argument("--no-config2", action="store_true", help="skip the multi-mesh batch leg")
-    ap.add_argument("--only", choices=["adjoint", "config2"], default=None,
+    ap.add_argument("--no-config4", action="store_true", help="skip the large-site leg")
+    ap.add_argument("--config4-steps", type=int, default=4096)
+    ap.add_argument("--only", choices=["adjoint", "config2", "config4"], default=None,
                     help="run one secondary leg alone and print its JSON (profiling)")
     ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
@@ -393,6 +395,51 @@ def config2_batch(srs, args):
             "cluster_sizes": [s.config()["cluster_size"] for s in sims]}
 
 
+def config4_site(srs, args):
+    """Large release site: the multi-site mesh of about a million tets (five
+    clusters of 20 / 40 / 60 / 100 / 150 RyRs, one LCC per 7 RyRs), 32
+    realizations under the DefaultSpark protocol in FP32.  A realization does
+    not fit on chip, so the plain FP32 engine runs it: one fused kernel per
+    time step for all 32 realizations, the state streamed through HBM.  A
+    bounded sample of the 30 ms run: one run of 4096 + --config4-steps
+    steps; the engine advances it in chunks of up to 4096 steps, the first
+    chunk is the warm-up and the others are timed on the device
+    (srs_run_simulation_timed); FP64 total Ca per compartment
+    (srs_sim_total_ca) at the start and the end."""
+    from srs_gb300 import workloads as wl
+    import numpy as np
+    tmp = tempfile.mkdtemp(prefix="srs_c4_")
+    t0 = time.perf_counter()
+    base, rep_ = wl.config4_mesh(tmp)
+    t_gen = time.perf_counter() - t0
+    n, warm = args.config4_steps, 4096
+    p = wl.default_spark_params(T_FINAL=(warm + n - 0.5) * DT_MS, OUTPUT_STATES_INTERVAL=warm * DT_MS)
+    t0 = time.perf_counter()
+    g = srs.Grid(p, base)
+    t_load = time.perf_counter() - t0
+    R = 32
+    sim = srs.Simulation(g, p, R, srs.FP32, srs.ENGINE_PLAIN, seeds=list(range(1, R + 1)))
+    sim.reset()
+    tot0 = sim.total_ca()
+    _, _, n_run, launch_ms = sim.run_simulation(timed=True)
+    tot1 = sim.total_ca()
+    if len(launch_ms) < 2 or int(n_run.min()) != warm + n:
+        raise RuntimeError("config4 run: %d chunks, %d steps" % (len(launch_ms), int(n_run.min())))
+    ms = float(launch_ms[1:].sum())
+    n_el = rep_["n_tets"]
+    alg = n_el * R * n * (48.0 + 44.0 / R)
+    peak, peak_kind = measured_peaks()
+    return {"workload": "config4: multi-site release unit, %d tets (%d RyR in 5 clusters, %d LCC), "
+                        "32 realizations, DefaultSpark protocol, FP32 plain engine, %d timed steps"
+                        % (n_el, rep_["n_ryr"], rep_["n_lcc"], n),
+            "value": R * n * DT_MS / (ms / 1e3), "unit": UNIT, "ms_per_time_step": ms / n,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
+                         "note": "algorithmic 48 + 44/R B per element-step; peak %s" % peak_kind},
+            "mesh_generation_s": t_gen, "mesh_load_s": t_load,
+            "total_ca_start": np.asarray(tot0)[0].tolist(), "total_ca_end": np.asarray(tot1)[0].tolist()}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     dist = dist_init(ws)
@@ -411,7 +458,9 @@ def run_ours(args):
     grid = srs.Grid(p, base)
     if args.only:
         if rank == 0:
-            leg = adjoint_cost(srs, grid, p, args) if args.only == "adjoint" else config2_batch(srs, args)
+            legs = {"adjoint": adjoint_cost, "config2": lambda srs_, g_, p_, a_: config2_batch(srs_, a_),
+                    "config4": lambda srs_, g_, p_, a_: config4_site(srs_, a_)}
+            leg = legs[args.only](srs, grid, p, args)
             print(json.dumps(dict(leg, leg=args.only)))
         return 0
     R, S = args.realizations, args.launch_steps
@@ -516,6 +565,12 @@ def run_ours(args):
             c2 = config2_batch(srs, args)
         except Exception as e:  # noqa: BLE001
             c2 = {"error": "%s: %s" % (type(e).__name__, e)}
+    c4 = None
+    if rank == 0 and not args.no_config4:
+        try:
+            c4 = config4_site(srs, args)
+        except Exception as e:  # noqa: BLE001
+            c4 = {"error": "%s: %s" % (type(e).__name__, e)}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -546,6 +601,7 @@ def run_ours(args):
             "adjoint": adj,
             "plain_one_realization": plain1,
             "config2": c2,
+            "config4": c4,
         }
         print(json.dumps(line))
     if dist is not None:

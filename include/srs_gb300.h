@@ -340,6 +340,33 @@ void srs_box_mesh_default(srs_box_mesh_spec* spec);
 int srs_box_mesh_write(const srs_box_mesh_spec* spec, const char* base, int* report_ints,
                        double* report_max_a0);
 
+/* Multi-site release unit: n_sites cleft footprints over one box, each with a
+ * Poisson-disk RyR cluster of site_ryr[k] channels at least ryr_pitch apart
+ * in a disc of site_radius[k] around (site_x[k], site_y[k]) and one LCC per
+ * 7 RyRs in its footprint (half width site_radius[k] + foot_margin).  JSR
+ * caps over the footprints are joined by JSR sheets (half width sheet_half)
+ * along L-shaped paths between consecutive sites.  In-plane cells are about
+ * h_fine over the footprints and grow by `growth` up to h_max elsewhere; the
+ * cleft and the JSR take n_cleft_z and n_jsr_z layers.  Same six files and
+ * report as srs_box_mesh_write. */
+#define SRS_MAX_SITES 8
+typedef struct srs_multisite_spec {
+  double box_x, box_y, box_z;
+  double h_fine, h_max, growth;
+  double cleft_h, jsr_h;
+  int n_cleft_z, n_jsr_z;
+  double r_trpn;
+  int flag_tt;
+  int n_sites;
+  double site_x[SRS_MAX_SITES], site_y[SRS_MAX_SITES];
+  int site_ryr[SRS_MAX_SITES];
+  double site_radius[SRS_MAX_SITES];
+  double foot_margin, ryr_pitch, ryr_depth, sheet_half;
+  uint64_t seed; /* site k places its RyRs with seed + k, its LCCs with seed + 100 + k */
+} srs_multisite_spec;
+int srs_multisite_mesh_write(const srs_multisite_spec* spec, const char* base, int* report_ints,
+                             double* report_max_a0);
+
 /* ---- allocation-free step ---------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory — a framework that owns every allocation through its own pool, code

@@ -116,6 +116,22 @@ class BoxMeshSpec(C.Structure):
                 ("lcc_half", C.c_double), ("lcc_seed", C.c_uint64), ("seed", C.c_uint64)]
 
 
+MAX_SITES = 8
+
+
+class MultiSiteSpec(C.Structure):
+    """Synthetic multi-site release unit (srs_multisite_spec, csrc/meshgen.cpp)."""
+    _fields_ = [("box_x", C.c_double), ("box_y", C.c_double), ("box_z", C.c_double),
+                ("h_fine", C.c_double), ("h_max", C.c_double), ("growth", C.c_double),
+                ("cleft_h", C.c_double), ("jsr_h", C.c_double),
+                ("n_cleft_z", C.c_int), ("n_jsr_z", C.c_int), ("r_trpn", C.c_double),
+                ("flag_tt", C.c_int), ("n_sites", C.c_int),
+                ("site_x", C.c_double * MAX_SITES), ("site_y", C.c_double * MAX_SITES),
+                ("site_ryr", C.c_int * MAX_SITES), ("site_radius", C.c_double * MAX_SITES),
+                ("foot_margin", C.c_double), ("ryr_pitch", C.c_double), ("ryr_depth", C.c_double),
+                ("sheet_half", C.c_double), ("seed", C.c_uint64)]
+
+
 class LinescanDesc(C.Structure):
     """srs_linescan_desc (linescan/main.cpp:160-225)."""
     _fields_ = [("axis", C.c_int), ("offset1", C.c_double), ("offset2", C.c_double),
@@ -189,6 +205,7 @@ _SIGS = {
     "srs_write_grid_vtk": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
     "srs_box_mesh_default": (None, [C.POINTER(BoxMeshSpec)]),
     "srs_box_mesh_write": (C.c_int, [C.POINTER(BoxMeshSpec), C.c_char_p, _P, _P]),
+    "srs_multisite_mesh_write": (C.c_int, [C.POINTER(MultiSiteSpec), C.c_char_p, _P, _P]),
     "srs_explicit_step_fp64_noalloc": (C.c_int, [C.POINTER(NoallocStep)]),
     "srs_linescan_setup": (C.c_int, [_P, C.POINTER(LinescanDesc), C.POINTER(C.c_int)]),
     "srs_linescan": (C.c_int, [_P, _P, _P]),
@@ -264,6 +281,29 @@ def write_box_mesh(base, spec=None, **kw):
     rep = np.zeros(6, np.int32)
     a0 = np.zeros(1, np.float64)
     _check(_lib.srs_box_mesh_write(C.byref(s), str(base).encode(), _ptr(rep), _ptr(a0)))
+    keys = ("n_tets", "n_faces", "n_nodes", "n_ryr", "n_lcc", "n_jsr_tets")
+    d = {k: int(v) for k, v in zip(keys, rep)}
+    d["max_a0"] = float(a0[0])
+    return d
+
+
+def multisite_mesh_spec(sites, **kw):
+    """srs_multisite_spec for sites = [(x, y, n_ryr, disc_radius), ...] and
+    the scalar fields in kw."""
+    s = MultiSiteSpec()
+    s.n_sites = len(sites)
+    for k, (x, y, n, r) in enumerate(sites):
+        s.site_x[k], s.site_y[k], s.site_ryr[k], s.site_radius[k] = x, y, n, r
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def write_multisite_mesh(base, spec):
+    """Writes the six reference mesh files for a multi-site release unit."""
+    rep = np.zeros(6, np.int32)
+    a0 = np.zeros(1, np.float64)
+    _check(_lib.srs_multisite_mesh_write(C.byref(spec), str(base).encode(), _ptr(rep), _ptr(a0)))
     keys = ("n_tets", "n_faces", "n_nodes", "n_ryr", "n_lcc", "n_jsr_tets")
     d = {k: int(v) for k, v in zip(keys, rep)}
     d["max_a0"] = float(a0[0])

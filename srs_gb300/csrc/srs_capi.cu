@@ -2448,6 +2448,27 @@ void srs_box_mesh_default(srs_box_mesh_spec* spec) {
   std::memcpy(spec, &s, sizeof(s));
 }
 
+int srs_multisite_mesh_write(const srs_multisite_spec* spec, const char* base, int* rep_i,
+                             double* rep_a0) {
+  if (!spec || !base) return fail(SRS_ERR_INPUT, "null argument");
+  static_assert(sizeof(MultiSiteSpec) == sizeof(srs_multisite_spec), "spec layouts differ");
+  MultiSiteSpec s;
+  std::memcpy(&s, spec, sizeof(s));
+  MeshGenReport rep;
+  int rc = meshgen_multisite(s, base, &rep);
+  if (rc) return fail(rc, "multi-site mesh generation failed");
+  if (rep_i) {
+    rep_i[0] = rep.n_tets;
+    rep_i[1] = rep.n_faces;
+    rep_i[2] = rep.n_nodes;
+    rep_i[3] = rep.n_ryr;
+    rep_i[4] = rep.n_lcc;
+    rep_i[5] = rep.n_jsr_tets;
+  }
+  if (rep_a0) *rep_a0 = rep.max_a0;
+  return SRS_OK;
+}
+
 int srs_box_mesh_write(const srs_box_mesh_spec* spec, const char* base, int* rep_i, double* rep_a0) {
   if (!spec || !base) return fail(SRS_ERR_INPUT, "null argument");
   MeshGenSpec s;

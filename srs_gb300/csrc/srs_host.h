@@ -134,6 +134,27 @@ struct MeshGenReport {
 void meshgen_default_spec(MeshGenSpec* s);
 int meshgen_box(const MeshGenSpec& s, const char* base, MeshGenReport* rep);
 
+// Multi-site release unit: several cleft footprints with Poisson-disk RyR
+// clusters over one box (same layout as srs_multisite_spec).
+#ifndef SRS_MAX_SITES
+#define SRS_MAX_SITES 8
+#endif
+struct MultiSiteSpec {
+  double box_x, box_y, box_z;
+  double h_fine, h_max, growth;
+  double cleft_h, jsr_h;
+  int n_cleft_z, n_jsr_z;
+  double r_trpn;
+  int flag_tt;
+  int n_sites;
+  double site_x[SRS_MAX_SITES], site_y[SRS_MAX_SITES];
+  int site_ryr[SRS_MAX_SITES];
+  double site_radius[SRS_MAX_SITES];
+  double foot_margin, ryr_pitch, ryr_depth, sheet_half;
+  uint64_t seed;
+};
+int meshgen_multisite(const MultiSiteSpec& s, const char* base, MeshGenReport* rep);
+
 // Output formats (cpu/OutputFuncs.cpp): one states row and one VTK snapshot.
 int states_row(const Mesh& m, const srs_params& p, const double* ca, const int* ryr_state,
                const int* lcc_state, const int* lccv_state, double V, double t, float* row,

@@ -87,3 +87,25 @@ def config2_protocols(max_a0):
     for p in (leak, trig):
         p.set(T_STEP=stable_dt(p, max_a0))
     return leak, trig
+
+
+# Large release site: a 3 x 3 x 4 um box with five cleft footprints holding
+# Poisson-disk RyR groups of 20 / 40 / 60 / 100 / 150 channels (30 nm minimum
+# spacing, seed 7), one LCC per 7 RyRs, JSR caps joined by 50 nm-thick JSR
+# sheets; about a million tets.  The disc radius follows the config-2 rule
+# (about a third of the disc covered by the exclusion discs).
+CONFIG4_SITES = [(-0.85, -0.80, 20), (0.75, -0.85, 40), (-0.05, 0.05, 60), (-0.80, 0.85, 100),
+                 (0.80, 0.70, 150)]
+
+
+def config4_mesh_spec(h_fine=0.035, h_max=0.2):
+    sites = [(x, y, n, 0.026 * n ** 0.5) for (x, y, n) in CONFIG4_SITES]
+    return srs.multisite_mesh_spec(
+        sites, box_x=3.0, box_y=3.0, box_z=4.0, h_fine=h_fine, h_max=h_max, growth=1.2,
+        cleft_h=0.015, jsr_h=0.050, n_cleft_z=2, n_jsr_z=2, r_trpn=0.2, flag_tt=1,
+        foot_margin=0.05, ryr_pitch=0.030, ryr_depth=0.0075, sheet_half=0.025, seed=7)
+
+
+def config4_mesh(directory, **kw):
+    base = os.path.join(directory, "c4_site")
+    return base, srs.write_multisite_mesh(base, config4_mesh_spec(**kw))

@@ -183,3 +183,65 @@ def test_config2_meshes_have_the_specified_sizes(srs, tmp_path):
         assert leak.reals[srs.R["T_STEP"]] == 9e-6 and trig.reals[srs.R["T_STEP"]] == 9e-6
         g = srs.Grid(leak, base)
         assert g.n_ele == r["n_tets"]
+
+
+def _small_multisite(srs, base):
+    sites = [(-0.5, -0.4, 12, 0.09), (0.45, -0.3, 20, 0.12), (0.0, 0.5, 30, 0.14)]
+    spec = srs.multisite_mesh_spec(
+        sites, box_x=2.0, box_y=2.0, box_z=1.5, h_fine=0.06, h_max=0.3, growth=1.25,
+        cleft_h=0.015, jsr_h=0.050, n_cleft_z=1, n_jsr_z=1, r_trpn=0.2, flag_tt=1,
+        foot_margin=0.05, ryr_pitch=0.030, ryr_depth=0.0075, sheet_half=0.025, seed=3)
+    return srs.write_multisite_mesh(base, spec), sites
+
+
+def test_multisite_mesh_layout(srs, oracle, tmp_path):
+    """Several footprints over one box: every RyR's cleft tet in the cytosol
+    and JSR tet in the JSR, one LCC per 7 RyRs per site, the JSR (caps and
+    sheets) one connected region, a conservative symmetric operator, and the
+    product loader equal to the oracle's restatement."""
+    from oracle import Mesh
+    base = str(tmp_path / "ms")
+    rep, sites = _small_multisite(srs, base)
+    assert rep["n_ryr"] == sum(n for _, _, n, _ in sites)
+    assert rep["n_lcc"] == sum(max(1, round(n / 7)) for _, _, n, _ in sites)
+    p = srs.default_parameters().set(T_STEP=9e-6)
+    g = srs.Grid(p, base)
+    e, ch = g.elements(), g.channels()
+    assert abs(e["V0"].sum() - 2.0 * 2.0 * 1.5) < 1e-6
+    dom = e["domain"]
+    assert np.all(dom[ch["ryr_ele"]] == 0) and np.all(dom[ch["ryr_jsr"]] == 1)
+    aij, nij, _ = g.operator()
+    a, n = aij.reshape(-1, 5), nij.reshape(-1, 4)
+    assert np.max(np.abs(a.sum(1)) / np.abs(a[:, 0])) < 1e-12
+    jsr = np.flatnonzero(dom == 1)
+    seen, stack = {int(jsr[0])}, [int(jsr[0])]
+    while stack:
+        i = stack.pop()
+        for j in n[i]:
+            j = int(j)
+            if j != i and dom[j] == 1 and j not in seen:
+                seen.add(j)
+                stack.append(j)
+    assert len(seen) == len(jsr)
+    m = Mesh(oracle, base, 1, np.array(p.reals[:]))
+    for x, y in zip(g.operator(), m.operator()):
+        assert np.array_equal(x, y)
+    gc, mc = g.channels(), m.channels()
+    for k in gc:
+        assert np.array_equal(gc[k], mc[k]), k
+
+
+def test_config4_mesh_has_the_specified_size(srs, tmp_path):
+    """Large release site: about a million tets, clusters of 20 / 40 / 60 /
+    100 / 150 RyRs with one LCC per 7, stable at dt = 9 ns."""
+    from srs_gb300 import workloads as wl
+    base, rep = wl.config4_mesh(str(tmp_path))
+    assert 0.95e6 < rep["n_tets"] < 1.1e6
+    assert rep["n_ryr"] == 370 and rep["n_lcc"] == 3 + 6 + 9 + 14 + 21
+    p = wl.default_spark_params()
+    g = srs.Grid(p, base)
+    d = max(p.reals[srs.R[k]] for k in ("D_CA", "D_ATP", "D_CMDN", "D_DYE"))
+    assert d * p.reals[srs.R["T_STEP"]] * g.max_diag < 1.0
+    ch = g.channels()
+    dom = g.elements()["domain"]
+    assert np.all(dom[ch["ryr_ele"]] == 0) and np.all(dom[ch["ryr_jsr"]] == 1)
