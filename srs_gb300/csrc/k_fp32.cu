@@ -34,18 +34,17 @@ namespace srs {
 // ===========================================================================
 // Plain FP32 engine
 // ===========================================================================
-__global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
-  const int r = blockIdx.y;
+// One element of one realization: release flux of its channels, then the
+// FP32 update (tet_update).
+__device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int j) {
   RealCtl* ctlp = a.CS.ctl + r;
-  if (ctlp->done) return;
   const int N = a.N;
   const float4* M = a.M_in + (size_t)r * N;
   const float* I = a.I_in + (size_t)r * N;
   float4* Mo = a.M_out + (size_t)r * N;
   float* Io = a.I_out + (size_t)r * N;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < N) {
-    const uint32_t fl = a.flags[j];
+  const uint32_t fl = a.flags[j];
+  {
     float flux = 0.0f;
     if (fl & 4u) {
       const int32_t* ryr = a.CS.ryr + (size_t)r * a.C.NR;
@@ -80,14 +79,13 @@ __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
     a.CI[(size_t)r * N + j] = ci;
     if (!isfinite(out.x)) atomicOr(&ctlp->status, 1u);
   }
-  __shared__ int s_last;
-  __shared__ int32_t s_nb[1024];
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = (atomicAdd(a.counters + r, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
+}
+
+// Gating of one realization's channels from the new state, then the
+// protocol of the next step (one block).
+__device__ __forceinline__ void plain32_gate(const Plain32Args& a, int r, int32_t* s_nb) {
+  RealCtl* ctlp = a.CS.ctl + r;
+  float4* Mo = a.M_out + (size_t)r * a.N;
   RealCtl ctl = *ctlp;
   const float* rest = a.rest_ca;
   auto ca = [&](int e) -> double {
@@ -114,6 +112,47 @@ __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
   }
 }
 
+// Small meshes: one launch per time step.  Grid: x over realizations, y over
+// blocks of 256 elements, so the blocks that run together share the geometry
+// of one element range in L2; the last block of a realization gates.
+__global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
+  const int r = blockIdx.x;
+  if (a.CS.ctl[r].done) return;
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  const uint32_t fl = j < a.N ? a.flags[j] : 0u;
+  if (j < a.N) plain32_element(a, r, j);
+  __shared__ int s_last;
+  __shared__ int32_t s_nb[1024];
+  // The last block of the realization gates its channels from the new Ca of
+  // the channel elements, so blocks holding channel elements make their
+  // writes visible before they count themselves in; the others need not.
+  if (__syncthreads_or((fl & 4u) != 0)) {
+    __threadfence();
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) s_last = (atomicAdd(a.counters + r, 1u) == gridDim.y - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  plain32_gate(a, r, s_nb);
+}
+
+// Large meshes: the element update alone, without the gating code, so it
+// runs at six blocks per SM; k_plain32_gate follows as its own launch.
+__global__ void __launch_bounds__(256, 6) k_plain32_update(Plain32Args a) {
+  const int r = blockIdx.x;
+  if (a.CS.ctl[r].done) return;
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  if (j < a.N) plain32_element(a, r, j);
+}
+
+__global__ void __launch_bounds__(256) k_plain32_gate(Plain32Args a) {
+  const int r = blockIdx.x;
+  if (a.CS.ctl[r].done) return;
+  __shared__ int32_t s_nb[1024];
+  plain32_gate(a, r, s_nb);
+}
+
 __global__ void k_plain32_prestep(Plain32Args a, int write_initial_row) {
   const int r = blockIdx.x;
   if (threadIdx.x != 0) return;
@@ -129,9 +168,17 @@ __global__ void k_plain32_prestep(Plain32Args a, int write_initial_row) {
   a.CS.ctl[r] = ctl;
 }
 
+int plain32_kernels_per_step(const Plain32Args& a) { return a.N >= PLAIN32_SPLIT_N ? 2 : 1; }
+
 int launch_plain32_step(const Plain32Args& a, cudaStream_t st) {
-  dim3 grid((a.N + 255) / 256, a.R);
-  k_plain32_step<<<grid, 256, 0, st>>>(a);
+  if ((a.N + 255) / 256 > 65535) return -1;  // grid y limit: 16.7 M elements
+  dim3 grid(a.R, (a.N + 255) / 256);
+  if (a.N >= PLAIN32_SPLIT_N) {
+    k_plain32_update<<<grid, 256, 0, st>>>(a);
+    k_plain32_gate<<<a.R, 256, 0, st>>>(a);
+  } else {
+    k_plain32_step<<<grid, 256, 0, st>>>(a);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStream_t st) {

@@ -906,6 +906,7 @@ int plain_launch(srs_sim* s, int parity) {
     a.M_out = s->d_M[parity ^ 1];
     a.I_out = s->d_I[parity ^ 1];
     rc = launch_plain32_step(a, s->st);
+    s->launches += plain32_kernels_per_step(a) - 1;
   }
   s->launches++;
   if (rc) return fail(SRS_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(cudaGetLastError()));
@@ -950,9 +951,10 @@ int plain_steps(srs_sim* s, int64_t n) {
       cudaGraphDestroy(g);
       s->graph_plain_len = G;
     }
+    const int per = s->d.precision == SRS_FP64 ? 1 : plain32_kernels_per_step(s->a32);
     while (n - done >= G) {
       SRS_CUDA(cudaGraphLaunch(s->graph_plain, s->st));
-      s->launches += G;
+      s->launches += (int64_t)G * per;
       done += G;
     }
   }

@@ -76,6 +76,10 @@ struct Plain32Args {
   ChanState CS;
   unsigned int* counters;
 };
+// Meshes of at least this many elements take the split form of the plain
+// FP32 step (element update, then gating, as two launches).
+constexpr int PLAIN32_SPLIT_N = 65536;
+int plain32_kernels_per_step(const Plain32Args& a);
 int launch_plain32_step(const Plain32Args& a, cudaStream_t st);
 int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStream_t st);
 

@@ -129,6 +129,35 @@ def test_fp32_plain_bit_exact_with_fp32_oracle(srs, oracle):
         assert np.array_equal(got["lcc"], lcc) and np.array_equal(got["lccv"], lccv)
 
 
+def test_fp32_plain_split_form_bit_exact_with_fp32_oracle(srs, oracle, tmp_path):
+    """Meshes of 65,536 elements and more take the split form of the plain
+    FP32 step (element update and gating as two launches): the same results
+    as the oracle's FP32 restatement."""
+    base = str(tmp_path / "big")
+    rep = srs.write_box_mesh(base, box_x=3.0, box_y=3.0, box_z=3.0, foot_half_x=0.3,
+                             foot_half_y=0.3, n_foot_x=10, n_foot_y=10, n_out_x=6, n_out_y=6,
+                             n_above_z=22)
+    assert rep["n_tets"] >= 65536
+    p = golden_params(srs)
+    g = srs.Grid(p, base)
+    seeds = [61, 62]
+    sim = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    st0 = [sim.get_state(r) for r in range(len(seeds))]
+    n = 48
+    sim.explicit_step(n)
+    assert sim.config()["kernel_launches"] >= 2 * n
+    m = oracle_mesh(oracle, p, base)
+    for r, sd in enumerate(seeds):
+        s0 = st0[r]
+        st = m.to_fp32(s0["states"])
+        ryr, lcc, lccv, res = (s0["ryr"].copy(), s0["lcc"].copy(), s0["lccv"].copy(),
+                               s0["residuals"].copy())
+        m.steps_fp32(st, sd, 0, n, ryr, lcc, lccv, res, gating=True)
+        got = sim.get_state(r)
+        assert np.array_equal(got["states"], m.from_fp32(st))
+        assert np.array_equal(got["ryr"], ryr) and np.array_equal(got["residuals"], res)
+
+
 def test_fp32_plain_within_tolerance_of_fp64(srs):
     p = golden_params(srs, "spark_nogating")
     g = srs.Grid(p, GOLDEN_MESH)
