@@ -289,13 +289,23 @@ def run_reference(args):
     return 0
 
 
+# Parameters of the adjoint leg's target run (+10 %): the diffusion
+# coefficients of Ca and dye, calmodulin / troponin / SL-site buffering, RyR
+# unit flux and SERCA.
+TARGET_PERTURBED = ("D_CA", "D_DYE", "K_ON_CMDN", "K_OFF_CMDN", "K_ON_TRPN", "K_OFF_TRPN",
+                    "B_TOT_SL_HI", "K_D_SL_HI", "V_RYR", "A_P")
+
+
 def adjoint_cost(srs, grid, p, args):
-    """Cost of the pathwise adjoint against the forward pass it differentiates:
-    the config mesh x R realizations, n explicit steps with gating, the x
-    line scan through the cluster sampled every 128 steps, checkpoints every
-    256 steps; wall time of srs_adjoint (checkpointed forward, segment
-    recomputation with trajectory recording, reverse sweep) over wall time of
-    the same n steps of the resident engine."""
+    """Cost of the pathwise adjoint against the forward pass it differentiates
+    (config 3, a bounded sample of its 10 ms): the config mesh x R
+    realizations, n explicit steps with gating, the x line scan through the
+    cluster sampled every 128 steps, the loss the L2 misfit of the
+    realizations' mean dF/F0 trace against the mean trace of a run with the
+    same seeds and the parameters in TARGET_PERTURBED raised by 10 %; wall
+    time of srs_adjoint (forward pass, with checkpoints every 256 steps and
+    segment recomputation, or keeping the whole trajectory; reverse sweep)
+    over wall time of the same n steps of the resident engine."""
     import numpy as np
     import torch
     Ra, n, te = args.adjoint_realizations, args.adjoint_steps, 128
@@ -312,7 +322,26 @@ def adjoint_cost(srs, grid, p, args):
                             pad_res=0.0, pad_min=0.0, pad_max=0.0, domain=(0, 0, 0, 0, 0, 0))
     sim.reset()
     _, f0 = sim.linescan()
-    sim.adjoint(512, te, f0, checkpoint_every=256)  # warm-up: kernels, allocator
+    # target: mean dF/F0 trace of the perturbed run (its own F0), same seeds
+    pt = p.copy()
+    for name in TARGET_PERTURBED:
+        pt.reals[srs.R[name]] *= 1.1
+    simt = srs.Simulation(srs.Grid(pt, grid.mesh_base), pt, Ra, srs.FP32, srs.ENGINE_RESIDENT,
+                          seeds=list(range(1, Ra + 1)), cluster_size=t["cluster_size"],
+                          threads_per_cta=t["threads_per_cta"], steps_per_launch=te)
+    simt.reset()
+    simt.linescan_setup(axis=0, offset1=0.0, offset2=0.1, x_min=-1.0, x_max=1.0, res=0.05,
+                        var_x=0.0289, var_y=0.1154, var_z=0.0289, r_thresh=1.0, f0_pad=0.0,
+                        pad_res=0.0, pad_min=0.0, pad_max=0.0, domain=(0, 0, 0, 0, 0, 0))
+    _, f0t = simt.linescan()
+    target = np.zeros((n // te, ns))
+    for k in range(n // te):
+        simt.advance_async(te)
+        Ft, _ = simt.linescan()
+        target[k] = Ft.mean(0) / f0t - 1.0
+    del simt
+    flags = args.adjoint_flags | srs.ADJ_MEAN_TRACE
+    sim.adjoint(512, te, f0, target[:512 // te], checkpoint_every=256, flags=flags)  # warm-up
     sim.reset()
     sim.time_advance(512)
     sim.reset()
@@ -332,15 +361,17 @@ def adjoint_cost(srs, grid, p, args):
     for K, key in modes:
         sim.reset()
         kw = dict(checkpoint_every=K, threads_per_cta=args.adjoint_threads,
-                  cta_partitions=args.adjoint_partitions, flags=args.adjoint_flags)
-        sim.adjoint(n, te, f0, **kw)  # warm: work buffers of this mode
+                  cta_partitions=args.adjoint_partitions, flags=flags)
+        sim.adjoint(n, te, f0, target, **kw)  # warm: work buffers of this mode
         sim.reset()
         t0 = time.perf_counter()
-        loss, grad, _ = sim.adjoint(n, te, f0, **kw)
+        loss, grad, _ = sim.adjoint(n, te, f0, target, **kw)
         adj = time.perf_counter() - t0
         if not np.isfinite(grad).all():
             raise SystemExit("non-finite adjoint gradient")
-        out[key] = {"adjoint_s": adj, "cost_ratio": adj / fwd}
+        g = grad.sum(0)
+        out[key] = {"adjoint_s": adj, "cost_ratio": adj / fwd, "loss": float(loss[0]),
+                    "grad": {name: float(g[k]) for k, name in enumerate(srs.ADJ_PARAMS)}}
     return out
 
 

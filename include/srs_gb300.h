@@ -290,12 +290,20 @@ enum {
 /* SRS_ADJ_STAGE always stages the slices (the library does not choose it by
  * itself: on the measured meshes it is not faster). */
 #define SRS_ADJ_STAGE 4
+/* SRS_ADJ_MEAN_TRACE: the loss is the misfit of the realizations' mean
+ * trace, L = 1/2 sum_ticks sum_i (mean_r(F_ri) / F0_i - 1 - target_i)^2,
+ * with target [n_steps/tick_every][n_samples] shared by all realizations;
+ * loss[0] receives L (the other entries 0) and grad[r] the part of dL/dtheta
+ * that flows through realization r (their sum is dL/dtheta).  Without it
+ * each realization has its own loss against target[r]. */
+#define SRS_ADJ_MEAN_TRACE 8
 typedef struct srs_adjoint_desc {
   int64_t n_steps;
   int tick_every;
   int checkpoint_every;
   const double* f0;      /* [n_samples] reference fluorescence F0 */
-  const double* target;  /* [R][n_steps/tick_every][n_samples], or NULL (zero) */
+  const double* target;  /* [R][n_steps/tick_every][n_samples] ([n_steps/tick_every]
+                            [n_samples] with SRS_ADJ_MEAN_TRACE), or NULL (zero) */
   int flags;
   int threads_per_cta;   /* reverse-sweep kernel: a multiple of 32 in [64, 512] (0: chosen
                             by the library) */

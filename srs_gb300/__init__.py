@@ -147,6 +147,7 @@ NOALLOC_MAX_REALIZATIONS = 256
 ADJ_LAMBDA_GLOBAL = 1
 ADJ_NO_STAGE = 2
 ADJ_STAGE = 4
+ADJ_MEAN_TRACE = 8
 
 
 class _AdjDesc(C.Structure):
@@ -317,6 +318,7 @@ class Grid:
         h = C.c_void_p()
         _check(_lib.srs_read_grid(C.byref(params), str(mesh_base).encode(), C.byref(h)))
         self._h = h
+        self.mesh_base = str(mesh_base)
         info = _GridInfo()
         _check(_lib.srs_grid_get_info(h, C.byref(info)))
         self.n_ele, self.n_face, self.n_nodes = info.n_ele, info.n_face, info.n_nodes
@@ -490,15 +492,19 @@ class Simulation:
         """srs_adjoint: pathwise gradient of the line-scan dF/F0 loss.
 
         Returns (loss[R], grad[R][N_ADJ] in ADJ_PARAMS order, and
-        dL/d(initial state)[R][6][N] when grad_state is true, else None)."""
+        dL/d(initial state)[R][6][N] when grad_state is true, else None).
+        With flags & ADJ_MEAN_TRACE the loss is that of the realizations'
+        mean trace against target[n_ticks][n_samples]: loss[0] holds it and
+        grad.sum(0) is its gradient."""
         f0 = np.ascontiguousarray(f0, dtype=np.float64)
         if len(f0) != getattr(self, "_ls_n", -1):
             raise ValueError("f0 needs one value per line-scan sample (call linescan_setup first)")
         n_ticks = int(n_steps) // int(tick_every)
         tg = None
         if target is not None:
-            tg = np.ascontiguousarray(np.broadcast_to(target, (self.R, n_ticks, len(f0))),
-                                      dtype=np.float64)
+            shape = ((n_ticks, len(f0)) if int(flags) & ADJ_MEAN_TRACE
+                     else (self.R, n_ticks, len(f0)))
+            tg = np.ascontiguousarray(np.broadcast_to(target, shape), dtype=np.float64)
         loss = np.zeros(self.R)
         grad = np.zeros((self.R, N_ADJ))
         gs = np.zeros((self.R, 6, self.grid.n_ele)) if grad_state else None

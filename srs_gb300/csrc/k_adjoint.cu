@@ -579,11 +579,48 @@ __global__ void k_adj_tick(AdjTickArgs a) {
     double F = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) F += red[q];
     F += a.base[i];
+    if (a.mean_trace) {  // F itself; k_adj_tick_mean forms the loss
+      a.coef[((size_t)z * a.R + r) * a.n_samples + i] = F;
+      return;
+    }
     const int tick = a.tick0 + z;
     const double tg = a.target ? a.target[((size_t)r * a.n_ticks + tick) * a.n_samples + i] : 0.0;
     const double e = F / a.f0[i] - 1.0 - tg;
     a.coef[((size_t)z * a.R + r) * a.n_samples + i] = e / a.f0[i];
     a.loss[((size_t)tick * a.R + r) * a.n_samples + i] = 0.5 * e * e;
+  }
+}
+
+// Mean-trace loss at the ticks of a segment: coef holds F of every
+// realization (k_adj_tick); the mean over the realizations (FP64, fixed
+// order) against the shared target gives e_i, the loss term e_i^2 / 2 (in
+// realization 0's slot) and dL/dF_ri = e_i / (R F0_i) for every r.  One
+// block per (sample, tick).
+__global__ void k_adj_tick_mean(AdjTickArgs a) {
+  const int i = blockIdx.x, z = blockIdx.y;
+  double* Fz = a.coef + (size_t)z * a.R * a.n_samples;
+  double acc = 0.0;
+  for (int r = threadIdx.x; r < a.R; r += blockDim.x) acc += Fz[(size_t)r * a.n_samples + i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double red[32];
+  __shared__ double s_e;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  const int tick = a.tick0 + z;
+  if (threadIdx.x == 0) {
+    double S = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) S += red[q];
+    const double tg = a.target ? a.target[(size_t)tick * a.n_samples + i] : 0.0;
+    const double e = (S / a.R) / a.f0[i] - 1.0 - tg;
+    a.loss[((size_t)tick * a.R) * a.n_samples + i] = 0.5 * e * e;
+    s_e = e;
+  }
+  __syncthreads();
+  const double c = s_e / ((double)a.R * a.f0[i]);
+  for (int r = threadIdx.x; r < a.R; r += blockDim.x) {
+    Fz[(size_t)r * a.n_samples + i] = c;
+    if (r > 0) a.loss[((size_t)tick * a.R + r) * a.n_samples + i] = 0.0;
   }
 }
 
@@ -672,6 +709,7 @@ int launch_adj_tick(const AdjTickArgs& a, cudaStream_t st) {
     c.traj_u = a.traj_u + (size_t)z0 * a.slot_stride;
     c.coef = a.coef + (size_t)z0 * a.R * a.n_samples;
     k_adj_tick<<<dim3(a.n_samples, a.R, c.n_seg_ticks), 128, 0, st>>>(c);
+    if (a.mean_trace) k_adj_tick_mean<<<dim3(a.n_samples, c.n_seg_ticks), 128, 0, st>>>(c);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -2133,13 +2133,15 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   SRS_TRY(sc.get(&loss, (size_t)std::max<int64_t>(n_ticks, 1) * R * ns));  // [tick][R][sample]
   SRS_TRY(sc.get(&f0, (size_t)ns));
   SRS_CUDA(cudaMemcpyAsync(f0, d->f0, sizeof(double) * ns, cudaMemcpyHostToDevice, s->st));
+  const bool mean_trace = (d->flags & SRS_ADJ_MEAN_TRACE) != 0;
+  const size_t tg_rows = mean_trace ? 1 : (size_t)R;  // target per realization or shared
   {
     double* tg;
-    SRS_TRY(sc.get(&tg, (size_t)R * std::max<int64_t>(n_ticks, 1) * ns));
+    SRS_TRY(sc.get(&tg, tg_rows * std::max<int64_t>(n_ticks, 1) * ns));
     if (d->target && n_ticks > 0) target = tg;
   }
   if (target) {
-    SRS_CUDA(cudaMemcpyAsync(target, d->target, sizeof(double) * R * n_ticks * ns,
+    SRS_CUDA(cudaMemcpyAsync(target, d->target, sizeof(double) * tg_rows * n_ticks * ns,
                              cudaMemcpyHostToDevice, s->st));
   }
   s->P.run_protocol = 0;
@@ -2303,6 +2305,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   ta.base = s->d_ls_base;
   ta.R = R;
   ta.loss = loss;
+  ta.mean_trace = mean_trace ? 1 : 0;
   for (int64_t k = nseg - 1; k >= 0; --k) {
     const int64_t s0 = k * K;
     const int len = (int)std::min<int64_t>(K, n_steps - s0);

@@ -237,6 +237,7 @@ struct AdjTickArgs {
   const float4* traj_u;  // trajectory slot of the first tick [R][n_state]
   double* coef;          // [n_seg_ticks][R][n_samples]
   double* loss;          // [n_ticks][R][n_samples]: loss terms of every tick
+  int32_t mean_trace;    // loss on the realizations' mean trace (target [n_ticks][n_samples])
 };
 
 size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, bool stage);

@@ -174,3 +174,43 @@ def test_adjoint_rejects_unsupported_configurations(srs, case):
     with pytest.raises(srs.SrsError) as e:
         s2.adjoint(0, 5, case["f0"])
     assert e.value.status == -1  # SRS_ERR_INPUT
+
+
+def test_mean_trace_loss_matches_fp64_oracle(srs, oracle, case):
+    """SRS_ADJ_MEAN_TRACE: L = 1/2 sum (mean_r F_r / F0 - 1 - target)^2.  Its
+    gradient is the sum over realizations of per-realization gradients whose
+    targets are shifted so that each residual is the mean residual / R; the
+    oracle computes those, with F from the FP64 engine (bit-exact with it)."""
+    from oracle import Mesh
+    p, g, f0 = case["p"], case["g"], case["f0"]
+    R, nt = len(SEEDS), N_STEPS // TICK
+    tgt = np.random.default_rng(5).standard_normal((nt, len(f0))) * 0.01
+    _, sim = _start(srs, p, srs.FP32, srs.ENGINE_RESIDENT)
+    loss, grad, _ = sim.adjoint(N_STEPS, TICK, f0, tgt, checkpoint_every=K,
+                                flags=srs.ADJ_MEAN_TRACE)
+    assert np.all(loss[1:] == 0.0)
+    _, s64 = _start(srs, p, srs.FP64, srs.ENGINE_PLAIN)
+    for r, st in enumerate(case["start"]):
+        s64.set_state(r, st["states"], st["ryr"], st["lcc"], st["lccv"], st["residuals"])
+    F = np.zeros((R, nt, len(f0)))
+    for k in range(nt):
+        s64.explicit_step(TICK)
+        F[:, k, :], _ = s64.linescan()
+    e = F.mean(0) / f0[None, :] - 1.0 - tgt
+    L = 0.5 * float((e * e).sum())
+    assert abs(loss[0] - L) <= 1e-5 * L
+    W, pad = linescan_weights(g)
+    m = Mesh(oracle, GOLDEN_MESH, 1, np.array(p.reals[:]))
+    ints = np.array(p.ints[:], np.int32)
+    go = np.zeros(srs.N_ADJ)
+    scale = np.zeros(srs.N_ADJ)
+    for r, seed in enumerate(SEEDS):
+        st = case["start"][r]
+        shifted = F[r] / f0[None, :] - 1.0 - e / R
+        _, gr = m.adjoint(ints, st["states"], st, seed, N_STEPS, TICK, W, pad, f0, shifted)
+        go += gr
+        scale += np.abs(gr)
+    got = grad.sum(0)
+    for k in range(srs.N_ADJ):
+        if scale[k] > 0:
+            assert abs(got[k] - go[k]) <= 1e-3 * scale[k], (srs.ADJ_PARAMS[k], got[k], go[k])
