@@ -137,11 +137,31 @@ __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
   plain32_gate(a, r, s_nb);
 }
 
+// Bulk prefetch into L2 of [p, p + bytes) within an array that starts on a
+// 16-byte boundary: the span is trimmed inward to 16-byte boundaries.
+__device__ __forceinline__ void prefetch_span(const void* p, size_t bytes) {
+  const uintptr_t b0 = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+  const uintptr_t b1 = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+  if (b1 > b0) l2_prefetch((const void*)b0, (uint32_t)(b1 - b0));
+}
+
 // Large meshes: the element update alone, without the gating code, so it
-// runs at six blocks per SM; k_plain32_gate follows as its own launch.
+// runs at six blocks per SM; k_plain32_gate follows as its own launch.  The
+// first thread of each block asks L2 for the state this realization needs
+// pf_rows element blocks later (about one wave of blocks ahead), so those
+// blocks find it there instead of waiting on DRAM.
 __global__ void __launch_bounds__(256, 6) k_plain32_update(Plain32Args a) {
   const int r = blockIdx.x;
   if (a.CS.ctl[r].done) return;
+  if (threadIdx.x == 0 && a.pf_rows > 0 && blockIdx.y + a.pf_rows < gridDim.y) {
+    const size_t e0 = (size_t)(blockIdx.y + a.pf_rows) * blockDim.x;
+    const size_t n = min((size_t)blockDim.x, (size_t)a.N - e0);
+    const size_t o = (size_t)r * a.N + e0;
+    prefetch_span(a.M_in + o, n * sizeof(float4));
+    prefetch_span(a.CM + o, n * sizeof(float4));
+    prefetch_span(a.I_in + o, n * sizeof(float));
+    prefetch_span(a.CI + o, n * sizeof(float));
+  }
   const int j = blockIdx.y * blockDim.x + threadIdx.x;
   if (j < a.N) plain32_element(a, r, j);
 }

@@ -873,6 +873,13 @@ void refresh_args(srs_sim* s) {
     s->a32.C = s->ch;
     s->a32.CS = cs;
     s->a32.counters = s->d_counters;
+    {
+      // one wave of update blocks (six per SM) ahead, counted in element blocks
+      int dev = 0, n_sm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+      s->a32.pf_rows = std::max(1, (n_sm * 6 + s->R - 1) / s->R);
+    }
     s->a32.k = make_consts32(s);
     s->a32.CM = s->d_CM;
     s->a32.CI = s->d_CI;

@@ -75,6 +75,7 @@ struct Plain32Args {
   Channels C;
   ChanState CS;
   unsigned int* counters;
+  int32_t pf_rows;  // split form: element blocks ahead whose state is prefetched into L2
 };
 // Meshes of at least this many elements take the split form of the plain
 // FP32 step (element update, then gating, as two launches).
