@@ -392,7 +392,11 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
             }
             __syncwarp();
             resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane, cs);
-            if (lane == 0) tail->done_flag[s & 3] = ctl.done;
+            if (lane == 0) {
+              tail->done_flag[s & 3] = ctl.done;
+              // a speculating launch must not end a run before its last step
+              if (spec && ctl.done && s + 1 < a.steps) bad |= 2;
+            }
           }
         };
         // termination decided at the end of step s - 1
@@ -412,13 +416,9 @@ __global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
         int idx = wt;
         if (worker) update(idx, n_ch, n_ch + n_int, wn);
         if (a.ch_interior && rank == 0 && n_ch > 0) channels();
-        if (spec) {
+        if (spec) {  // no termination inside this launch: nothing to read
           cl_wait<C>();
           pending = false;
-          if (finished()) {  // cannot happen when the host allows speculation
-            bad |= 2;
-            break;
-          }
         }
         // boundary elements: some neighbour in another partition
         if (worker) update(idx, n_ch + n_int, n_loc, wn);
