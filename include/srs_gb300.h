@@ -100,7 +100,7 @@ typedef struct srs_sim_desc {
   int n_realizations;   /* independent realizations sharing the grid */
   int precision;        /* SRS_FP64 or SRS_FP32 */
   int engine;           /* SRS_ENGINE_PLAIN or SRS_ENGINE_RESIDENT */
-  int threads_per_cta;  /* 0: chosen by the tuner */
+  int threads_per_cta;  /* resident engine: a multiple of 32 up to 640 (0: 512) */
   int cluster_size;     /* resident engine: CTAs sharing one realization, 0: tuner */
   int steps_per_launch; /* resident engine: time steps per persistent launch, 0: tuner */
   const uint64_t* seeds;/* n_realizations Philox keys; NULL: 1..n_realizations */

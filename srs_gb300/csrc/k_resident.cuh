@@ -153,7 +153,10 @@ static __device__ void resident_prestep(const ResidentArgs& a, RealCtl& ctl, con
 // from, its Ca rate before the rapid-buffer factor and the channel states it
 // uses (the trajectory the adjoint is conditioned on).
 template <int C, bool TRAJ>
-__global__ void __launch_bounds__(768, 1) k_resident32(ResidentArgs a) {
+// At most 640 threads per CTA: two CTAs of up to 320 threads share an SM
+// with up to 96 registers per thread (the tuned configurations), and
+// single-CTA configurations keep the same budget.
+__global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(ResidentArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int P = a.P;
   float4* buf0 = reinterpret_cast<float4*>(smem);

@@ -1205,8 +1205,9 @@ int srs_sim_create(const srs_grid* g, const srs_params* ps, const srs_sim_desc* 
     else {
       // resident: smallest cluster whose partition fits in shared memory
       int threads = d->threads_per_cta > 0 ? d->threads_per_cta : 512;
-      if (threads > 768 || threads % 32)
-        rc = fail(SRS_ERR_INPUT, "resident engine: threads_per_cta must be a multiple of 32, <= 768");
+      if (threads > SRS_RESIDENT_MAX_THREADS || threads % 32)
+        rc = fail(SRS_ERR_INPUT, "resident engine: threads_per_cta must be a multiple of 32, <= " +
+                                     std::to_string(SRS_RESIDENT_MAX_THREADS));
       int C = d->cluster_size;
       if (C <= 0) {
         int dev = 0, optin = 0;

@@ -100,6 +100,9 @@ struct __align__(16) AdjRec {
                    // set: JSR element
 };
 
+// Largest CTA of the resident engine (its kernel's launch bound).
+#define SRS_RESIDENT_MAX_THREADS 640
+
 struct ResidentArgs {
   int32_t R;
   int32_t P;

@@ -25,7 +25,7 @@ def _key(grid, R):
 
 
 def tune_resident(grid, params, R, seeds=None, clusters=(1, 2, 3, 4, 5, 6, 8),
-                  threads=(256, 288, 320, 352, 384, 448, 512, 768), trial_steps=200, repeats=2, use_cache=True,
+                  threads=(256, 288, 320, 352, 384, 448, 512, 640), trial_steps=200, repeats=2, use_cache=True,
                   verbose=False):
     """Returns dict(cluster_size, threads_per_cta, ms_per_step, trials)."""
     key = _key(grid, R)
