@@ -245,3 +245,20 @@ def test_config4_mesh_has_the_specified_size(srs, tmp_path):
     ch = g.channels()
     dom = g.elements()["domain"]
     assert np.all(dom[ch["ryr_ele"]] == 0) and np.all(dom[ch["ryr_jsr"]] == 1)
+
+
+@pytest.mark.parametrize("field,value", [("n_sites", 0), ("n_sites", 9), ("h_fine", 0.0),
+                                         ("h_max", 0.01), ("growth", 1.0), ("n_cleft_z", 0)])
+def test_multisite_spec_errors(srs, tmp_path, field, value):
+    """Invalid multi-site specifications end in SRS_ERR_INPUT before any file
+    is written."""
+    spec = srs.multisite_mesh_spec(
+        [(0.0, 0.0, 10, 0.09)], box_x=1.0, box_y=1.0, box_z=1.0, h_fine=0.05, h_max=0.2,
+        growth=1.25, cleft_h=0.015, jsr_h=0.05, n_cleft_z=1, n_jsr_z=1, r_trpn=0.2, flag_tt=1,
+        foot_margin=0.05, ryr_pitch=0.03, ryr_depth=0.0075, sheet_half=0.025, seed=1)
+    setattr(spec, field, value)
+    base = str(tmp_path / "bad")
+    with pytest.raises(srs.SrsError) as e:
+        srs.write_multisite_mesh(base, spec)
+    assert e.value.status == -1
+    assert not os.path.exists(base + ".ele")
