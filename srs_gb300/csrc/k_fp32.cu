@@ -197,7 +197,9 @@ int launch_plain32_step(const Plain32Args& a, cudaStream_t st) {
     k_plain32_update<<<grid, 256, 0, st>>>(a);
     k_plain32_gate<<<a.R, 256, 0, st>>>(a);
   } else {
-    k_plain32_step<<<grid, 256, 0, st>>>(a);
+    // few realizations: 64-thread blocks spread the step over more SMs
+    const int bs = (size_t)((a.N + 255) / 256) * a.R < 304 ? 64 : 256;
+    k_plain32_step<<<dim3(a.R, (a.N + bs - 1) / bs), bs, 0, st>>>(a);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

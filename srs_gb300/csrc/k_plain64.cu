@@ -136,8 +136,12 @@ __global__ void __launch_bounds__(256) k_plain64_step(Plain64Args a) {
   // ---- last block of this realization: gating + next step's protocol ----
   __shared__ int s_last;
   __shared__ int32_t s_nb[1024];
-  __threadfence();
-  __syncthreads();
+  // the last block gates from the new Ca of the channel elements: blocks
+  // holding channel elements make their writes visible before counting in
+  if (__syncthreads_or(j < N && (a.flags[j] & 4) != 0)) {
+    __threadfence();
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
     unsigned int done = atomicAdd(a.counters + r, 1u);
     s_last = (done == gridDim.x - 1);
@@ -185,8 +189,11 @@ __global__ void k_plain64_prestep(Plain64Args a, int write_initial_row) {
 }
 
 int launch_plain64_step(const Plain64Args& a, cudaStream_t st) {
-  dim3 grid((a.N + 255) / 256, a.R);
-  k_plain64_step<<<grid, 256, 0, st>>>(a);
+  // Few realizations: 64-thread blocks spread the element updates (and their
+  // FP64 arithmetic) over more SMs than 256-thread blocks would.
+  const int bs = (size_t)((a.N + 255) / 256) * a.R < 304 ? 64 : 256;
+  dim3 grid((a.N + bs - 1) / bs, a.R);
+  k_plain64_step<<<grid, bs, 0, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 int launch_plain64_prestep(const Plain64Args& a, int write_initial_row, cudaStream_t st) {
