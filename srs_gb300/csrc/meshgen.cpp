@@ -662,7 +662,9 @@ int meshgen_multisite(const MultiSiteSpec& s, const char* base, MeshGenReport* r
     for (int l = 0; l < n_lcc; ++l) {
       const double x = s.site_x[k] + (2.0 * lrng.uniform() - 1.0) * half[k];
       const double y = s.site_y[k] + (2.0 * lrng.uniform() - 1.0) * half[k];
-      ch.lcc_ele.push_back(nearest_tet(B, {x, y, 0.0}, -1, &cand));
+      const int le = nearest_tet(B, {x, y, 0.0}, -1, &cand);
+      if (le < 0) return SRS_ERR_INPUT;
+      ch.lcc_ele.push_back(le);
     }
   }
   return write_mesh(B, ch, s.flag_tt, base, rep);
