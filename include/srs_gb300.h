@@ -156,6 +156,18 @@ int srs_run_simulation(srs_sim* s, srs_run_output* out);
  * steps_per_launch steps (resident engine) or up to 4096 (plain engines). */
 int srs_run_simulation_timed(srs_sim* s, srs_run_output* out, float* launch_ms, int max_launches,
                              int* n_launches);
+/* srs_run_simulation with the grid files of WriteToGridFiles
+ * (cpu/RunSimulation.cpp:545-549): when OUTPUT_GRID_FLAG is set, the run
+ * stops at every step where the reference writes a grid file and calls
+ * cb(user, n, t, done) with the file index n (1, 2, ...; the initial file is
+ * 0), the time t and done[r] != 0 for realizations already finished (the
+ * reference writes none for them).  The callback may read any realization
+ * (srs_sim_get_state, srs_write_grid_vtk).  Every realization must start at
+ * the same step.  launch_ms / max_launches / n_launches as in
+ * srs_run_simulation_timed (NULL: not timed). */
+typedef void (*srs_grid_callback)(void* user, int64_t n, double t, const int* done);
+int srs_run_simulation_grid(srs_sim* s, srs_run_output* out, srs_grid_callback cb, void* user,
+                            float* launch_ms, int max_launches, int* n_launches);
 
 /* Time-stepping without protocol, for throughput measurement: advances every
  * realization by n_steps (gating on), device-resident, stream-ordered; the

@@ -119,6 +119,9 @@ class BoxMeshSpec(C.Structure):
 MAX_SITES = 8
 
 
+_GRID_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_int))
+
+
 class MultiSiteSpec(C.Structure):
     """Synthetic multi-site release unit (srs_multisite_spec, csrc/meshgen.cpp)."""
     _fields_ = [("box_x", C.c_double), ("box_y", C.c_double), ("box_z", C.c_double),
@@ -198,6 +201,8 @@ _SIGS = {
     "srs_run_simulation": (C.c_int, [_P, C.POINTER(_RunOutput)]),
     "srs_run_simulation_timed": (C.c_int, [_P, C.POINTER(_RunOutput), C.POINTER(C.c_float), C.c_int,
                                            C.POINTER(C.c_int)]),
+    "srs_run_simulation_grid": (C.c_int, [_P, C.POINTER(_RunOutput), C.c_void_p, C.c_void_p,
+                                          C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "srs_sim_advance_async": (C.c_int, [_P, C.c_int64]),
     "srs_sim_synchronize": (C.c_int, [_P]),
     "srs_sim_time_advance": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
@@ -432,10 +437,12 @@ class Simulation:
     def row_width(self):
         return STATES_ROW_BASE + (self.grid.n_ryr if self.params.ints[I["FLAG_RYR_OUT"]] else 0)
 
-    def run_simulation(self, row_capacity=None, timed=False):
+    def run_simulation(self, row_capacity=None, timed=False, grid_callback=None):
         """RunSimulation for every realization; returns per-realization rows,
         final times and step counts (and, with timed=True, the device time in
-        ms of each time-step launch)."""
+        ms of each time-step launch).  grid_callback(n, t, done) is called at
+        every grid-file step when OUTPUT_GRID_FLAG is set (done: bool array of
+        the realizations already finished); it may read the simulation."""
         p = self.params
         if row_capacity is None:
             row_capacity = int(p.reals[R["T_FINAL"]] / p.reals[R["OUTPUT_STATES_INTERVAL"]]) + 8
@@ -448,13 +455,20 @@ class Simulation:
                          n_rows.ctypes.data_as(C.POINTER(C.c_int64)),
                          t_end.ctypes.data_as(C.POINTER(C.c_double)),
                          n_steps.ctypes.data_as(C.POINTER(C.c_int64)))
-        if timed:
-            cap = 1 << 16
-            ms = np.zeros(cap, np.float32)
-            n = C.c_int(0)
-            _check(_lib.srs_run_simulation_timed(self._h, C.byref(out),
-                                                 ms.ctypes.data_as(C.POINTER(C.c_float)), cap,
-                                                 C.byref(n)))
+        cb = None
+        if grid_callback is not None:
+            R_ = self.R
+
+            def _cb(user, n, t, done):
+                grid_callback(int(n), float(t), np.ctypeslib.as_array(done, shape=(R_,)).astype(bool))
+            cb = _GRID_CB(_cb)
+        cap = 1 << 16 if timed else 0
+        ms = np.zeros(max(cap, 1), np.float32)
+        n = C.c_int(0)
+        if timed or cb is not None:
+            _check(_lib.srs_run_simulation_grid(
+                self._h, C.byref(out), C.cast(cb, C.c_void_p) if cb is not None else None, None,
+                ms.ctypes.data_as(C.POINTER(C.c_float)) if timed else None, cap, C.byref(n)))
         else:
             _check(_lib.srs_run_simulation(self._h, C.byref(out)))
         res = [rows[r, :n_rows[r]].copy() for r in range(self.R)], t_end, n_steps

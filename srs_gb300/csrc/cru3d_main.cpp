@@ -11,7 +11,7 @@
 // the Philox stream of that realization.  Outputs keep the reference names
 // and formats: <out>/states_<rank>_<index>.out (float32 rows, see
 // cpu/OutputFuncs.cpp:223-350) and grid_<rank>_<index>_<n>.vtk snapshots at
-// the start and end of each realization.
+// the start, at every grid-output interval while it runs, and at its end.
 #include <sys/stat.h>
 
 #include <cstdio>
@@ -22,6 +22,26 @@
 #include <vector>
 
 #include "srs_gb300.h"
+
+// Grid files during the run (cpu/RunSimulation.cpp:545-549): one per
+// running realization at every grid-file step, numbered as the reference's
+// output_counter.
+struct GridOut {
+  srs_sim* s;
+  std::string out;
+  int rank, idx0;
+  std::vector<int> last;  // index of the last grid file written per realization
+};
+static void grid_cb(void* user, int64_t n, double t, const int* done) {
+  GridOut* g = static_cast<GridOut*>(user);
+  for (size_t i = 0; i < g->last.size(); ++i) {
+    if (done[i]) continue;
+    char fn[1024];
+    std::snprintf(fn, sizeof(fn), "%s/grid_%d_%d_%d.vtk", g->out.c_str(), g->rank, g->idx0 + (int)i, (int)n);
+    srs_write_grid_vtk(g->s, (int)i, fn, g->idx0 + (int)i, g->rank, (int)n, t);
+    g->last[i] = (int)n;
+  }
+}
 
 static int die(const char* what, int rc) {
   std::fprintf(stderr, "Error: %s: %s (%s)\n", what, srs_status_string(rc), srs_last_error());
@@ -108,8 +128,9 @@ int main(int argc, char** argv) {
   std::vector<int64_t> n_rows(n_sims), n_steps(n_sims);
   std::vector<double> t_end(n_sims);
   srs_run_output ro{rows.data(), cap, width, n_rows.data(), t_end.data(), n_steps.data()};
+  GridOut go{s, out, rank, idx0, std::vector<int>(n_sims, 0)};
   std::clock_t c0 = std::clock();
-  rc = srs_run_simulation(s, &ro);
+  rc = srs_run_simulation_grid(s, &ro, ps.ints[0] ? grid_cb : nullptr, &go, nullptr, 0, nullptr);
   std::clock_t c1 = std::clock();
   if (rc) return die("running simulation", rc);
   for (int i = 0; i < n_sims; ++i) {
@@ -122,8 +143,10 @@ int main(int argc, char** argv) {
     }
     std::fwrite(&rows[(size_t)i * cap * width], sizeof(float), (size_t)n_rows[i] * width, f);
     std::fclose(f);
-    std::snprintf(fn, sizeof(fn), "%s/grid_%d_%d_%d.vtk", out.c_str(), rank, idx0 + i, 1);
-    if (ps.ints[0]) srs_write_grid_vtk(s, i, fn, idx0 + i, rank, 1, t_end[i]);
+    // the final file takes the next index (cpu/RunSimulation.cpp:582)
+    const int nf = go.last[i] + 1;
+    std::snprintf(fn, sizeof(fn), "%s/grid_%d_%d_%d.vtk", out.c_str(), rank, idx0 + i, nf);
+    if (ps.ints[0]) srs_write_grid_vtk(s, i, fn, idx0 + i, rank, nf, t_end[i]);
   }
   std::printf("Simulation completed in %f secs (rank %d, %d realizations).\n",
               (double)(c1 - c0) / CLOCKS_PER_SEC, rank, n_sims);

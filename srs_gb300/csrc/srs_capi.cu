@@ -1509,11 +1509,16 @@ int run_finish(srs_sim* s, srs_run_output* out, const std::vector<int64_t>& befo
 extern "C" {
 
 int srs_run_simulation(srs_sim* s, srs_run_output* out) {
-  return srs_run_simulation_timed(s, out, nullptr, 0, nullptr);
+  return srs_run_simulation_grid(s, out, nullptr, nullptr, nullptr, 0, nullptr);
 }
 
 int srs_run_simulation_timed(srs_sim* s, srs_run_output* out, float* launch_ms, int max_launches,
                              int* n_launches) {
+  return srs_run_simulation_grid(s, out, nullptr, nullptr, launch_ms, max_launches, n_launches);
+}
+
+int srs_run_simulation_grid(srs_sim* s, srs_run_output* out, srs_grid_callback cb, void* user,
+                            float* launch_ms, int max_launches, int* n_launches) {
   if (launch_ms && max_launches < 0) return fail(SRS_ERR_INPUT, "max_launches must be >= 0");
   if (!s) return fail(SRS_ERR_INPUT, "bad output");
   Schedule sc;
@@ -1547,21 +1552,60 @@ int srs_run_simulation_timed(srs_sim* s, srs_run_output* out, float* launch_ms, 
     n_timed++;
     return SRS_OK;
   };
+  // Grid-file steps (OUTPUT_GRID_FLAG): the launches end there and the
+  // callback sees the state before that step, as WriteToGridFiles does
+  // (cpu/RunSimulation.cpp:545-549).  Realizations advance in lock step, so
+  // they must start from the same step.
+  const bool grid = cb != nullptr && !sc.grid_steps.empty();
+  const int64_t base = before.empty() ? 0 : before[0];
+  if (grid)
+    for (int64_t b : before)
+      if (b != base) return fail(SRS_ERR_STATE, "grid snapshots need every realization at the same step");
+  size_t gi = 0;
+  while (grid && gi < sc.grid_steps.size() && sc.grid_steps[gi] <= base) ++gi;
+  const size_t G = grid ? sc.grid_steps.size() : 0;
+  std::vector<int64_t> since = before;  // steps at the last buffer normalisation
+  auto deliver = [&]() -> int {
+    SRS_TRY(normalize_buffers(s, since));  // the state in buffer 0 for every realization
+    since = ctl_steps(s);
+    std::vector<RealCtl> ctl(s->R);
+    SRS_CUDA(cudaMemcpy(ctl.data(), s->d_ctl, sizeof(RealCtl) * s->R, cudaMemcpyDeviceToHost));
+    std::vector<int> dn(s->R);
+    for (int r = 0; r < s->R; ++r) dn[r] = ctl[r].done != 0;
+    cb(user, (int64_t)gi + 1, sc.grid_times[gi], dn.data());
+    ++gi;
+    return SRS_OK;
+  };
   bool done = false;
+  int64_t cur = base;  // step of the realizations still running
   if (s->d.engine != SRS_ENGINE_RESIDENT) {
     SRS_TRY(plain_prestep(s, 1));
-    int64_t total = 0;
+    int64_t total = 0;  // steps since the last normalisation (buffer parity)
     const int64_t chunk = 4096;
     while (true) {
-      int64_t n = std::min<int64_t>(chunk, sc.n_steps + 1 - total);
+      int64_t n = std::min<int64_t>(chunk, sc.n_steps + 1 - (cur - base));
       if (n <= 0) break;
-      // plain_steps assumes buffer 0 at the start: alternate by the global count
+      bool stop = false;
+      if (gi < G && sc.grid_steps[gi] - cur <= n) {
+        n = sc.grid_steps[gi] - cur;
+        stop = true;
+      } else {
+        n += n & 1;  // whole chunks keep the double-buffer parity
+      }
+      // plain_steps assumes buffer 0 at the start: alternate by the count
       if (total & 1) return fail(SRS_ERR_STATE, "internal: odd chunk");
-      SRS_TRY(t_begin());
-      SRS_TRY(plain_steps(s, n + (n & 1)));
-      SRS_TRY(t_end());
-      total += n + (n & 1);
+      if (n > 0) {
+        SRS_TRY(t_begin());
+        SRS_TRY(plain_steps(s, n));
+        SRS_TRY(t_end());
+        total += n;
+        cur += n;
+      }
       SRS_TRY(all_done(s, &done));
+      if (stop) {
+        SRS_TRY(deliver());
+        total = 0;
+      }
       if (done) break;
     }
   } else {
@@ -1569,15 +1613,21 @@ int srs_run_simulation_timed(srs_sim* s, srs_run_output* out, float* launch_ms, 
     const int S = s->d.steps_per_launch > 0 ? s->d.steps_per_launch : 1000;
     int first = 1;
     while (!done) {
-      SRS_TRY(t_begin());
-      SRS_TRY(resident_launch(s, S, first));
-      SRS_TRY(t_end());
-      first = 0;
+      int steps = S;
+      if (gi < G && sc.grid_steps[gi] - cur < steps) steps = (int)(sc.grid_steps[gi] - cur);
+      if (steps > 0) {
+        SRS_TRY(t_begin());
+        SRS_TRY(resident_launch(s, steps, first));
+        SRS_TRY(t_end());
+        first = 0;
+        cur += steps;
+      }
       SRS_TRY(all_done(s, &done));
+      if (gi < G && cur == sc.grid_steps[gi]) SRS_TRY(deliver());
     }
   }
   if (n_launches) *n_launches = n_timed;
-  return run_finish(s, out, before);
+  return run_finish(s, out, since);
 }
 
 }  // extern "C"

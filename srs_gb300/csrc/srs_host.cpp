@@ -700,6 +700,8 @@ Schedule make_schedule(const srs_params& p, double t0) {
   const double dt = p.reals[R_T_STEP];
   const double T_FINAL = p.reals[R_T_FINAL];
   const double I_states = p.reals[R_OUTPUT_STATES_INTERVAL];
+  const double I_grid = p.reals[R_OUTPUT_GRID_INTERVAL];
+  const bool grid = p.ints[I_OUTPUT_GRID_FLAG] != 0;
   double t = t0, dt_last = 0;
   int64_t n = 0;
   bool clamp = p.ints[I_FLAG_V_CLAMP] != 0;
@@ -707,6 +709,11 @@ Schedule make_schedule(const srs_params& p, double t0) {
   while (t <= T_FINAL) {
     if (clamp && s.clamp_end_step < 0 && !(t <= p.reals[R_T_CLAMP])) s.clamp_end_step = n;
     if (hold && s.hold_end_step < 0 && !(t < p.reals[R_INIT_RYR_HOLD])) s.hold_end_step = n;
+    // grid files are tested first, states rows second (cpu/RunSimulation.cpp:545-553)
+    if (grid && std::floor(t / I_grid) > std::floor((t - dt_last) / I_grid)) {
+      s.grid_steps.push_back(n);
+      s.grid_times.push_back(t);
+    }
     if (std::floor(t / I_states) > std::floor((t - dt_last) / I_states)) {
       s.tick_steps.push_back(n);
       s.tick_times.push_back(t);

@@ -100,6 +100,8 @@ struct Schedule {
   int64_t n_steps = 0;             // steps taken while t <= T_FINAL
   std::vector<int64_t> tick_steps; // steps before which a states row is written
   std::vector<double> tick_times;  // t at those steps
+  std::vector<int64_t> grid_steps; // steps before which a grid file is written (OUTPUT_GRID_FLAG)
+  std::vector<double> grid_times;  // t at those steps
   int64_t clamp_end_step = -1;     // first step with t > T_CLAMP (clamp protocol)
   int64_t hold_end_step = -1;      // first step with t >= INIT_RYR_HOLD
   double t_end = 0.0;              // t after the last step

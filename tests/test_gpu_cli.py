@@ -66,3 +66,32 @@ def test_vtk_snapshot_has_reference_layout(srs, tmp_path):
     assert txt[:2] == ["#", "vtk"]
     assert "UNSTRUCTURED_GRID" in txt and "CELL_DATA" in txt
     assert str(g.n_ele) in txt
+
+
+def test_cru3d_writes_grid_files_during_the_run(srs, tmp_path):
+    """flag_output_grid: grid_<rank>_<index>_<n>.vtk at the start (n = 0), at
+    every grid interval while the realization runs and at its end, numbered
+    as the reference's output_counter (cpu/RunSimulation.cpp:421, 545-549,
+    582)."""
+    import math
+    vals = dict(t_final="0.2", t_step="9", states_interval="0.01", grid_interval="0.045",
+                sims_per_proc="2", ryr_open_init="4", ryr_open_time="0.05",
+                flag_use_clock="false", flag_noflux="true", flag_output_grid="true")
+    param = str(tmp_path / "p.xml")
+    _xml(param, vals)
+    out = str(tmp_path / "out")
+    exe = os.path.join(ROOT, "srs_gb300", "bin", "cru3d")
+    r = subprocess.run([exe, "-param", param, "-mesh", GOLDEN_MESH, "-out", out],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    p = srs.read_parameters(param)
+    dt, T, I = (p.reals[srs.R[k]] for k in ("T_STEP", "T_FINAL", "OUTPUT_GRID_INTERVAL"))
+    t, last, n_grid = 0.0, 0.0, 0
+    while t <= T:
+        n_grid += math.floor(t / I) > math.floor((t - last) / I)
+        t += dt
+        last = dt
+    assert n_grid >= 3
+    for i in range(2):
+        names = sorted(f for f in os.listdir(out) if f.startswith("grid_0_%d_" % i))
+        assert names == sorted("grid_0_%d_%d.vtk" % (i, n) for n in range(n_grid + 2)), names

@@ -226,6 +226,54 @@ def test_timed_run_simulation_gives_the_same_run(srs):
     assert len(ms) == -(-int(na.max()) // launch) and np.all(ms > 0)
 
 
+@pytest.mark.parametrize("engine,prec", [("RESIDENT", 32), ("PLAIN", 32), ("PLAIN", 64)])
+def test_grid_snapshots_during_run(srs, engine, prec):
+    """OUTPUT_GRID_FLAG: the run stops at the reference's grid-file steps
+    (floor(t / OUTPUT_GRID_INTERVAL) increments, cpu/RunSimulation.cpp:545);
+    each snapshot is the state of a run that ends at that step, and the run's
+    own rows and final states are those of a run without snapshots."""
+    import math
+    eng = getattr(srs, "ENGINE_" + engine)
+    pr = srs.FP32 if prec == 32 else srs.FP64
+    p = golden_params(srs, "spark")
+    dt, T = p.reals[srs.R["T_STEP"]], p.reals[srs.R["T_FINAL"]]
+    I = T / 4.3
+    pg = p.copy().set(OUTPUT_GRID_FLAG=1, OUTPUT_GRID_INTERVAL=I)
+    g = srs.Grid(p, GOLDEN_MESH)
+    seeds = [71, 72]
+    kw = dict(seeds=seeds, cluster_size=2, steps_per_launch=300) if engine == "RESIDENT" else dict(seeds=seeds)
+    sim = srs.Simulation(g, pg, len(seeds), pr, eng, **kw)
+    snaps = []
+
+    def cb(n, t, done):
+        snaps.append((n, t, [sim.get_state(r)["states"] for r in range(len(seeds))], done.copy()))
+
+    rows, t_end, nst = sim.run_simulation(grid_callback=cb)
+    steps, times = [], []
+    t, last, n = 0.0, 0.0, 0
+    while t <= T:
+        if math.floor(t / I) > math.floor((t - last) / I):
+            steps.append(n)
+            times.append(t)
+        t += dt
+        last = dt
+        n += 1
+    assert len(steps) >= 3
+    assert [x[0] for x in snaps] == list(range(1, len(steps) + 1))
+    assert [x[1] for x in snaps] == times
+    for (_, _, states, done), gs in zip(snaps, steps):
+        assert not done.any()
+        q = srs.Simulation(g, p.copy().set(T_FINAL=(gs - 0.5) * dt), len(seeds), pr, eng, **kw)
+        q.run_simulation()
+        for r in range(len(seeds)):
+            assert np.array_equal(q.get_state(r)["states"], states[r]), (gs, r)
+    ref = srs.Simulation(g, p, len(seeds), pr, eng, **kw)
+    rows2, t2, n2 = ref.run_simulation()
+    for r in range(len(seeds)):
+        assert np.array_equal(rows[r], rows2[r]) and t_end[r] == t2[r] and nst[r] == n2[r]
+        assert np.array_equal(sim.get_state(r)["states"], ref.get_state(r)["states"])
+
+
 def test_resident_on_config_mesh_matches_plain(srs, box_mesh):
     base, _ = box_mesh
     p = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24,
