@@ -74,8 +74,10 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=4096)
     ap.add_argument("--no-config2", action="store_true", help="skip the multi-mesh batch leg")
     ap.add_argument("--no-config4", action="store_true", help="skip the large-site leg")
+    ap.add_argument("--no-config0", action="store_true", help="skip the single-spark leg")
+    ap.add_argument("--config0-ms", type=float, default=2.0)
     ap.add_argument("--config4-steps", type=int, default=4096)
-    ap.add_argument("--only", choices=["adjoint", "config2", "config4"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "config0", "config2", "config4"], default=None,
                     help="run one secondary leg alone and print its JSON (profiling)")
     ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
@@ -426,6 +428,51 @@ def config2_batch(srs, args):
             "cluster_sizes": [s.config()["cluster_size"] for s in sims]}
 
 
+def config0_spark(srs, args):
+    """Plain single spark (config 0, the reference's CPU-runnable case): the
+    config mesh, one realization in FP64 on the plain engine under the
+    DefaultSpark protocol for --config0-ms, the Fluo-4 line scan along x
+    through the cluster centre (linescan/DefaultScan.xml PSF) sampled every
+    0.01 ms at the run's grid-file steps (srs_run_simulation_grid), and the
+    spark's amplitude (peak F/F0 - 1 at the centre sample), time to peak and
+    full duration at half maximum from it."""
+    from srs_gb300 import workloads as wl
+    import numpy as np
+    tmp = tempfile.mkdtemp(prefix="srs_c0_")
+    base, _ = wl.config_mesh(tmp)
+    T, I = args.config0_ms, 0.01
+    p = wl.default_spark_params(T_FINAL=T, OUTPUT_GRID_FLAG=1, OUTPUT_GRID_INTERVAL=I,
+                                OUTPUT_STATES_INTERVAL=I)
+    g = srs.Grid(p, base)
+    sim = srs.Simulation(g, p, 1, srs.FP64, srs.ENGINE_PLAIN, seeds=[1])
+    sim.reset()
+    ns = sim.linescan_setup(axis=0, offset1=0.0, offset2=0.1, x_min=-1.0, x_max=1.0, res=0.05,
+                            var_x=0.0289, var_y=0.1154, var_z=0.0289, r_thresh=1.0, f0_pad=0.0,
+                            pad_res=0.0, pad_min=0.0, pad_max=0.0, domain=(0, 0, 0, 0, 0, 0))
+    _, f0 = sim.linescan()
+    ts, F = [0.0], [np.ones(ns)]
+
+    def sample(n, t, done):
+        if not done[0]:
+            ts.append(t)
+            F.append(sim.linescan()[0][0] / f0)
+
+    t0 = time.perf_counter()
+    _, _, n_steps, launch_ms = sim.run_simulation(timed=True, grid_callback=sample)
+    wall = time.perf_counter() - t0
+    F = np.array(F)
+    c = F[:, ns // 2] - 1.0
+    k = int(np.argmax(c))
+    half = c >= 0.5 * c[k]
+    fdhm = float(np.sum(half) * I)
+    return {"workload": "config0: config mesh, 1 realization, FP64 plain engine, DefaultSpark, "
+                        "%.3g ms, line scan of %d samples every %.3g ms" % (T, ns, I),
+            "steps": int(n_steps[0]), "device_s": float(launch_ms.sum()) / 1e3, "wall_s": wall,
+            "value": T / wall, "unit": UNIT,
+            "spark": {"amplitude_dF_F0": float(c[k]), "time_to_peak_ms": float(ts[k]),
+                      "fdhm_ms": fdhm}}
+
+
 def config4_site(srs, args):
     """Large release site: the multi-site mesh of about a million tets (five
     clusters of 20 / 40 / 60 / 100 / 150 RyRs, one LCC per 7 RyRs), 32
@@ -490,7 +537,8 @@ def run_ours(args):
     if args.only:
         if rank == 0:
             legs = {"adjoint": adjoint_cost, "config2": lambda srs_, g_, p_, a_: config2_batch(srs_, a_),
-                    "config4": lambda srs_, g_, p_, a_: config4_site(srs_, a_)}
+                    "config4": lambda srs_, g_, p_, a_: config4_site(srs_, a_),
+                    "config0": lambda srs_, g_, p_, a_: config0_spark(srs_, a_)}
             leg = legs[args.only](srs, grid, p, args)
             print(json.dumps(dict(leg, leg=args.only)))
         return 0
@@ -596,6 +644,12 @@ def run_ours(args):
             c2 = config2_batch(srs, args)
         except Exception as e:  # noqa: BLE001
             c2 = {"error": "%s: %s" % (type(e).__name__, e)}
+    c0 = None
+    if rank == 0 and not args.no_config0:
+        try:
+            c0 = config0_spark(srs, args)
+        except Exception as e:  # noqa: BLE001
+            c0 = {"error": "%s: %s" % (type(e).__name__, e)}
     c4 = None
     if rank == 0 and not args.no_config4:
         try:
@@ -633,6 +687,7 @@ def run_ours(args):
             "plain_one_realization": plain1,
             "config2": c2,
             "config4": c4,
+            "config0": c0,
         }
         print(json.dumps(line))
     if dist is not None:
