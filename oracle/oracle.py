@@ -5,7 +5,7 @@
                 cpu/RunSimulation.cpp driven by oracle/ref_harness.cpp
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
-this module, and only as the checker.
+this module, and only to compare against.
 """
 import ctypes as C
 import os

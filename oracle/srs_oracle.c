@@ -1,7 +1,7 @@
 /*
  * srs_oracle.c — CPU oracle of the spark timestep.  TEST INFRASTRUCTURE:
- * only tests/, the smoke check and bench.py's CPU-baseline leg use it, as
- * the checker; the product never does.
+ * only tests/, the smoke check and bench.py's CPU-baseline leg use it, to
+ * compare against; the product never does.
  *
  * Each function restates the reference function it names
  * (mwalker174/srs, cpu/*.cpp) in plain C99, keeping its arithmetic order,

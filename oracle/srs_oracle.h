@@ -2,7 +2,7 @@
  * srs_oracle.h — CPU oracle of the spark timestep (test infrastructure only).
  *
  * A plain-C restatement of the reference path, used by tests/, by the smoke
- * check and by the CPU baseline of bench.py as the checker.  The product
+ * check and by the CPU baseline of bench.py, to compare against.  The product
  * (srs_gb300/) never links, imports or calls it.
  *
  * Two gating modes:

@@ -1040,7 +1040,7 @@ int check_device() {
   cudaDeviceProp prop;
   SRS_CUDA(cudaGetDeviceProperties(&prop, dev));
   if (prop.major != 10 || prop.minor != 3)
-    return fail(SRS_ERR_CUDA, "this build targets sm_103a (GB300); device is sm_" +
+    return fail(SRS_ERR_CUDA, "the library targets sm_103a (GB300); device is sm_" +
                                   std::to_string(prop.major) + std::to_string(prop.minor));
   return SRS_OK;
 }
