@@ -1,6 +1,6 @@
 """The FP64 pathwise adjoint of the oracle against central finite differences.
 
-The oracle's adjoint (oracle/srs_oracle.c, or_adjoint) is the checker of the
+The oracle's adjoint (oracle/srs_oracle.c, or_adjoint) is the reference for the
 device adjoint, so it is itself pinned here: on the golden mesh, from the
 reset state of one realization, 600 explicit steps with Philox gating (or
 none), a line-scan loss at every 100th step, and every parameter whose loss
