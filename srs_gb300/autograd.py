@@ -6,11 +6,14 @@
     loss.backward()                                 # theta.grad from srs_adjoint
 
 The loss is the line-scan dF/F0 loss of srs_adjoint summed over the
-realizations; the initial state of every realization is fixed (taken from a
-reset at the problem's own parameters), so the gradient is the one of the
-explicit-step map conditioned on the recorded gating path.  `loss_fp64`
-evaluates the same loss with the FP64 engine from the same start (common
-random numbers), for finite differences.
+realizations, or with mean_trace=True the misfit of the realizations' mean
+dF/F0 trace against one shared target (SRS_ADJ_MEAN_TRACE); the initial state
+of every realization is fixed (taken from a reset at the problem's own
+parameters), so the gradient is the one of the explicit-step map conditioned
+on the recorded gating path.  `loss_fp64` evaluates the same loss with the
+FP64 engine from the same start (common random numbers), for finite
+differences; `mean_trace_fp64` gives the mean trace itself (e.g. a target
+from perturbed parameters).
 """
 import numpy as np
 import torch
@@ -20,7 +23,7 @@ import srs_gb300 as srs
 
 class AdjointProblem:
     def __init__(self, mesh_base, params, seeds, linescan, n_steps, tick_every, target=None,
-                 checkpoint_every=0, cluster_size=0):
+                 checkpoint_every=0, cluster_size=0, mean_trace=False):
         self.mesh_base = str(mesh_base)
         self.params = params.copy()
         self.seeds = [int(s) for s in seeds]
@@ -31,8 +34,10 @@ class AdjointProblem:
         _, self.f0 = sim.linescan()
         self.start = [sim.get_state(r) for r in range(len(self.seeds))]
         n_ticks = self.n_steps // self.tick_every
-        self.target = (np.zeros((len(self.seeds), n_ticks, len(self.f0))) if target is None
-                       else np.broadcast_to(target, (len(self.seeds), n_ticks, len(self.f0))).copy())
+        self.mean_trace = bool(mean_trace)
+        shape = ((n_ticks, len(self.f0)) if self.mean_trace
+                 else (len(self.seeds), n_ticks, len(self.f0)))
+        self.target = (np.zeros(shape) if target is None else np.broadcast_to(target, shape).copy())
 
     def theta0(self):
         return torch.tensor([self.params.reals[srs.R[n]] for n in srs.ADJ_PARAMS], dtype=torch.float64)
@@ -57,19 +62,34 @@ class AdjointProblem:
     def loss_and_grad(self, theta):
         sim = self._sim(self.params_at(theta), srs.FP32, srs.ENGINE_RESIDENT)
         loss, grad, _ = sim.adjoint(self.n_steps, self.tick_every, self.f0, self.target,
-                                    checkpoint_every=self.checkpoint_every)
+                                    checkpoint_every=self.checkpoint_every,
+                                    flags=srs.ADJ_MEAN_TRACE if self.mean_trace else 0)
         return float(loss.sum()), grad.sum(axis=0)
+
+    def _traces_fp64(self, theta):
+        """dF/F0 of every realization at every tick [R][n_ticks][n_samples]
+        from the FP64 engine (same start, same seeds)."""
+        sim = self._sim(self.params_at(theta), srs.FP64, srs.ENGINE_PLAIN)
+        n_ticks = self.n_steps // self.tick_every
+        out = np.zeros((len(self.seeds), n_ticks, len(self.f0)))
+        for k in range(n_ticks):
+            sim.explicit_step(self.tick_every)
+            F, _ = sim.linescan()
+            out[:, k, :] = F / self.f0[None, :] - 1.0
+        return out
+
+    def mean_trace_fp64(self, theta):
+        """The realizations' mean dF/F0 trace [n_ticks][n_samples] (FP64)."""
+        return self._traces_fp64(theta).mean(axis=0)
 
     def loss_fp64(self, theta):
         """The same loss from the FP64 engine (same start, same seeds)."""
-        sim = self._sim(self.params_at(theta), srs.FP64, srs.ENGINE_PLAIN)
-        L = 0.0
-        for k in range(self.n_steps // self.tick_every):
-            sim.explicit_step(self.tick_every)
-            F, _ = sim.linescan()
-            e = F / self.f0[None, :] - 1.0 - self.target[:, k, :]
-            L += 0.5 * float((e * e).sum())
-        return L
+        tr = self._traces_fp64(theta)
+        if self.mean_trace:
+            e = tr.mean(axis=0) - self.target
+        else:
+            e = tr - self.target
+        return 0.5 * float((e * e).sum())
 
 
 class LinescanLoss(torch.autograd.Function):
