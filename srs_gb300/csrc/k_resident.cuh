@@ -121,6 +121,9 @@ static __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const 
       s_ryr[i] = srs_gate_ryr(g, s_ryr[i], ca_s, ca_j, no, nc, &rr, ctl.seed, (uint32_t)i,
                               (uint64_t)ctl.step);
       s_res[i] = rr;
+      // the RyR hold of the next step's protocol (cpu/RunSimulation.cpp:540-542),
+      // applied here by the lane that gated the channel
+      if (i == a.P_.init_ryr && a.P_.run_protocol && ctl.step + 1 < a.P_.hold_end) s_ryr[i] = 1;
     } else {
       const int i = q - NR;
       float ca_l = src[cs.lc[i]].x + cs.lrest[i];
@@ -276,6 +279,7 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
       // them otherwise.
       cl_arrive<C>();
       bool pending = true;
+      int64_t next_ev = 0;  // channel warp: next step with protocol work (0: the first)
       for (int s = 0; s < a.steps; ++s) {
         const float4* src = cur ? buf1 : buf0;
         float4* dst = cur ? buf0 : buf1;
@@ -394,7 +398,13 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
               ctl.t += P_.dt;
             }
             __syncwarp();
-            resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane, cs);
+            // the protocol runs only at the steps where it has work (the RyR
+            // hold is applied by the gating)
+            if (ctl.step >= next_ev) {
+              resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane, cs);
+              if (lane == 0) next_ev = protocol_next_event(P_, ctl, !P_.nogating);
+              next_ev = __shfl_sync(0xffffffffu, next_ev, 0);
+            }
             if (lane == 0) {
               tail->done_flag[s & 3] = ctl.done;
               // a speculating launch must not end a run before its last step

@@ -102,6 +102,28 @@ __device__ void prestep(const Protocol& P, const Channels& C, RealCtl& ctl, int3
   }
 }
 
+// The next step at which prestep has work for this realization: the end of
+// the run (and every later step once done: never), the next output tick, the
+// LCC closing, the end of the voltage clamp, and -- unless the caller forces
+// the initial RyR open itself -- every step of the RyR hold.  Between two
+// such steps prestep changes nothing.
+__device__ __forceinline__ int64_t protocol_next_event(const Protocol& P, const RealCtl& ctl,
+                                                       bool hold_elsewhere) {
+  const int64_t never = INT64_MAX;
+  if (ctl.done || !P.run_protocol) return never;
+  const int64_t n = ctl.step;
+  int64_t e = P.n_steps;
+  if (ctl.tick_idx < P.n_ticks) {
+    // a cache entry for another tick or schedule: look again next step
+    const bool fresh = ctl.tick_cache_ver == P.sched_ver && ctl.tick_cache_idx == ctl.tick_idx;
+    e = min(e, fresh ? ctl.next_tick : n + 1);
+  }
+  if (P.flag_lcc && ctl.lcc_open && ctl.lcc_close_step >= 0) e = min(e, ctl.lcc_close_step);
+  if (P.flag_vclamp && n < P.clamp_end) e = min(e, P.clamp_end);
+  if (!hold_elsewhere && P.init_ryr != -1 && n < P.hold_end) e = min(e, n + 1);
+  return max(e, n + 1);
+}
+
 // Gating of every channel of one realization after time step `step`
 // (UpdateChannelGating, cpu/RunSimulation.cpp:656-674), spread over
 // `nlanes` cooperating threads.  Lattice coupling counts are taken from the
