@@ -121,9 +121,6 @@ static __device__ void resident_gate(const ResidentArgs& a, RealCtl& ctl, const 
       s_ryr[i] = srs_gate_ryr(g, s_ryr[i], ca_s, ca_j, no, nc, &rr, ctl.seed, (uint32_t)i,
                               (uint64_t)ctl.step);
       s_res[i] = rr;
-      // the RyR hold of the next step's protocol (cpu/RunSimulation.cpp:540-542),
-      // applied here by the lane that gated the channel
-      if (i == a.P_.init_ryr && a.P_.run_protocol && ctl.step + 1 < a.P_.hold_end) s_ryr[i] = 1;
     } else {
       const int i = q - NR;
       float ca_l = src[cs.lc[i]].x + cs.lrest[i];
@@ -396,10 +393,12 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
             if (lane == 0) {
               ctl.step += 1;
               ctl.t += P_.dt;
+              // the RyR hold of this step's protocol (cpu/RunSimulation.cpp:540-542)
+              if (P_.run_protocol && P_.init_ryr != -1 && ctl.step < P_.hold_end) s_ryr[P_.init_ryr] = 1;
             }
             __syncwarp();
             // the protocol runs only at the steps where it has work (the RyR
-            // hold is applied by the gating)
+            // hold is applied above)
             if (ctl.step >= next_ev) {
               resident_prestep(a, ctl, dst, s_ryr, s_lcc, s_lccv, r, 0, lane, cs);
               if (lane == 0) next_ev = protocol_next_event(P_, ctl, !P_.nogating);
