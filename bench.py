@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--no-config0", action="store_true", help="skip the single-spark leg")
     ap.add_argument("--config0-ms", type=float, default=2.0)
     ap.add_argument("--config4-steps", type=int, default=4096)
+    ap.add_argument("--config4-adjoint-steps", type=int, default=1024,
+                    help="steps of the large-site adjoint sample (0: skip it)")
     ap.add_argument("--only", choices=["adjoint", "config0", "config2", "config4"], default=None,
                     help="run one secondary leg alone and print its JSON (profiling)")
     ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
@@ -507,7 +509,11 @@ def config4_site(srs, args):
     n_el = rep_["n_tets"]
     alg = n_el * R * n * (48.0 + 44.0 / R)
     peak, peak_kind = measured_peaks()
-    return {"workload": "config4: multi-site release unit, %d tets (%d RyR in 5 clusters, %d LCC), "
+    adj = None
+    if args.config4_adjoint_steps > 0:
+        del sim
+        adj = config4_adjoint(srs, base, R, args.config4_adjoint_steps, ms / n)
+    return {"adjoint": adj, "workload": "config4: multi-site release unit, %d tets (%d RyR in 5 clusters, %d LCC), "
                         "32 realizations, DefaultSpark protocol, FP32 plain engine, %d timed steps"
                         % (n_el, rep_["n_ryr"], rep_["n_lcc"], n),
             "value": R * n * DT_MS / (ms / 1e3), "unit": UNIT, "ms_per_time_step": ms / n,
@@ -516,6 +522,66 @@ def config4_site(srs, args):
                          "note": "algorithmic 48 + 44/R B per element-step; peak %s" % peak_kind},
             "mesh_generation_s": t_gen, "mesh_load_s": t_load,
             "total_ca_start": np.asarray(tot0)[0].tolist(), "total_ca_end": np.asarray(tot1)[0].tolist()}
+
+
+def config4_adjoint(srs, base, R, n, fwd_ms_per_step):
+    """The adjoint over the start of the large-site run (the plain FP32
+    engine's reverse sweep, one launch per step, every array in HBM): n steps
+    of the 32 realizations from rest with gating, the x line scan through the
+    central cluster every 128 steps, the mean-trace misfit against the run
+    with TARGET_PERTURBED raised by 10 %.  Wall time of srs_adjoint with
+    segments of 64 steps; the reverse sweep's cost per step follows from it
+    and the forward steps of the call's checkpoint plan (srs_adjoint_plan),
+    and the plan for the first 5 ms projects the whole sweep."""
+    import numpy as np
+    te = 128
+    ls = dict(axis=0, offset1=0.0, offset2=0.1, x_min=-1.0, x_max=1.0, res=0.05, var_x=0.0289,
+              var_y=0.1154, var_z=0.0289, r_thresh=1.0, f0_pad=0.0, pad_res=0.0, pad_min=0.0,
+              pad_max=0.0, domain=(0, 0, 0, 0, 0, 0))
+    seeds = list(range(1, R + 1))
+    from srs_gb300 import workloads as wl
+    p = wl.default_spark_params()
+    pt = p.copy()
+    for name in TARGET_PERTURBED:
+        pt.reals[srs.R[name]] *= 1.1
+    simt = srs.Simulation(srs.Grid(pt, base), pt, R, srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    simt.reset()
+    ns = simt.linescan_setup(**ls)
+    _, f0t = simt.linescan()
+    target = np.zeros((n // te, ns))
+    for k in range(n // te):
+        simt.advance_async(te)
+        Ft, _ = simt.linescan()
+        target[k] = Ft.mean(0) / f0t - 1.0
+    del simt
+    sim = srs.Simulation(srs.Grid(p, base), p, R, srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    sim.linescan_setup(**ls)
+    sim.reset()
+    _, f0 = sim.linescan()
+    K = 64
+    kw = dict(checkpoint_every=K, flags=srs.ADJ_MEAN_TRACE)
+    sim.adjoint(2 * K, te, f0, target[:2 * K // te], **kw)  # warm-up
+    sim.reset()
+    seg, lev, fwd_steps = sim.adjoint_plan(n, te, checkpoint_every=K)
+    t0 = time.perf_counter()
+    loss, grad, _ = sim.adjoint(n, te, f0, target, **kw)
+    adj_s = time.perf_counter() - t0
+    if not np.isfinite(grad).all():
+        raise SystemExit("non-finite adjoint gradient (large site)")
+    rev_ms = max(adj_s * 1e3 - fwd_steps * fwd_ms_per_step, 0.0) / n
+    n5 = int(round(5.0 / DT_MS))
+    seg5, lev5, fwd5 = sim.adjoint_plan(n5, te, checkpoint_every=K)
+    gsum = grad.sum(0)
+    return {"workload": "adjoint over the first %d steps (%.2f us) of the large site, %d realizations, "
+                        "line scan of %d samples every %d steps, mean-trace loss" % (n, n * DT_MS * 1e3, R, ns, te),
+            "segment_steps": seg, "levels": lev, "forward_steps": fwd_steps, "adjoint_s": adj_s,
+            "forward_ms_per_step": fwd_ms_per_step, "reverse_ms_per_step": rev_ms,
+            "cost_ratio": adj_s * 1e3 / (n * fwd_ms_per_step), "loss": float(loss[0]),
+            "grad": {name: float(gsum[k]) for k, name in enumerate(srs.ADJ_PARAMS)},
+            "first_5ms": {"steps": n5, "segment_steps": seg5, "levels": lev5, "forward_steps": fwd5,
+                          "projected_s": (fwd5 * fwd_ms_per_step + n5 * rev_ms) / 1e3,
+                          "projected_cost_ratio": (fwd5 * fwd_ms_per_step + n5 * rev_ms) /
+                                                  (n5 * fwd_ms_per_step)}}
 
 
 def run_ours(args):

@@ -265,13 +265,19 @@ int srs_sim_total_ca(srs_sim* s, double* out);
  * Returned: loss[r], grad[r][SRS_N_ADJ] = dL_r/dtheta (parameter order
  * below, each the derivative with respect to that ParamStruct::Reals entry)
  * and optionally grad_state[r][6][N] = dL_r/d(initial state), reference
- * numbering and species order.  The state is checkpointed every
- * checkpoint_every steps and each segment but the last is recomputed once,
- * recording its trajectory, for the reverse sweep; checkpoint_every = 0
- * keeps the whole trajectory of the forward pass (no recomputation) when it
- * takes at most half of the free device memory and checkpoints every 256
- * steps otherwise.  The simulation is left at the state after n_steps.
- * FP32 resident engine only (SRS_ERR_UNSUPPORTED otherwise). */
+ * numbering and species order.  The run is cut into segments of
+ * checkpoint_every steps; each segment's trajectory is recorded by a forward
+ * pass from a snapshot of its start, then swept in reverse.  With a snapshot
+ * for every segment start (when device memory holds them) each segment but
+ * the last is recomputed once; otherwise snapshots are taken on several
+ * levels (the first forward pass keeps every f^(L-1)-th segment start, the
+ * pass over one such piece every f^(L-2)-th, ...) and the run is recomputed
+ * up to L times.  checkpoint_every = 0 keeps the whole trajectory of the
+ * forward pass (no recomputation) when it takes at most half of the free
+ * device memory, else segments of 256 steps (fewer when 256 recorded steps
+ * would take more than a quarter).  The simulation is left at the state after
+ * n_steps.  FP32 engines: the resident engine, and the plain engine for
+ * meshes too large for it (SRS_ERR_UNSUPPORTED for FP64). */
 #define SRS_N_ADJ 18
 enum {
   SRS_ADJ_D_CA = 0,
@@ -321,6 +327,10 @@ typedef struct srs_adjoint_desc {
                             by the library) */
   int cta_partitions;    /* forward partitions per reverse-sweep CTA, a divisor of the
                             cluster size (0: chosen by the library) */
+  int max_checkpoints;   /* at most this many state snapshots besides the final state
+                            (0: as many as the free device memory holds); fewer
+                            snapshots than segments make the sweep recompute the forward
+                            run on more levels */
 } srs_adjoint_desc;
 typedef struct srs_adjoint_out {
   double* loss;        /* [R] */
@@ -330,6 +340,11 @@ typedef struct srs_adjoint_out {
 /* ParamStruct::Reals index of each gradient entry. */
 int srs_adjoint_param_index(int k);
 int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out);
+/* The plan srs_adjoint would take for d with the device memory free now: the
+ * steps of one recorded segment, the checkpoint levels, and the forward steps
+ * the sweep runs in all (n_steps with one level and the whole trajectory). */
+int srs_adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, int* segment_steps, int* levels,
+                     int64_t* forward_steps);
 
 /* ---- output formats (cpu/OutputFuncs.cpp) -------------------------------- */
 /* WriteToGridFiles (cpu/OutputFuncs.cpp:42-220): legacy ASCII VTK of the

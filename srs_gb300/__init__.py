@@ -156,7 +156,8 @@ ADJ_MEAN_TRACE = 8
 class _AdjDesc(C.Structure):
     _fields_ = [("n_steps", C.c_int64), ("tick_every", C.c_int), ("checkpoint_every", C.c_int),
                 ("f0", C.c_void_p), ("target", C.c_void_p), ("flags", C.c_int),
-                ("threads_per_cta", C.c_int), ("cta_partitions", C.c_int)]
+                ("threads_per_cta", C.c_int), ("cta_partitions", C.c_int),
+                ("max_checkpoints", C.c_int)]
 
 
 class _AdjOut(C.Structure):
@@ -224,6 +225,8 @@ _SIGS = {
     "srs_batch_run_simulation": (C.c_int, [_P, _P]),
     "srs_adjoint_param_index": (C.c_int, [C.c_int]),
     "srs_adjoint": (C.c_int, [_P, C.POINTER(_AdjDesc), C.POINTER(_AdjOut)]),
+    "srs_adjoint_plan": (C.c_int, [_P, C.POINTER(_AdjDesc), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int64)]),
 }
 
 
@@ -502,7 +505,7 @@ class Simulation:
         return out
 
     def adjoint(self, n_steps, tick_every, f0, target=None, checkpoint_every=0, grad_state=False,
-                flags=0, threads_per_cta=0, cta_partitions=0):
+                flags=0, threads_per_cta=0, cta_partitions=0, max_checkpoints=0):
         """srs_adjoint: pathwise gradient of the line-scan dF/F0 loss.
 
         Returns (loss[R], grad[R][N_ADJ] in ADJ_PARAMS order, and
@@ -524,10 +527,20 @@ class Simulation:
         gs = np.zeros((self.R, 6, self.grid.n_ele)) if grad_state else None
         d = _AdjDesc(int(n_steps), int(tick_every), int(checkpoint_every), f0.ctypes.data,
                      tg.ctypes.data if tg is not None else None, int(flags), int(threads_per_cta),
-                     int(cta_partitions))
+                     int(cta_partitions), int(max_checkpoints))
         o = _AdjOut(loss.ctypes.data, grad.ctypes.data, gs.ctypes.data if gs is not None else None)
         _check(_lib.srs_adjoint(self._h, C.byref(d), C.byref(o)))
         return loss, grad, gs
+
+    def adjoint_plan(self, n_steps, tick_every, checkpoint_every=0, max_checkpoints=0):
+        """srs_adjoint_plan: (segment steps, checkpoint levels, forward steps)
+        that srs_adjoint would use now for these settings."""
+        f0 = np.zeros(max(getattr(self, "_ls_n", 1), 1))
+        d = _AdjDesc(int(n_steps), int(tick_every), int(checkpoint_every), f0.ctypes.data, None, 0, 0,
+                     0, int(max_checkpoints))
+        seg, lev, fw = C.c_int(), C.c_int(), C.c_int64()
+        _check(_lib.srs_adjoint_plan(self._h, C.byref(d), C.byref(seg), C.byref(lev), C.byref(fw)))
+        return seg.value, lev.value, fw.value
 
     def write_grid_vtk(self, r, path, run=0, rank=0, n=0, t=0.0):
         _check(_lib.srs_write_grid_vtk(self._h, r, str(path).encode(), run, rank, n, float(t)))

@@ -49,6 +49,7 @@ def _units():
         ("k_noalloc.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_noalloc.cu")]),
         ("k_linescan.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_linescan.cu")]),
         ("k_adjoint.o", common_cu + ["-c", os.path.join(CSRC, "k_adjoint.cu")]),
+        ("k_adjoint_plain.o", common_cu + ["-c", os.path.join(CSRC, "k_adjoint_plain.cu")]),
         ("k_mass.o", common_cu + ["-fmad=false", "-c", os.path.join(CSRC, "k_mass.cu")]),
         ("srs_host.o", common_cc + ["-c", os.path.join(CSRC, "srs_host.cpp")]),
         ("meshgen.o", common_cc + ["-c", os.path.join(CSRC, "meshgen.cpp")]),

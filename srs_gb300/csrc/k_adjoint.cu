@@ -29,6 +29,7 @@
 // precision.
 #include <type_traits>
 
+#include "srs_adjoint.cuh"
 #include "srs_cluster.cuh"
 #include "srs_engine.h"
 
@@ -37,29 +38,6 @@ namespace srs {
 namespace {
 
 constexpr int NA = SRS_N_ADJ;
-
-__device__ __forceinline__ void kadd(float& s, float& c, float v) {
-  float y = v - c;
-  float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-
-// One buffer reaction r = kon (B - b) c - koff b of an element: adds its
-// Jacobian-transpose terms and its kon/koff gradient terms.
-__device__ __forceinline__ void adj_buffer(const Consts32& k, const AdjConsts& ak, int q, float c,
-                                           float ub, float lb, float w, float& ob, float& oc,
-                                           float& dG, float* g, int gi) {
-  const float free = k.bfree[q] - ub;
-  const float alpha = k.kon[q] * free;
-  const float beta = fmaf(k.kon[q], c, k.koff[q]);
-  dG -= alpha;            // dF_Ca/dCa (times B)
-  ob = fmaf(beta, w - lb, ob);  // dF_Ca/db * lambda_Ca + dF_b/db * lambda_b
-  oc = fmaf(alpha, lb, oc);      // dF_b/dCa * lambda_b
-  const float d = lb - w;
-  g[gi] = fmaf(d * free, c, g[gi]);                  // dr/dkon = (B - b) c
-  g[gi + 1] = fmaf(-d, ak.brest[q] + ub, g[gi + 1]);  // dr/dkoff = -b
-}
 
 }  // namespace
 
@@ -102,14 +80,6 @@ __device__ __forceinline__ float tick_injection(const AdjArgs& a, const double* 
   return (float)inj;
 }
 
-// 1 / B(c), B the rapid-buffer factor of UpdateFastBuffer
-// (cpu/RunSimulation.cpp:15-22).
-__device__ __forceinline__ float sl_inv_factor(const Consts32& k, float bsl, float c) {
-  if (bsl == 0.0f) return 1.0f;
-  const float kc = k.khi + c;
-  const float kc2 = kc * kc;
-  return __fdividef(kc2, kc2 + bsl);
-}
 
 }  // namespace
 
@@ -401,38 +371,10 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
         Sy = fmaf(at.w, n3.w, Sy);
         Sy = fmaf(-sa, me.w, Sy);
         float* g = gstep;  // this element's terms go straight into the thread's sums
-        // D gradients: sum_j lambda_j (L u)_j = sum_j u_j (L^T lambda)_j
-        g[SRS_ADJ_D_CA] = fmaf(x.x, Sc, g[SRS_ADJ_D_CA]);
-        g[SRS_ADJ_D_ATP] = fmaf(x.y, Sa, g[SRS_ADJ_D_ATP]);
-        g[SRS_ADJ_D_CMDN] = fmaf(x.z, Sm, g[SRS_ADJ_D_CMDN]);
-        g[SRS_ADJ_D_DYE] = fmaf(x.w, Sy, g[SRS_ADJ_D_DYE]);
-        float oc = k.D[0] * Sc, oa = k.D[1] * Sa, om = k.D[2] * Sm, oy = k.D[3] * Sy, oi = 0.0f;
         const float w = me.x;
-        float dG = 0.0f;
-        const float c = (jsr ? k.c0j : k.c0) + x.x;
-        if (!jsr) {
-          adj_buffer(k, ak, 0, c, x.w, me.w, w, oy, oc, dG, g, SRS_ADJ_K_ON_DYE);
-          adj_buffer(k, ak, 1, c, x.y, me.y, w, oa, oc, dG, g, SRS_ADJ_K_ON_ATP);
-          adj_buffer(k, ak, 2, c, x.z, me.z, w, om, oc, dG, g, SRS_ADJ_K_ON_CMDN);
-          if (trpn) {
-            adj_buffer(k, ak, 3, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_TRPN);
-            // SERCA v(Ki), Ki = (c / K_D_i)^2 (cpu/RunSimulation.cpp:83-91)
-            float Ki = c * k.inv_kdi;
-            Ki = Ki * Ki;
-            const float den = fmaf(Ki * Ki, k.sd2, fmaf(Ki, k.sd1, k.sd0));
-            const float num = fmaf(Ki * Ki, 3.24873e12f, fmaf(Ki, k.sn1, -k.sn0));
-            const float iden = __fdividef(1.0f, den);
-            const float v = num * iden;
-            const float dnum = fmaf(2.0f * Ki, 3.24873e12f, k.sn1);
-            const float dden = fmaf(2.0f * Ki, k.sd2, k.sd1);
-            const float dv = (dnum - v * dden) * iden * (2.0f * c * k.inv_kdi * k.inv_kdi);
-            dG = fmaf(-k.serca_scale, dv, dG);
-            g[SRS_ADJ_A_P] = fmaf(-w * ak.serca_per_ap, v, g[SRS_ADJ_A_P]);
-          }
-        } else {
-          adj_buffer(k, ak, 4, c, xim, li, w, oi, oc, dG, g, SRS_ADJ_K_ON_CSQN);
-          dG -= k.refill_v;
-        }
+        const AdjTerms lt = adj_local(k, ak, x, xim, me, li, jsr, trpn, Sc, Sa, Sm, Sy, g);
+        float oc = lt.oc, dG = lt.dG;
+        const float oa = lt.oa, om = lt.om, oy = lt.oy, oi = lt.oi, c = lt.c;
         if (i < n_ch) {
           // channel elements and their RyR partners all sit in partition 0
           for (int q = s_cptr[i]; q < s_cptr[i + 1]; ++q) {
@@ -457,18 +399,7 @@ __global__ void __launch_bounds__(512, 1) k_adjoint32(AdjArgs a) {
             }
           }
         }
-        oc = fmaf(dG, w, oc);
-        if (bsl != 0.0f) {
-          // F_Ca = G / B(c):  -G B'(c) / B^2 lambda_Ca = 2 bsl G w / (B kc^3)
-          const float kc = k.khi + c;
-          const float ikc = __fdividef(1.0f, kc);
-          const float bk2 = bsl * ikc * ikc;           // B - 1
-          const float GB = __fdividef(G, 1.0f + bk2);  // G / B
-          const float t3 = GB * bk2 * ikc;             // G bsl / (B kc^3)
-          oc = fmaf(2.0f * t3, w, oc);
-          g[SRS_ADJ_B_TOT_SL] = fmaf(-w * GB, bk2 * ak.inv_btot_sl, g[SRS_ADJ_B_TOT_SL]);
-          g[SRS_ADJ_K_D_SL] = fmaf(-w * t3, (c - k.khi) * ak.inv_khi, g[SRS_ADJ_K_D_SL]);
-        }
+        adj_rapid(k, ak, bsl, c, G, w, dG, oc, g);
         // compensated update of lambda
         float4 L = make_float4(lx, me.y, me.z, me.w);
         float lnew = li;

@@ -35,7 +35,9 @@ namespace srs {
 // Plain FP32 engine
 // ===========================================================================
 // One element of one realization: release flux of its channels, then the
-// FP32 update (tet_update).
+// FP32 update (tet_update).  TRAJ: also record the state the step starts
+// from and the Ca rate (the adjoint's trajectory).
+template <bool TRAJ>
 __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int j) {
   RealCtl* ctlp = a.CS.ctl + r;
   const int N = a.N;
@@ -71,8 +73,18 @@ __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int
     float ci = a.CI[(size_t)r * N + j];
     float4 out;
     float imo;
-    tet_update(a.k, M[j], I[j], M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
-               a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo);
+    if constexpr (TRAJ) {
+      float g;
+      const float4 x = M[j];
+      const float im = I[j];
+      tet_update(a.k, x, im, M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
+                 a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo, &g);
+      a.traj_u[(size_t)r * N + j] = x;
+      a.traj_ig[(size_t)r * N + j] = make_float2(im, g);
+    } else {
+      tet_update(a.k, M[j], I[j], M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
+                 a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo);
+    }
     Mo[j] = out;
     Io[j] = imo;
     a.CM[(size_t)r * N + j] = cm;
@@ -82,7 +94,9 @@ __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int
 }
 
 // Gating of one realization's channels from the new state, then the
-// protocol of the next step (one block).
+// protocol of the next step (one block).  TRAJ: first record the channel
+// states the step used.
+template <bool TRAJ>
 __device__ __forceinline__ void plain32_gate(const Plain32Args& a, int r, int32_t* s_nb) {
   RealCtl* ctlp = a.CS.ctl + r;
   float4* Mo = a.M_out + (size_t)r * a.N;
@@ -96,6 +110,17 @@ __device__ __forceinline__ void plain32_gate(const Plain32Args& a, int r, int32_
   int32_t* lcc_w = a.CS.lcc + (size_t)r * a.C.NL;
   int32_t* lccv_w = a.CS.lccv + (size_t)r * a.C.NL;
   double* res = a.CS.res + (size_t)r * (a.C.NR + a.C.NL);
+  if constexpr (TRAJ) {
+    const int NR = a.C.NR, NL = a.C.NL, W = NR + 2 * NL + 1;
+    int32_t* rec = a.traj_ch + (size_t)r * W;
+    for (int q = threadIdx.x; q < NR; q += blockDim.x) rec[q] = ryr_w[q];
+    for (int q = threadIdx.x; q < NL; q += blockDim.x) {
+      rec[NR + q] = lcc_w[q];
+      rec[NR + NL + q] = lccv_w[q];
+    }
+    if (threadIdx.x == 0) rec[W - 1] = ctl.vsel;
+    __syncthreads();
+  }
   if (!a.P.nogating) {
     gate_all(a.P, a.C, ctl.vsel, ctl.seed, ctl.step, ryr_w, lcc_w, lccv_w, res, s_nb,
              threadIdx.x, blockDim.x, ca, []() { __syncthreads(); });
@@ -115,12 +140,13 @@ __device__ __forceinline__ void plain32_gate(const Plain32Args& a, int r, int32_
 // Small meshes: one launch per time step.  Grid: x over realizations, y over
 // blocks of 256 elements, so the blocks that run together share the geometry
 // of one element range in L2; the last block of a realization gates.
+template <bool TRAJ>
 __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
   const int r = blockIdx.x;
   if (a.CS.ctl[r].done) return;
   const int j = blockIdx.y * blockDim.x + threadIdx.x;
   const uint32_t fl = j < a.N ? a.flags[j] : 0u;
-  if (j < a.N) plain32_element(a, r, j);
+  if (j < a.N) plain32_element<TRAJ>(a, r, j);
   __shared__ int s_last;
   __shared__ int32_t s_nb[1024];
   // The last block of the realization gates its channels from the new Ca of
@@ -134,7 +160,7 @@ __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  plain32_gate(a, r, s_nb);
+  plain32_gate<TRAJ>(a, r, s_nb);
 }
 
 // Bulk prefetch into L2 of [p, p + bytes) within an array that starts on a
@@ -150,6 +176,7 @@ __device__ __forceinline__ void prefetch_span(const void* p, size_t bytes) {
 // first thread of each block asks L2 for the state this realization needs
 // pf_rows element blocks later (about one wave of blocks ahead), so those
 // blocks find it there instead of waiting on DRAM.
+template <bool TRAJ>
 __global__ void __launch_bounds__(256, 6) k_plain32_update(Plain32Args a) {
   const int r = blockIdx.x;
   if (a.CS.ctl[r].done) return;
@@ -163,14 +190,15 @@ __global__ void __launch_bounds__(256, 6) k_plain32_update(Plain32Args a) {
     prefetch_span(a.CI + o, n * sizeof(float));
   }
   const int j = blockIdx.y * blockDim.x + threadIdx.x;
-  if (j < a.N) plain32_element(a, r, j);
+  if (j < a.N) plain32_element<TRAJ>(a, r, j);
 }
 
+template <bool TRAJ>
 __global__ void __launch_bounds__(256) k_plain32_gate(Plain32Args a) {
   const int r = blockIdx.x;
   if (a.CS.ctl[r].done) return;
   __shared__ int32_t s_nb[1024];
-  plain32_gate(a, r, s_nb);
+  plain32_gate<TRAJ>(a, r, s_nb);
 }
 
 __global__ void k_plain32_prestep(Plain32Args a, int write_initial_row) {
@@ -193,13 +221,21 @@ int plain32_kernels_per_step(const Plain32Args& a) { return a.N >= PLAIN32_SPLIT
 int launch_plain32_step(const Plain32Args& a, cudaStream_t st) {
   if ((a.N + 255) / 256 > 65535) return -1;  // grid y limit: 16.7 M elements
   dim3 grid(a.R, (a.N + 255) / 256);
+  const bool traj = a.traj_u != nullptr;
   if (a.N >= PLAIN32_SPLIT_N) {
-    k_plain32_update<<<grid, 256, 0, st>>>(a);
-    k_plain32_gate<<<a.R, 256, 0, st>>>(a);
+    if (traj) {
+      k_plain32_update<true><<<grid, 256, 0, st>>>(a);
+      k_plain32_gate<true><<<a.R, 256, 0, st>>>(a);
+    } else {
+      k_plain32_update<false><<<grid, 256, 0, st>>>(a);
+      k_plain32_gate<false><<<a.R, 256, 0, st>>>(a);
+    }
   } else {
     // few realizations: 64-thread blocks spread the step over more SMs
     const int bs = (size_t)((a.N + 255) / 256) * a.R < 304 ? 64 : 256;
-    k_plain32_step<<<dim3(a.R, (a.N + bs - 1) / bs), bs, 0, st>>>(a);
+    const dim3 g2(a.R, (a.N + bs - 1) / bs);
+    if (traj) k_plain32_step<true><<<g2, bs, 0, st>>>(a);
+    else k_plain32_step<false><<<g2, bs, 0, st>>>(a);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

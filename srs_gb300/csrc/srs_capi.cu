@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -107,6 +108,8 @@ struct srs_sim {
   int adj_ls_version = -1;
   AdjRec* d_adj_geo = nullptr;  // reverse-sweep records of the CTA grouping
   int adj_geo_m = 0;
+  float4* d_adjp_aT = nullptr;  // plain engine: transposed coefficients [N]
+  float2* d_adjp_bs = nullptr;  // plain engine: (bsl, sum a + kb) with the domain flags
   // total Ca (built on first use)
   MassArgs mass{};
   // adjoint work buffers, kept between calls (name -> allocation)
@@ -2095,6 +2098,127 @@ int adjoint_geometry(srs_sim* s, int m, int bits) {
   return SRS_OK;
 }
 
+// Reverse-step records of the plain engine: aT in engine order and (bsl,
+// sum a + kb) with TropC and JSR in the sign bits.
+int adjoint_plain_geometry(srs_sim* s) {
+  if (s->d_adjp_aT) return SRS_OK;
+  const int N = s->N;
+  std::vector<float2> bs(N);
+  for (int e = 0; e < N; ++e) {
+    const int j = s->ref_of_eng[e];
+    float a[4];
+    for (int k = 0; k < 4; ++k) a[k] = (float)s->op.aij[5 * (size_t)j + 1 + k];
+    const float sa = ((a[0] + a[1]) + (a[2] + a[3])) + (float)s->op.kb[j];
+    const float bsl = bsl_of(s, j);
+    if (bsl < 0.0f || sa < 0.0f || std::signbit(bsl) || std::signbit(sa))
+      return fail(SRS_ERR_MESH, "negative SL capacity or coupling coefficient");
+    bs[e] = make_float2(s->m.tropc[j] ? -bsl : bsl, s->m.domain[j] == DOMAIN_JSR ? -sa : sa);
+  }
+  SRS_TRY(dev_upload(s, &s->d_adjp_aT, s->aT_h.data(), s->aT_h.size()));
+  SRS_TRY(dev_upload(s, &s->d_adjp_bs, bs.data(), bs.size()));
+  return SRS_OK;
+}
+
+// Checkpoint plan of a reverse sweep over nseg trajectory segments: L levels
+// of at most f - 1 snapshots each (f^L >= nseg), plus the final state.  The
+// sweep recomputes the forward run L times at most; one level is the plain
+// "checkpoint every K steps" scheme.  Returns false when max_snaps snapshots
+// cannot hold any plan.
+bool checkpoint_plan(int64_t nseg, int64_t max_snaps, int* L, int64_t* f) {
+  for (int l = 1; l <= 12; ++l) {
+    int64_t g = (int64_t)std::ceil(std::pow((double)nseg, 1.0 / l));
+    while (g > 1) {  // the smallest fan-out with g^l >= nseg
+      int64_t p = 1;
+      for (int i = 0; i < l && p < nseg; ++i) p *= g - 1;
+      if (p >= nseg) --g;
+      else break;
+    }
+    for (;;) {
+      int64_t p = 1;
+      for (int i = 0; i < l && p < nseg; ++i) p *= g;
+      if (p >= nseg) break;
+      ++g;
+    }
+    if ((int64_t)l * std::max<int64_t>(g - 1, 0) + 1 <= max_snaps) {
+      *L = l;
+      *f = std::max<int64_t>(g, 1);
+      return true;
+    }
+  }
+  return false;
+}
+
+// Segment length and checkpoint plan of srs_adjoint for the device memory
+// free now (buffers the previous calls keep count as free).
+struct AdjPlan {
+  int K;        // steps of a recorded segment
+  int L;        // checkpoint levels (forward recomputations)
+  int64_t fan;  // pieces per level
+  int64_t forward_steps;  // forward steps the sweep runs (advance and record)
+};
+
+int adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, AdjPlan* pl) {
+  if (s->d.precision != SRS_FP32)
+    return fail(SRS_ERR_UNSUPPORTED, "the adjoint runs on the FP32 engines");
+  if (d->n_steps < 1 || d->tick_every < 1 || d->checkpoint_every < 0 || d->max_checkpoints < 0)
+    return fail(SRS_ERR_INPUT, "n_steps and tick_every must be positive");
+  const bool plain = s->d.engine != SRS_ENGINE_RESIDENT;
+  const int R = s->R, NR = s->NR, NL = s->NL, W = NR + 2 * NL + 1, te = d->tick_every;
+  const size_t NE = eng_count(s);
+  const int ns = s->ls.n_samples;
+  const int64_t n_steps = d->n_steps, n_ticks = n_steps / te;
+  // bytes: one recorded step, one snapshot of the whole state, lambda
+  const size_t step_b = (size_t)R * (NE * 24 + (size_t)W * 4);
+  const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
+                        (size_t)R * sizeof(RealCtl);
+  const size_t lam_b = (size_t)R * NE * (plain ? 76 : 44);
+  size_t free_b = 0, total_b = 0, held = 0;
+  for (auto& b : s->adj_bufs) held += b.second;
+  SRS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  free_b += held;
+  int K = d->checkpoint_every;
+  if (K == 0) {
+    // automatic: keep the whole trajectory (no recomputation) when it takes
+    // at most half of the free device memory, else segments of 256 steps
+    // (fewer when 256 recorded steps would take more than a quarter)
+    const size_t whole = (size_t)(n_steps + 1) * step_b;
+    if (n_steps <= INT32_MAX && whole <= free_b / 2) {
+      K = (int)n_steps;
+    } else {
+      K = 256;
+      while (K > 8 && (size_t)(K + 1) * step_b > free_b / 4) K /= 2;
+    }
+  }
+  const int64_t nseg = (n_steps + K - 1) / K;
+  // memory: snapshots, one segment of trajectory, lambda, tick coefficients
+  const size_t traj_b = (size_t)(K + 1) * R * NE * 24 + (size_t)K * R * W * 4;
+  const size_t fixed = traj_b + lam_b + (size_t)(K / te + 2) * R * ns * 8 +
+                       (size_t)R * std::max<int64_t>(n_ticks, 1) * ns * 16;
+  const size_t usable = free_b / 10 * 9;
+  int64_t max_snaps = usable > fixed ? (int64_t)((usable - fixed) / snap_b) : 0;
+  if (d->max_checkpoints > 0) max_snaps = std::min<int64_t>(max_snaps, d->max_checkpoints + 1);
+  int L = 1;
+  int64_t fan = 1;
+  if (!checkpoint_plan(nseg, max_snaps, &L, &fan))
+    return fail(SRS_ERR_NOMEM, "adjoint needs " + std::to_string((fixed + 2 * snap_b) >> 20) +
+                                   " MiB of device memory at least (" + std::to_string(free_b >> 20) +
+                                   " MiB free): lower checkpoint_every or the realizations");
+  pl->K = K;
+  pl->L = L;
+  pl->fan = fan;
+  // forward steps of the recursion (see srs_adjoint)
+  std::vector<int64_t> q(L + 1);
+  q[L] = K;
+  for (int l = L - 1; l >= 0; --l) q[l] = l == L - 1 ? K : std::min<int64_t>(INT64_MAX / 2, q[l + 1] * fan);
+  std::function<int64_t(int, int64_t)> cnt = [&](int l, int64_t len) -> int64_t {
+    if (l == L) return len;
+    const int64_t p = (len + q[l] - 1) / q[l];
+    return (p - 1) * q[l] + cnt(l + 1, len - (p - 1) * q[l]) + (p - 1) * cnt(l + 1, q[l]);
+  };
+  pl->forward_steps = cnt(0, n_steps);
+  return SRS_OK;
+}
+
 int snap_alloc(srs_sim* s, Scratch& sc, StateSnap* o) {
   const size_t n = (size_t)s->R * eng_count(s);
   SRS_TRY(sc.get(&o->M, n));
@@ -2133,44 +2257,24 @@ extern "C" {
 
 int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   if (!s || !d || !out || !out->loss || !out->grad || !d->f0) return fail(SRS_ERR_INPUT, "null argument");
-  if (s->d.precision != SRS_FP32 || s->d.engine != SRS_ENGINE_RESIDENT)
-    return fail(SRS_ERR_UNSUPPORTED, "the adjoint runs on the FP32 resident engine");
   if (!s->ls.ptr) return fail(SRS_ERR_STATE, "call srs_linescan_setup first");
-  if (d->n_steps < 1 || d->tick_every < 1 || d->checkpoint_every < 0)
-    return fail(SRS_ERR_INPUT, "n_steps and tick_every must be positive");
+  AdjPlan pl;
+  SRS_TRY(adjoint_plan(s, d, &pl));  // also checks the descriptor
+  const bool plain = s->d.engine != SRS_ENGINE_RESIDENT;
   const int R = s->R, NR = s->NR, NL = s->NL, W = NR + 2 * NL + 1, te = d->tick_every;
   const size_t NE = eng_count(s);
   const int ns = s->ls.n_samples;
   const int64_t n_steps = d->n_steps, n_ticks = n_steps / te;
-  int K = d->checkpoint_every;
-  if (K == 0) {
-    // automatic: keep the whole trajectory (no recomputation) when it takes
-    // at most half of the free device memory, else checkpoint every 256 steps
-    size_t free0 = 0, total0 = 0, held0 = 0;
-    for (auto& b : s->adj_bufs) held0 += b.second;
-    SRS_CUDA(cudaMemGetInfo(&free0, &total0));
-    const size_t whole = (size_t)(n_steps + 1) * R * (NE * 24 + (size_t)W * 4);
-    K = (n_steps <= INT32_MAX && whole <= (free0 + held0) / 2) ? (int)n_steps : 256;
-  }
-  const int64_t nseg = (n_steps + K - 1) / K;
+  const int K = pl.K, L = pl.L;
+  const int64_t fan = pl.fan;
   SRS_TRY(adjoint_setup(s));
-  // memory: checkpoints (nseg + 1), one segment of trajectory, lambda
-  const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
-                        (size_t)R * sizeof(RealCtl);
-  const size_t traj_b = (size_t)(K + 1) * R * NE * 24 + (size_t)K * R * W * 4;
-  const size_t need = snap_b * (size_t)(nseg + 1) + traj_b + (size_t)R * NE * 44 +
-                      (size_t)(K / te + 2) * R * ns * 8 + (size_t)R * n_ticks * ns * 8;
-  size_t free_b = 0, total_b = 0, held = 0;
-  for (auto& b : s->adj_bufs) held += b.second;
-  SRS_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  free_b += held;
-  if (need > free_b / 10 * 9)
-    return fail(SRS_ERR_NOMEM, "adjoint needs " + std::to_string(need >> 20) + " MiB of device memory (" +
-                                   std::to_string(free_b >> 20) + " MiB free): raise checkpoint_every "
-                                   "or lower n_steps");
   Scratch sc{s};
-  std::vector<StateSnap> ck(nseg + 1);
-  for (auto& c : ck) SRS_TRY(snap_alloc(s, sc, &c));
+  // level l holds the starts of its pieces but the last; then the final state
+  std::vector<std::vector<StateSnap>> lv(L, std::vector<StateSnap>(std::max<int64_t>(fan - 1, 0)));
+  for (auto& l : lv)
+    for (auto& c : l) SRS_TRY(snap_alloc(s, sc, &c));
+  StateSnap fin;
+  SRS_TRY(snap_alloc(s, sc, &fin));
   float4* traj_u;
   float2* traj_ig;
   int32_t* traj_ch;
@@ -2204,153 +2308,227 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   }
   s->P.run_protocol = 0;
   refresh_args(s);
-  // ---- forward with checkpoints ------------------------------------------------
-  // (the last segment records its trajectory on the way: it is the first
-  // one the reverse sweep needs)
-  auto traj_launch = [&](int len) -> int {
-    ResidentArgs ra = s->ar;
-    ra.steps = len;
-    ra.prestep_first = 0;
-    ra.initial_row = 0;
-    ra.speculate = 1;
-    ra.traj_u = traj_u;
-    ra.traj_ig = traj_ig;
-    ra.traj_ch = traj_ch;
-    if (launch_resident(ra, s->C, s->n_clusters, s->threads, s->smem, s->st))
-      return fail(SRS_ERR_CUDA, std::string("trajectory launch: ") + cudaGetErrorString(cudaGetLastError()));
-    s->launches++;
+  // plain engine: the published slots (double buffered) and the gradient
+  // rows of the reverse-step blocks
+  float4* pub[2] = {nullptr, nullptr};
+  double* part = nullptr;
+  int adjp_by = 0;
+  if (plain) {
+    int dev = 0, n_sm = 0;
+    SRS_CUDA(cudaGetDevice(&dev));
+    SRS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    adjp_by = adjp_blocks_per_realization((int)NE, R, n_sm);
+    SRS_TRY(sc.get(&pub[0], (size_t)R * NE));
+    SRS_TRY(sc.get(&pub[1], (size_t)R * NE));
+    SRS_TRY(sc.get(&part, (size_t)R * adjp_by * SRS_N_ADJ));
+    SRS_TRY(adjoint_plain_geometry(s));
+  }
+
+  // ---- engine operations on the live state ----------------------------------
+  // advance: len steps without recording (the plain engine's state returns
+  // to buffer 0)
+  auto advance_live = [&](int64_t len) -> int {
+    if (!plain) {
+      for (int64_t done = 0; done < len;) {
+        const int k = (int)std::min<int64_t>(K, len - done);
+        SRS_TRY(resident_launch(s, k));
+        done += k;
+      }
+      return SRS_OK;
+    }
+    SRS_TRY(plain_steps(s, len));
+    if (len & 1) {
+      SRS_CUDA(cudaMemcpyAsync(s->d_M[0], s->d_M[1], sizeof(float4) * R * NE, cudaMemcpyDeviceToDevice, s->st));
+      SRS_CUDA(cudaMemcpyAsync(s->d_I[0], s->d_I[1], sizeof(float) * R * NE, cudaMemcpyDeviceToDevice, s->st));
+    }
     return SRS_OK;
   };
-  for (int64_t k = 0; k < nseg; ++k) {
-    const int len = (int)std::min<int64_t>(K, n_steps - k * K);
-    if (k < nseg - 1) {
-      SRS_TRY(snap_copy(s, ck[k], true));
-      SRS_TRY(resident_launch(s, len));
-    } else {
-      SRS_TRY(traj_launch(len));
+  // record: len steps writing trajectory slots 0 .. len (slot t = x_{s0+t})
+  auto record_live = [&](int len) -> int {
+    if (!plain) {
+      ResidentArgs ra = s->ar;
+      ra.steps = len;
+      ra.prestep_first = 0;
+      ra.initial_row = 0;
+      ra.speculate = 1;
+      ra.traj_u = traj_u;
+      ra.traj_ig = traj_ig;
+      ra.traj_ch = traj_ch;
+      if (launch_resident(ra, s->C, s->n_clusters, s->threads, s->smem, s->st))
+        return fail(SRS_ERR_CUDA, std::string("trajectory launch: ") + cudaGetErrorString(cudaGetLastError()));
+      s->launches++;
+      return SRS_OK;
     }
-  }
-  SRS_TRY(snap_copy(s, ck[nseg], true));
+    for (int t = 0; t < len; ++t) {
+      Plain32Args a = s->a32;
+      const int par = t & 1;
+      a.M_in = s->d_M[par];
+      a.I_in = s->d_I[par];
+      a.M_out = s->d_M[par ^ 1];
+      a.I_out = s->d_I[par ^ 1];
+      a.traj_u = traj_u + (size_t)t * R * NE;
+      a.traj_ig = traj_ig + (size_t)t * R * NE;
+      a.traj_ch = traj_ch + (size_t)t * R * W;
+      if (launch_plain32_step(a, s->st))
+        return fail(SRS_ERR_CUDA, std::string("trajectory step: ") + cudaGetErrorString(cudaGetLastError()));
+      s->launches += plain32_kernels_per_step(a);
+    }
+    const int par = len & 1;
+    SRS_CUDA(cudaMemcpyAsync(traj_u + (size_t)len * R * NE, s->d_M[par], sizeof(float4) * R * NE,
+                             cudaMemcpyDeviceToDevice, s->st));
+    if (par) {
+      SRS_CUDA(cudaMemcpyAsync(s->d_M[0], s->d_M[1], sizeof(float4) * R * NE, cudaMemcpyDeviceToDevice, s->st));
+      SRS_CUDA(cudaMemcpyAsync(s->d_I[0], s->d_I[1], sizeof(float) * R * NE, cudaMemcpyDeviceToDevice, s->st));
+    }
+    return SRS_OK;
+  };
+
+  // ---- reverse-sweep arguments ------------------------------------------------
+  AdjConsts ak{};
   {
-    std::vector<RealCtl> ctl(R);
-    SRS_CUDA(cudaMemcpyAsync(ctl.data(), ck[nseg].ctl, sizeof(RealCtl) * R, cudaMemcpyDeviceToHost, s->st));
-    SRS_CUDA(cudaStreamSynchronize(s->st));
-    for (auto& c : ctl) {
-      if (c.status & 1u) return fail(SRS_ERR_NONFINITE, "a realization produced a non-finite Ca value");
-      if (c.done) return fail(SRS_ERR_STATE, "a realization is finished; reset it before the adjoint");
-    }
+    const RestValues& rv = s->rv;
+    const double brest[5] = {rv.dye, rv.atp, rv.cmdn, rv.trpn, rv.csqn};
+    for (int q = 0; q < 5; ++q) ak.brest[q] = (float)brest[q];
+    const double bt = s->p.reals[R_B_TOT_SL_HI];
+    ak.inv_btot_sl = bt != 0.0 ? (float)(1.0 / bt) : 0.0f;
+    ak.serca_per_ap = 2e-3f;
+    ak.v_cell = (float)s->p.reals[R_V_CELL];
+    ak.inv_khi = (float)(1.0 / s->p.reals[R_K_D_SL_HI]);
   }
-  // ---- reverse sweep -----------------------------------------------------------
   SRS_CUDA(cudaMemsetAsync(lam, 0, sizeof(float4) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(lam_c4, 0, sizeof(float4) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(lam_im, 0, sizeof(float) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(lam_cim, 0, sizeof(float) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * R * SRS_N_ADJ, s->st));
+  if (part) SRS_CUDA(cudaMemsetAsync(part, 0, sizeof(double) * R * adjp_by * SRS_N_ADJ, s->st));
   SRS_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * std::max<int64_t>(n_ticks, 1) * R * ns, s->st));
   AdjArgs aa{};
-  aa.R = R;
-  aa.P = s->P_stride;
-  aa.n_local = s->ar.n_local;
-  aa.n_chtet = s->ar.n_chtet;
-  aa.n_int = s->ar.n_int;
-  aa.ch_interior = s->ar.ch_interior;
-  aa.ch_ptr = s->ar.ch_ptr;
-  aa.ch_list = s->ar.ch_list;
-  aa.ryr_cleft_code = s->ar.ryr_cleft_code;
-  aa.ryr_jsr_code = s->ar.ryr_jsr_code;
-  aa.ryr_s_cl = s->d_ryr_s_cl;
-  aa.ryr_s_js = s->d_ryr_s_js;
-  aa.NR = NR;
-  aa.NL = NL;
-  aa.traj_u = traj_u;
-  aa.traj_ig = traj_ig;
-  aa.traj_ch = traj_ch;
-  aa.tick_every = te;
-  aa.n_samples = ns;
-  aa.coef = coef;
-  aa.wt_ptr = s->d_wt_ptr;
-  aa.wt_idx = s->d_wt_idx;
-  aa.wt_w = s->d_wt_w;
-  aa.lam = lam;
-  aa.lam_im = lam_im;
-  aa.lam_c4 = lam_c4;
-  aa.lam_cim = lam_cim;
-  aa.lam_c = lam_c;
-  aa.grad = grad;
-  aa.k = s->ar.k;
-  {
-    const RestValues& rv = s->rv;
-    const double brest[5] = {rv.dye, rv.atp, rv.cmdn, rv.trpn, rv.csqn};
-    for (int q = 0; q < 5; ++q) aa.ak.brest[q] = (float)brest[q];
-    const double bt = s->p.reals[R_B_TOT_SL_HI];
-    aa.ak.inv_btot_sl = bt != 0.0 ? (float)(1.0 / bt) : 0.0f;
-    aa.ak.serca_per_ap = 2e-3f;
-    aa.ak.v_cell = (float)s->p.reals[R_V_CELL];
-    aa.ak.inv_khi = (float)(1.0 / s->p.reals[R_K_D_SL_HI]);
-  }
-  const int n_ent = 2 * NR + NL;
-  if (d->threads_per_cta != 0 &&
-      (d->threads_per_cta % 32 || d->threads_per_cta < 64 || d->threads_per_cta > 512))
-    return fail(SRS_ERR_INPUT, "threads_per_cta must be a multiple of 32 in [64, 512]");
-  if (d->cta_partitions < 0 || (d->cta_partitions > 0 && s->C % d->cta_partitions))
-    return fail(SRS_ERR_INPUT, "cta_partitions must divide the cluster size");
-  // CTA grouping: m forward partitions per CTA (clusters of C/m CTAs), the
-  // owner state of lambda on chip when it fits next to the published slots,
-  // 256 or 512 threads.  Chosen by the estimated time, rounds of clusters x
-  // slots per thread; at equal estimate the 256-thread CTA wins (two CTAs per
-  // SM overlap each other's barrier waits).
-  int best_m = 0, best_C = 0, adj_ncl = 0, best_bits = 0, adj_threads = 0;
+  int best_C = 0, adj_ncl = 0, adj_threads = 0;
   size_t adj_smem = 0;
-  bool best_own = false, best_stage = false;
-  double best_cost = 1e300;
-  const std::vector<int> thr_list =
-      d->threads_per_cta ? std::vector<int>{d->threads_per_cta} : std::vector<int>{256, 512};
-  for (int thr : thr_list) {
-    for (int m = 1; m <= s->C; ++m) {
-      if (s->C % m || (d->cta_partitions && m != d->cta_partitions)) continue;
-      const int Ca = s->C / m, Pc = m * s->P_stride;
-      int bits = 1, rbits = 0;
-      while ((1 << bits) < Pc) ++bits;
-      while ((1 << rbits) < Ca) ++rbits;
-      if (bits + rbits > 16) continue;
-      for (int stage = 1; stage >= 0; --stage) {
-        if (stage && (d->flags & SRS_ADJ_NO_STAGE)) continue;
-        if (!stage && (d->flags & SRS_ADJ_STAGE)) continue;
-        for (int own = 1; own >= 0; --own) {
-          if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
-          const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0, stage != 0);
-          const int ncl = std::min(adjoint_max_clusters(Ca, thr, sm), R);
-          if (ncl <= 0) continue;
-          const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / thr) *
-                              (own ? 1.0 : 1.15) * (stage ? 1.01 : 1.0) * (thr == 512 ? 1.02 : 1.0);
-          if (cost < best_cost) {
-            best_cost = cost;
-            best_m = m;
-            best_C = Ca;
-            adj_ncl = ncl;
-            adj_smem = sm;
-            best_own = own != 0;
-            best_stage = stage != 0;
-            best_bits = bits;
-            adj_threads = thr;
-          }
-          break;  // the on-chip variant when it fits
-        }
-      }
-    }
-  }
-  if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
-  SRS_TRY(adjoint_geometry(s, best_m, best_bits));
-  aa.own_in_smem = best_own;
-  aa.stage = best_stage;
   unsigned int* d_status;
   SRS_TRY(sc.get(&d_status, 1));
   SRS_CUDA(cudaMemsetAsync(d_status, 0, sizeof(unsigned int), s->st));
-  aa.status = d_status;
-  aa.m_sub = best_m;
-  aa.off_bits = best_bits;
-  aa.ch_off_bits = s->off_bits;
-  aa.geo = s->d_adj_geo;
+  if (!plain) {
+    aa.R = R;
+    aa.P = s->P_stride;
+    aa.n_local = s->ar.n_local;
+    aa.n_chtet = s->ar.n_chtet;
+    aa.n_int = s->ar.n_int;
+    aa.ch_interior = s->ar.ch_interior;
+    aa.ch_ptr = s->ar.ch_ptr;
+    aa.ch_list = s->ar.ch_list;
+    aa.ryr_cleft_code = s->ar.ryr_cleft_code;
+    aa.ryr_jsr_code = s->ar.ryr_jsr_code;
+    aa.ryr_s_cl = s->d_ryr_s_cl;
+    aa.ryr_s_js = s->d_ryr_s_js;
+    aa.NR = NR;
+    aa.NL = NL;
+    aa.traj_u = traj_u;
+    aa.traj_ig = traj_ig;
+    aa.traj_ch = traj_ch;
+    aa.tick_every = te;
+    aa.n_samples = ns;
+    aa.coef = coef;
+    aa.wt_ptr = s->d_wt_ptr;
+    aa.wt_idx = s->d_wt_idx;
+    aa.wt_w = s->d_wt_w;
+    aa.lam = lam;
+    aa.lam_im = lam_im;
+    aa.lam_c4 = lam_c4;
+    aa.lam_cim = lam_cim;
+    aa.lam_c = lam_c;
+    aa.grad = grad;
+    aa.k = s->ar.k;
+    aa.ak = ak;
+    const int n_ent = 2 * NR + NL;
+    if (d->threads_per_cta != 0 &&
+        (d->threads_per_cta % 32 || d->threads_per_cta < 64 || d->threads_per_cta > 512))
+      return fail(SRS_ERR_INPUT, "threads_per_cta must be a multiple of 32 in [64, 512]");
+    if (d->cta_partitions < 0 || (d->cta_partitions > 0 && s->C % d->cta_partitions))
+      return fail(SRS_ERR_INPUT, "cta_partitions must divide the cluster size");
+    // CTA grouping: m forward partitions per CTA (clusters of C/m CTAs), the
+    // owner state of lambda on chip when it fits next to the published slots,
+    // 256 or 512 threads.  Chosen by the estimated time, rounds of clusters x
+    // slots per thread; at equal estimate the 256-thread CTA wins (two CTAs per
+    // SM overlap each other's barrier waits).
+    int best_m = 0, best_bits = 0;
+    bool best_own = false, best_stage = false;
+    double best_cost = 1e300;
+    const std::vector<int> thr_list =
+        d->threads_per_cta ? std::vector<int>{d->threads_per_cta} : std::vector<int>{256, 512};
+    for (int thr : thr_list) {
+      for (int m = 1; m <= s->C; ++m) {
+        if (s->C % m || (d->cta_partitions && m != d->cta_partitions)) continue;
+        const int Ca = s->C / m, Pc = m * s->P_stride;
+        int bits = 1, rbits = 0;
+        while ((1 << bits) < Pc) ++bits;
+        while ((1 << rbits) < Ca) ++rbits;
+        if (bits + rbits > 16) continue;
+        for (int stage = 1; stage >= 0; --stage) {
+          if (stage && (d->flags & SRS_ADJ_NO_STAGE)) continue;
+          if (!stage && (d->flags & SRS_ADJ_STAGE)) continue;
+          for (int own = 1; own >= 0; --own) {
+            if (own && (d->flags & SRS_ADJ_LAMBDA_GLOBAL)) continue;
+            const size_t sm = adjoint_smem_bytes(Pc, s->part_nch[0], n_ent, own != 0, stage != 0);
+            const int ncl = std::min(adjoint_max_clusters(Ca, thr, sm), R);
+            if (ncl <= 0) continue;
+            const double cost = std::ceil((double)R / ncl) * std::ceil((double)Pc / thr) *
+                                (own ? 1.0 : 1.15) * (stage ? 1.01 : 1.0) * (thr == 512 ? 1.02 : 1.0);
+            if (cost < best_cost) {
+              best_cost = cost;
+              best_m = m;
+              best_C = Ca;
+              adj_ncl = ncl;
+              adj_smem = sm;
+              best_own = own != 0;
+              best_stage = stage != 0;
+              best_bits = bits;
+              adj_threads = thr;
+            }
+            break;  // the on-chip variant when it fits
+          }
+        }
+      }
+    }
+    if (adj_ncl <= 0) return fail(SRS_ERR_UNSUPPORTED, "adjoint configuration does not fit on the device");
+    SRS_TRY(adjoint_geometry(s, best_m, best_bits));
+    aa.own_in_smem = best_own;
+    aa.stage = best_stage;
+    aa.status = d_status;
+    aa.m_sub = best_m;
+    aa.off_bits = best_bits;
+    aa.ch_off_bits = s->off_bits;
+    aa.geo = s->d_adj_geo;
+  }
+  AdjPlainArgs pa{};
+  if (plain) {
+    pa.N = (int32_t)NE;
+    pa.R = R;
+    pa.NR = NR;
+    pa.NL = NL;
+    pa.n_samples = ns;
+    pa.aT = s->d_adjp_aT;
+    pa.nb = s->a32.nb;
+    pa.bs = s->d_adjp_bs;
+    pa.flags = s->a32.flags;
+    pa.ch_ptr = s->a32.chan_ptr;
+    pa.ch_list = s->a32.chan_list;
+    pa.ryr_cleft = s->ch.ryr_cleft;
+    pa.ryr_jsr = s->ch.ryr_jsr;
+    pa.ryr_s_cl = s->d_ryr_s_cl;
+    pa.ryr_s_js = s->d_ryr_s_js;
+    pa.wt_ptr = s->d_wt_ptr;
+    pa.wt_idx = s->d_wt_idx;
+    pa.wt_w = s->d_wt_w;
+    pa.lam_c = lam_c;
+    pa.lam_im = lam_im;
+    pa.lam_cim = lam_cim;
+    pa.lam_c4 = lam_c4;
+    pa.lam = lam;
+    pa.part = part;
+    pa.k = s->a32.k;
+    pa.ak = ak;
+  }
   AdjTickArgs ta{};
   ta.n_samples = ns;
   ta.n_state = (int32_t)NE;
@@ -2364,13 +2542,8 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   ta.R = R;
   ta.loss = loss;
   ta.mean_trace = mean_trace ? 1 : 0;
-  for (int64_t k = nseg - 1; k >= 0; --k) {
-    const int64_t s0 = k * K;
-    const int len = (int)std::min<int64_t>(K, n_steps - s0);
-    if (k < nseg - 1) {
-      SRS_TRY(snap_copy(s, ck[k], false));
-      SRS_TRY(traj_launch(len));
-    }
+  // the reverse sweep over the recorded segment [s0, s0 + len)
+  auto reverse_segment = [&](int64_t s0, int len) -> int {
     // every tick of the segment in one launch
     const int64_t n1 = (s0 / te + 1) * te;
     if (n1 <= s0 + len) {
@@ -2382,17 +2555,103 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       if (launch_adj_tick(ta, s->st)) return fail(SRS_ERR_CUDA, "tick launch failed");
       s->launches++;
     }
-    aa.n_steps = len;
-    aa.s0 = s0;
-    if (launch_adjoint(aa, best_C, adj_ncl, adj_threads, adj_smem, s->st))
-      return fail(SRS_ERR_CUDA, std::string("adjoint launch: ") + cudaGetErrorString(cudaGetLastError()));
+    if (!plain) {
+      aa.n_steps = len;
+      aa.s0 = s0;
+      if (launch_adjoint(aa, best_C, adj_ncl, adj_threads, adj_smem, s->st))
+        return fail(SRS_ERR_CUDA, std::string("adjoint launch: ") + cudaGetErrorString(cudaGetLastError()));
+      s->launches++;
+      return SRS_OK;
+    }
+    // dL/dF of the tick at global step n of this segment, or null
+    auto coef_at = [&](int64_t n) -> const double* {
+      if (n <= s0 || n % te) return nullptr;
+      return coef + (size_t)(n / te - s0 / te - 1) * R * ns;
+    };
+    auto slot = [&](int t) { return (size_t)t * R * NE; };
+    int cur = 0;
+    pa.tu = traj_u + slot(len - 1);
+    pa.coef_cur = coef_at(s0 + len);
+    pa.nxt = pub[cur];
+    if (launch_adjp_publish(pa, adjp_by, s->st)) return fail(SRS_ERR_CUDA, "adjoint publish launch failed");
     s->launches++;
+    for (int t = len; t >= 1; --t) {
+      pa.pub = pub[cur];
+      pa.nxt = pub[cur ^ 1];
+      pa.tu = traj_u + slot(t - 1);
+      pa.tig = traj_ig + slot(t - 1);
+      pa.tprev = t > 1 ? traj_u + slot(t - 2) : nullptr;
+      pa.rec = traj_ch + (size_t)(t - 1) * R * W;
+      pa.coef_next = t > 1 ? coef_at(s0 + t - 1) : nullptr;
+      pa.last = t == 1;
+      if (launch_adjp_step(pa, adjp_by, s->st))
+        return fail(SRS_ERR_CUDA, std::string("adjoint step launch: ") + cudaGetErrorString(cudaGetLastError()));
+      s->launches++;
+      cur ^= 1;
+    }
+    return SRS_OK;
+  };
+
+  // ---- forward with checkpoints, reverse sweep ---------------------------------
+  // rev(l, a, b): reverses steps [a, b) from the live state x_a.  Level l
+  // cuts the range into pieces of K * fan^(L-1-l) steps, runs forward to the
+  // start of its last piece keeping the starts of the others, recurses into
+  // the last piece from the live state, then restores and recurses into the
+  // others from last to first.  At level L a piece is one segment: recorded,
+  // then reversed.  The first segment recorded is the last of the run, whose
+  // end state is kept as the final state (restored at the end).
+  int64_t piece_steps[16];
+  {
+    int64_t q = K;
+    for (int l = L - 1; l >= 0; --l) {
+      piece_steps[l] = q;
+      if (l > 0) q = (q > INT64_MAX / fan) ? INT64_MAX : q * fan;
+    }
   }
-  SRS_TRY(snap_copy(s, ck[nseg], false));
+  bool fin_saved = false;
+  std::function<int(int, int64_t, int64_t)> rev = [&](int l, int64_t a, int64_t b) -> int {
+    if (l == L) {
+      const int len = (int)(b - a);
+      SRS_TRY(record_live(len));
+      if (!fin_saved) {
+        SRS_TRY(snap_copy(s, fin, true));
+        std::vector<RealCtl> ctl(R);
+        SRS_CUDA(cudaMemcpyAsync(ctl.data(), fin.ctl, sizeof(RealCtl) * R, cudaMemcpyDeviceToHost, s->st));
+        SRS_CUDA(cudaStreamSynchronize(s->st));
+        for (auto& c : ctl) {
+          if (c.status & 1u) return fail(SRS_ERR_NONFINITE, "a realization produced a non-finite Ca value");
+          if (c.done) return fail(SRS_ERR_STATE, "a realization is finished; reset it before the adjoint");
+        }
+        fin_saved = true;
+      }
+      return reverse_segment(a, len);
+    }
+    const int64_t q = piece_steps[l];
+    const int64_t p = (b - a + q - 1) / q;
+    for (int64_t i = 0; i + 1 < p; ++i) {
+      SRS_TRY(snap_copy(s, lv[l][i], true));
+      SRS_TRY(advance_live(q));
+    }
+    SRS_TRY(rev(l + 1, a + (p - 1) * q, b));
+    for (int64_t i = p - 2; i >= 0; --i) {
+      SRS_TRY(snap_copy(s, lv[l][i], false));
+      SRS_TRY(rev(l + 1, a + i * q, a + (i + 1) * q));
+    }
+    return SRS_OK;
+  };
+  SRS_TRY(rev(0, 0, n_steps));
+  SRS_TRY(snap_copy(s, fin, false));
   std::vector<double> loss_t((size_t)std::max<int64_t>(n_ticks, 1) * R * ns);
   SRS_CUDA(cudaMemcpyAsync(loss_t.data(), loss, sizeof(double) * loss_t.size(), cudaMemcpyDeviceToHost,
                            s->st));
-  SRS_CUDA(cudaMemcpyAsync(out->grad, grad, sizeof(double) * R * SRS_N_ADJ, cudaMemcpyDeviceToHost, s->st));
+  std::vector<double> part_h;
+  if (plain) {
+    part_h.resize((size_t)R * adjp_by * SRS_N_ADJ);
+    SRS_CUDA(cudaMemcpyAsync(part_h.data(), part, sizeof(double) * part_h.size(), cudaMemcpyDeviceToHost,
+                             s->st));
+  } else {
+    SRS_CUDA(cudaMemcpyAsync(out->grad, grad, sizeof(double) * R * SRS_N_ADJ, cudaMemcpyDeviceToHost, s->st));
+  }
   std::vector<float4> hl, hc;
   std::vector<float> hi, hci;
   if (out->grad_state) {
@@ -2407,11 +2666,20 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   }
   SRS_CUDA(cudaStreamSynchronize(s->st));
   SRS_CUDA(cudaGetLastError());
+  if (plain) {  // the blocks' rows in a fixed order
+    const double dt = (double)pa.k.dt;
+    for (int r = 0; r < R; ++r)
+      for (int p = 0; p < SRS_N_ADJ; ++p) {
+        double v = 0.0;
+        for (int b = 0; b < adjp_by; ++b) v += part_h[((size_t)r * adjp_by + b) * SRS_N_ADJ + p];
+        out->grad[(size_t)r * SRS_N_ADJ + p] = v * dt;
+      }
+  }
   for (int r = 0; r < R; ++r) {  // ticks in time order: the same sum for any segmentation
-    double L = 0.0;
+    double Ls = 0.0;
     for (int64_t t = 0; t < n_ticks; ++t)
-      for (int i = 0; i < ns; ++i) L += loss_t[((size_t)t * R + r) * ns + i];
-    out->loss[r] = L;
+      for (int i = 0; i < ns; ++i) Ls += loss_t[((size_t)t * R + r) * ns + i];
+    out->loss[r] = Ls;
   }
   if (out->grad_state) {
     const int N = s->N;
@@ -2419,13 +2687,13 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       double* g = out->grad_state + (size_t)r * 6 * N;
       for (int j = 0; j < N; ++j) {
         const size_t e = (size_t)r * NE + s->eng_of_ref[j];
-        const float4 L = hl[e], Cc = hc[e];
+        const float4 Lv = hl[e], Cc = hc[e];
         const double li = (double)hi[e] - (double)hci[e];
         const bool jsr = s->m.domain[j] == DOMAIN_JSR;
-        g[SP_CA * (size_t)N + j] = (double)L.x - (double)Cc.x;
-        g[SP_ATP * (size_t)N + j] = (double)L.y - (double)Cc.y;
-        g[SP_CMDN * (size_t)N + j] = (double)L.z - (double)Cc.z;
-        g[SP_DYE * (size_t)N + j] = (double)L.w - (double)Cc.w;
+        g[SP_CA * (size_t)N + j] = (double)Lv.x - (double)Cc.x;
+        g[SP_ATP * (size_t)N + j] = (double)Lv.y - (double)Cc.y;
+        g[SP_CMDN * (size_t)N + j] = (double)Lv.z - (double)Cc.z;
+        g[SP_DYE * (size_t)N + j] = (double)Lv.w - (double)Cc.w;
         g[SP_TRPN * (size_t)N + j] = (!jsr && s->m.tropc[j]) ? li : 0.0;
         g[SP_CSQN * (size_t)N + j] = jsr ? li : 0.0;
       }
@@ -2440,6 +2708,17 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     for (int p = 0; p < SRS_N_ADJ; ++p)
       if (!std::isfinite(out->grad[(size_t)r * SRS_N_ADJ + p]))
         return fail(SRS_ERR_NONFINITE, "non-finite adjoint gradient");
+  return SRS_OK;
+}
+
+int srs_adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, int* segment_steps, int* levels,
+                     int64_t* forward_steps) {
+  if (!s || !d) return fail(SRS_ERR_INPUT, "null argument");
+  AdjPlan pl;
+  SRS_TRY(adjoint_plan(s, d, &pl));
+  if (segment_steps) *segment_steps = pl.K;
+  if (levels) *levels = pl.L;
+  if (forward_steps) *forward_steps = pl.forward_steps;
   return SRS_OK;
 }
 

@@ -76,6 +76,13 @@ struct Plain32Args {
   ChanState CS;
   unsigned int* counters;
   int32_t pf_rows;  // split form: element blocks ahead whose state is prefetched into L2
+  // trajectory recording for the adjoint (null: none): the slot of this
+  // step, [R][N] x_{n-1} and (immobile buffer, Ca rate before the
+  // rapid-buffer factor), and [R][NR + 2 NL + 1] the channel states the step
+  // used (RyR, LCC, LCC voltage state, voltage selector)
+  float4* traj_u;
+  float2* traj_ig;
+  int32_t* traj_ch;
 };
 // Meshes of at least this many elements take the split form of the plain
 // FP32 step (element update, then gating, as two launches).
@@ -243,6 +250,45 @@ struct AdjTickArgs {
   double* loss;          // [n_ticks][R][n_samples]: loss terms of every tick
   int32_t mean_trace;    // loss on the realizations' mean trace (target [n_ticks][n_samples])
 };
+
+// Reverse step of the plain FP32 engine's adjoint (k_adjoint_plain.cu); all
+// arrays [R][N] in the plain engine's numbering unless noted.
+struct AdjPlainArgs {
+  int32_t N, R, NR, NL, n_samples;
+  int32_t last;            // t == 1: write the boundary lambda instead of nxt
+  const float4* aT;        // [N] coefficient of this element in each neighbour's row
+  const int4* nb;          // [N] neighbours
+  const float2* bs;        // [N] (bsl, TropC in the sign bit; sum a + kb, JSR in the sign bit)
+  const uint32_t* flags;   // [N] bit 2: the element carries channel entries
+  const int32_t* ch_ptr;
+  const ChanEntry32* ch_list;
+  const int32_t* ryr_cleft;
+  const int32_t* ryr_jsr;
+  const float* ryr_s_cl;   // +1/V0 of each RyR's cleft element
+  const float* ryr_s_js;   // -1/V0 of each RyR's JSR element
+  const float4* tu;        // trajectory slot of x_{n-1}
+  const float2* tig;       // (immobile buffer, Ca rate) of x_{n-1}
+  const float4* tprev;     // slot of x_{n-2} (t > 1)
+  const int32_t* rec;      // [R][NR + 2 NL + 1] channel states of step n
+  const double* coef_cur;  // publish: dL/dF of the tick at s1 ([R][n_samples]) or null
+  const double* coef_next; // step: dL/dF of the tick at n - 1 or null
+  const int32_t* wt_ptr;   // [N + 1] element -> line-scan samples
+  const int32_t* wt_idx;
+  const double* wt_w;
+  const float4* pub;
+  float4* nxt;
+  float* lam_c;
+  float* lam_im;
+  float* lam_cim;
+  float4* lam_c4;
+  float4* lam;             // boundary lambda (Ca, ATP, CMDN, dye)
+  double* part;            // [R][blocks][SRS_N_ADJ] FP64 gradient rows of the blocks
+  Consts32 k;
+  AdjConsts ak;
+};
+int adjp_blocks_per_realization(int N, int R, int n_sm);
+int launch_adjp_publish(const AdjPlainArgs& a, int blocks, cudaStream_t st);
+int launch_adjp_step(const AdjPlainArgs& a, int blocks, cudaStream_t st);
 
 size_t adjoint_smem_bytes(int P, int n_chtet, int n_entries, bool own_in_smem, bool stage);
 int launch_adjoint(const AdjArgs& a, int C, int n_clusters, int threads, size_t smem,

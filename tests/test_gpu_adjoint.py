@@ -47,7 +47,7 @@ def case(srs):
     return dict(p=p, g=g, sim=sim, f0=f0, start=start, target=target, loss=loss, grad=grad, gs=gs)
 
 
-def test_adjoint_matches_fp64_oracle(srs, oracle, case):
+def _check_against_oracle(srs, oracle, case, loss, grad, gs_all):
     from oracle import Mesh
     p, g = case["p"], case["g"]
     W, pad = linescan_weights(g)
@@ -58,20 +58,85 @@ def test_adjoint_matches_fp64_oracle(srs, oracle, case):
         st = case["start"][r]
         L, go, lam0 = m.adjoint(ints, st["states"], st, seed, N_STEPS, TICK, W, pad, case["f0"],
                                 case["target"][r], grad_state=True)
-        assert abs(case["loss"][r] - L) <= 1e-5 * L
+        assert abs(loss[r] - L) <= 1e-5 * L
         scale = np.abs(go)
         for k in range(srs.N_ADJ):
             if scale[k] == 0:
                 continue
-            assert abs(case["grad"][r, k] - go[k]) <= 1e-3 * scale[k], (r, srs.ADJ_PARAMS[k],
-                                                                       case["grad"][r, k], go[k])
+            assert abs(grad[r, k] - go[k]) <= 1e-3 * scale[k], (r, srs.ADJ_PARAMS[k], grad[r, k], go[k])
         # dL/dS0: species by species, relative to the largest sensitivity
-        gs = case["gs"][r].reshape(-1)
+        gs = gs_all[r].reshape(-1)
         for sp in range(6):
             a, b = gs[sp * N:(sp + 1) * N], lam0[sp * N:(sp + 1) * N]
             ref = np.abs(b).max()
             if ref > 0:
                 assert np.abs(a - b).max() <= 1e-3 * ref, (r, sp)
+
+
+def test_adjoint_matches_fp64_oracle(srs, oracle, case):
+    _check_against_oracle(srs, oracle, case, case["loss"], case["grad"], case["gs"])
+
+
+@pytest.fixture(scope="module")
+def plain_case(srs, case):
+    """The same adjoint on the plain FP32 engine (one launch per reverse step,
+    every array in HBM): the form for meshes too large for the resident one."""
+    _, sim = _start(srs, case["p"], srs.FP32, srs.ENGINE_PLAIN)
+    loss, grad, gs = sim.adjoint(N_STEPS, TICK, case["f0"], case["target"], checkpoint_every=K,
+                                 grad_state=True)
+    return dict(sim=sim, loss=loss, grad=grad, gs=gs)
+
+
+def test_plain_engine_adjoint_matches_fp64_oracle(srs, oracle, case, plain_case):
+    _check_against_oracle(srs, oracle, case, plain_case["loss"], plain_case["grad"], plain_case["gs"])
+
+
+def test_plain_engine_adjoint_agrees_with_resident(srs, case, plain_case):
+    """Both FP32 engines run the same trajectory (bit-exact with the FP32
+    restatement); the line-scan sums and the gradient's FP32 partial sums are
+    grouped differently (1e-12 on the loss, 1e-5 on the gradients)."""
+    assert np.allclose(plain_case["loss"], case["loss"], rtol=1e-12, atol=0)
+    scale = np.abs(case["grad"]).max(0)
+    assert np.all(np.abs(plain_case["grad"] - case["grad"]) <= 1e-5 * scale[None, :])
+    N = case["g"].n_ele
+    for r in range(len(SEEDS)):
+        a, b = plain_case["gs"][r].reshape(-1), case["gs"][r].reshape(-1)
+        for sp in range(6):
+            ref = np.abs(b[sp * N:(sp + 1) * N]).max()
+            assert np.abs(a[sp * N:(sp + 1) * N] - b[sp * N:(sp + 1) * N]).max() <= 1e-5 * ref, (r, sp)
+
+
+@pytest.mark.parametrize("engine", ["RESIDENT", "PLAIN"])
+@pytest.mark.parametrize("K2,max_ck,levels", [(50, 6, 2), (25, 6, 3), (25, 0, 1)])
+def test_multilevel_checkpoints_give_the_same_result(srs, case, plain_case, engine, K2, max_ck, levels):
+    """Fewer snapshots than segments: the sweep takes snapshots on several
+    levels and recomputes the forward run more often, from the same states
+    with the same gating draws, so the trajectory, the loss and dL/dS0 are
+    bit-identical to the one-level sweep (the plain engine's gradient too: its
+    per-step block sums do not depend on the segmentation)."""
+    ref = case if engine == "RESIDENT" else plain_case
+    _, sim = _start(srs, case["p"], srs.FP32, getattr(srs, "ENGINE_" + engine))
+    seg, lev, fwd = sim.adjoint_plan(N_STEPS, TICK, checkpoint_every=K2, max_checkpoints=max_ck)
+    assert (seg, lev) == (K2, levels)
+    assert fwd > N_STEPS if levels > 1 else fwd == N_STEPS + (N_STEPS // K2 - 1) * K2
+    loss, grad, gs = sim.adjoint(N_STEPS, TICK, case["f0"], case["target"], checkpoint_every=K2,
+                                 max_checkpoints=max_ck, grad_state=True)
+    assert np.array_equal(loss, ref["loss"])
+    assert np.array_equal(gs, ref["gs"])
+    if engine == "PLAIN":
+        assert np.array_equal(grad, ref["grad"])
+    else:
+        assert np.allclose(grad, ref["grad"], rtol=1e-5, atol=0)
+    # the state after the call is the one after n_steps
+    for r in range(len(SEEDS)):
+        assert np.array_equal(sim.get_state(r)["states"], ref["sim"].get_state(r)["states"])
+
+
+def test_too_few_checkpoints_are_rejected(srs, case):
+    _, sim = _start(srs, case["p"], srs.FP32, srs.ENGINE_PLAIN)
+    with pytest.raises(srs.SrsError) as e:
+        sim.adjoint(N_STEPS, TICK, case["f0"], case["target"], checkpoint_every=50, max_checkpoints=2)
+    assert e.value.status == -10  # SRS_ERR_NOMEM: no plan with 3 snapshots covers 12 segments
 
 
 def test_adjoint_matches_fp64_finite_differences(srs, case):
@@ -161,7 +226,7 @@ def test_adjoint_leaves_the_state_after_n_steps(srs, case):
 
 def test_adjoint_rejects_unsupported_configurations(srs, case):
     p = case["p"]
-    _, plain = _start(srs, p, srs.FP32, srs.ENGINE_PLAIN)
+    _, plain = _start(srs, p, srs.FP64, srs.ENGINE_PLAIN)
     with pytest.raises(srs.SrsError) as e:
         plain.adjoint(10, 5, case["f0"])
     assert e.value.status == -6  # SRS_ERR_UNSUPPORTED
