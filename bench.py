@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--no-config0", action="store_true", help="skip the single-spark leg")
     ap.add_argument("--config0-ms", type=float, default=2.0)
     ap.add_argument("--config4-steps", type=int, default=4096)
+    ap.add_argument("--config4-realizations", type=int, default=32,
+                    help="realizations of the large-site leg (32: the workload; fewer for profiling)")
     ap.add_argument("--config4-adjoint-steps", type=int, default=1024,
                     help="steps of the large-site adjoint sample (0: skip it)")
     ap.add_argument("--only", choices=["adjoint", "config0", "config2", "config4"], default=None,
@@ -497,7 +499,7 @@ def config4_site(srs, args):
     t0 = time.perf_counter()
     g = srs.Grid(p, base)
     t_load = time.perf_counter() - t0
-    R = 32
+    R = args.config4_realizations
     sim = srs.Simulation(g, p, R, srs.FP32, srs.ENGINE_PLAIN, seeds=list(range(1, R + 1)))
     sim.reset()
     tot0 = sim.total_ca()
@@ -514,8 +516,8 @@ def config4_site(srs, args):
         del sim
         adj = config4_adjoint(srs, base, R, args.config4_adjoint_steps, ms / n)
     return {"adjoint": adj, "workload": "config4: multi-site release unit, %d tets (%d RyR in 5 clusters, %d LCC), "
-                        "32 realizations, DefaultSpark protocol, FP32 plain engine, %d timed steps"
-                        % (n_el, rep_["n_ryr"], rep_["n_lcc"], n),
+                        "%d realizations, DefaultSpark protocol, FP32 plain engine, %d timed steps"
+                        % (n_el, rep_["n_ryr"], rep_["n_lcc"], R, n),
             "value": R * n * DT_MS / (ms / 1e3), "unit": UNIT, "ms_per_time_step": ms / n,
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
@@ -560,7 +562,7 @@ def config4_adjoint(srs, base, R, n, fwd_ms_per_step):
     _, f0 = sim.linescan()
     K = 64
     kw = dict(checkpoint_every=K, flags=srs.ADJ_MEAN_TRACE)
-    sim.adjoint(2 * K, te, f0, target[:2 * K // te], **kw)  # warm-up
+    sim.adjoint(n, te, f0, target, **kw)  # warm-up (and the work buffers of this size)
     sim.reset()
     seg, lev, fwd_steps = sim.adjoint_plan(n, te, checkpoint_every=K)
     t0 = time.perf_counter()

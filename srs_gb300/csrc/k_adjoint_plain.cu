@@ -42,18 +42,15 @@ __device__ __forceinline__ float plain_injection(const AdjPlainArgs& a, const do
 }  // namespace
 
 // Start of a segment: publish lambda_{s1} (with the tick injection of step
-// s1) from the boundary arrays.  tu: the trajectory slot of x_{s1-1}.
+// s1) from the boundary arrays.  ib: 1 / B(x_{s1-1}) from the trajectory.
 __global__ void __launch_bounds__(ADJP_THREADS) k_adjp_publish(AdjPlainArgs a) {
   const int r = blockIdx.x;
   const double* coef = a.coef_cur ? a.coef_cur + (size_t)r * a.n_samples : nullptr;
   for (int j = blockIdx.y * blockDim.x + threadIdx.x; j < a.N; j += gridDim.y * blockDim.x) {
     const size_t o = (size_t)r * a.N + j;
     const float4 L = a.lam[o];
-    const float2 bs = a.bs[j];
-    const bool jsr = (__float_as_uint(bs.y) >> 31) != 0;
-    const float c = (jsr ? a.k.c0j : a.k.c0) + a.tu[o].x;
     const float inj = coef ? plain_injection(a, coef, j) : 0.0f;
-    a.nxt[o] = make_float4(L.x * sl_inv_factor(a.k, fabsf(bs.x), c), L.y, L.z, L.w + inj);
+    a.nxt[o] = make_float4(L.x * a.ib[o], L.y, L.z, L.w + inj);
     a.lam_c[o] = L.x;
   }
 }
@@ -150,9 +147,8 @@ __global__ void __launch_bounds__(ADJP_THREADS) k_adjp_step(AdjPlainArgs a) {
     a.lam_cim[o] = ci;
     a.lam_c4[o] = cm;
     if (!a.last) {
-      const float cprev = (jsr ? k.c0j : k.c0) + a.tprev[o].x;
       const float inj = coef ? plain_injection(a, coef, j) : 0.0f;
-      a.nxt[o] = make_float4(L.x * sl_inv_factor(k, bsl, cprev), L.y, L.z, L.w + inj);
+      a.nxt[o] = make_float4(L.x * a.ib[o], L.y, L.z, L.w + inj);
       a.lam_c[o] = L.x;
     } else {
       a.lam[o] = L;

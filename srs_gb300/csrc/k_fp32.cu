@@ -25,6 +25,7 @@
 //     while the other warps update everything else — one cluster barrier per
 //     time step, and the termination decision is known at that barrier.
 #include "k_resident.cuh"
+#include "srs_adjoint.cuh"
 #include "srs_engine.h"
 #include "srs_fp32_update.cuh"
 #include "srs_protocol.cuh"
@@ -81,6 +82,7 @@ __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int
                  a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo, &g);
       a.traj_u[(size_t)r * N + j] = x;
       a.traj_ig[(size_t)r * N + j] = make_float2(im, g);
+      a.traj_ib[(size_t)r * N + j] = sl_inv_factor(a.k, a.bsl[j], ((fl & 1u) ? a.k.c0j : a.k.c0) + x.x);
     } else {
       tet_update(a.k, M[j], I[j], M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
                  a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo);
@@ -161,14 +163,6 @@ __global__ void __launch_bounds__(256) k_plain32_step(Plain32Args a) {
   if (!s_last) return;
   __threadfence();
   plain32_gate<TRAJ>(a, r, s_nb);
-}
-
-// Bulk prefetch into L2 of [p, p + bytes) within an array that starts on a
-// 16-byte boundary: the span is trimmed inward to 16-byte boundaries.
-__device__ __forceinline__ void prefetch_span(const void* p, size_t bytes) {
-  const uintptr_t b0 = ((uintptr_t)p + 15) & ~(uintptr_t)15;
-  const uintptr_t b1 = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
-  if (b1 > b0) l2_prefetch((const void*)b0, (uint32_t)(b1 - b0));
 }
 
 // Large meshes: the element update alone, without the gating code, so it

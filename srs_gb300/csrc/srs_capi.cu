@@ -2168,7 +2168,7 @@ int adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, AdjPlan* pl) {
   const int ns = s->ls.n_samples;
   const int64_t n_steps = d->n_steps, n_ticks = n_steps / te;
   // bytes: one recorded step, one snapshot of the whole state, lambda
-  const size_t step_b = (size_t)R * (NE * 24 + (size_t)W * 4);
+  const size_t step_b = (size_t)R * (NE * (plain ? 28 : 24) + (size_t)W * 4);
   const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
                         (size_t)R * sizeof(RealCtl);
   const size_t lam_b = (size_t)R * NE * (plain ? 76 : 44);
@@ -2191,7 +2191,7 @@ int adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, AdjPlan* pl) {
   }
   const int64_t nseg = (n_steps + K - 1) / K;
   // memory: snapshots, one segment of trajectory, lambda, tick coefficients
-  const size_t traj_b = (size_t)(K + 1) * R * NE * 24 + (size_t)K * R * W * 4;
+  const size_t traj_b = (size_t)(K + 1) * R * NE * 24 + (size_t)K * R * (W + (plain ? NE : 0)) * 4;
   const size_t fixed = traj_b + lam_b + (size_t)(K / te + 2) * R * ns * 8 +
                        (size_t)R * std::max<int64_t>(n_ticks, 1) * ns * 16;
   const size_t usable = free_b / 10 * 9;
@@ -2278,9 +2278,11 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
   float4* traj_u;
   float2* traj_ig;
   int32_t* traj_ch;
+  float* traj_ib = nullptr;  // plain engine: 1 / B of every recorded state
   SRS_TRY(sc.get(&traj_u, (size_t)(K + 1) * R * NE));
   SRS_TRY(sc.get(&traj_ig, (size_t)(K + 1) * R * NE));
   SRS_TRY(sc.get(&traj_ch, (size_t)K * R * W));
+  if (plain) SRS_TRY(sc.get(&traj_ib, (size_t)K * R * NE));
   float4 *lam, *lam_c4;
   float *lam_im, *lam_cim;
   SRS_TRY(sc.get(&lam, (size_t)R * NE));
@@ -2369,6 +2371,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       a.traj_u = traj_u + (size_t)t * R * NE;
       a.traj_ig = traj_ig + (size_t)t * R * NE;
       a.traj_ch = traj_ch + (size_t)t * R * W;
+      a.traj_ib = traj_ib + (size_t)t * R * NE;
       if (launch_plain32_step(a, s->st))
         return fail(SRS_ERR_CUDA, std::string("trajectory step: ") + cudaGetErrorString(cudaGetLastError()));
       s->launches += plain32_kernels_per_step(a);
@@ -2570,7 +2573,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     };
     auto slot = [&](int t) { return (size_t)t * R * NE; };
     int cur = 0;
-    pa.tu = traj_u + slot(len - 1);
+    pa.ib = traj_ib + slot(len - 1);
     pa.coef_cur = coef_at(s0 + len);
     pa.nxt = pub[cur];
     if (launch_adjp_publish(pa, adjp_by, s->st)) return fail(SRS_ERR_CUDA, "adjoint publish launch failed");
@@ -2580,7 +2583,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
       pa.nxt = pub[cur ^ 1];
       pa.tu = traj_u + slot(t - 1);
       pa.tig = traj_ig + slot(t - 1);
-      pa.tprev = t > 1 ? traj_u + slot(t - 2) : nullptr;
+      pa.ib = t > 1 ? traj_ib + slot(t - 2) : nullptr;
       pa.rec = traj_ch + (size_t)(t - 1) * R * W;
       pa.coef_next = t > 1 ? coef_at(s0 + t - 1) : nullptr;
       pa.last = t == 1;

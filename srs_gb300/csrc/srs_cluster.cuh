@@ -43,6 +43,14 @@ __device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Bulk prefetch into L2 of [p, p + bytes) within an array that starts on a
+// 16-byte boundary: the span is trimmed inward to 16-byte boundaries.
+__device__ __forceinline__ void prefetch_span(const void* p, size_t bytes) {
+  const uintptr_t b0 = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+  const uintptr_t b1 = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+  if (b1 > b0) l2_prefetch((const void*)b0, (uint32_t)(b1 - b0));
+}
+
 // mbarrier and bulk asynchronous copies (global -> this CTA's shared memory).
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");

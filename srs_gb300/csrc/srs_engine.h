@@ -83,6 +83,7 @@ struct Plain32Args {
   float4* traj_u;
   float2* traj_ig;
   int32_t* traj_ch;
+  float* traj_ib;  // [R][N] 1 / B(x_{n-1}), B the rapid-buffer factor
 };
 // Meshes of at least this many elements take the split form of the plain
 // FP32 step (element update, then gating, as two launches).
@@ -148,6 +149,7 @@ struct ResidentArgs {
   float4* traj_u;
   float2* traj_ig;
   int32_t* traj_ch;
+  float* traj_ib;  // [R][N] 1 / B(x_{n-1}), B the rapid-buffer factor
 };
 // Line scan: F[r][i] = pad[i] + sum_q w[q] * dye(col[q]) over ptr[i]..ptr[i+1].
 struct LinescanArgs {
@@ -268,7 +270,8 @@ struct AdjPlainArgs {
   const float* ryr_s_js;   // -1/V0 of each RyR's JSR element
   const float4* tu;        // trajectory slot of x_{n-1}
   const float2* tig;       // (immobile buffer, Ca rate) of x_{n-1}
-  const float4* tprev;     // slot of x_{n-2} (t > 1)
+  const float* ib;         // [R][N] 1 / B of the state the published slots divide by:
+                           // x_{n-2} (step, t > 1) or x_{s1-1} (publish)
   const int32_t* rec;      // [R][NR + 2 NL + 1] channel states of step n
   const double* coef_cur;  // publish: dL/dF of the tick at s1 ([R][n_samples]) or null
   const double* coef_next; // step: dL/dF of the tick at n - 1 or null
