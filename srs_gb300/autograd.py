@@ -23,14 +23,16 @@ import srs_gb300 as srs
 
 class AdjointProblem:
     def __init__(self, mesh_base, params, seeds, linescan, n_steps, tick_every, target=None,
-                 checkpoint_every=0, cluster_size=0, mean_trace=False):
+                 checkpoint_every=0, cluster_size=0, mean_trace=False, engine=None):
         self.mesh_base = str(mesh_base)
         self.params = params.copy()
         self.seeds = [int(s) for s in seeds]
         self.linescan = dict(linescan)
         self.n_steps, self.tick_every = int(n_steps), int(tick_every)
         self.checkpoint_every, self.cluster_size = int(checkpoint_every), int(cluster_size)
-        sim = self._sim(self.params, srs.FP32, srs.ENGINE_RESIDENT, reset=True)
+        # FP32 engine of the adjoint: resident, or plain for meshes too large for it
+        self.engine = srs.ENGINE_RESIDENT if engine is None else int(engine)
+        sim = self._sim(self.params, srs.FP32, self.engine, reset=True)
         _, self.f0 = sim.linescan()
         self.start = [sim.get_state(r) for r in range(len(self.seeds))]
         n_ticks = self.n_steps // self.tick_every
@@ -60,7 +62,7 @@ class AdjointProblem:
         return sim
 
     def loss_and_grad(self, theta):
-        sim = self._sim(self.params_at(theta), srs.FP32, srs.ENGINE_RESIDENT)
+        sim = self._sim(self.params_at(theta), srs.FP32, self.engine)
         loss, grad, _ = sim.adjoint(self.n_steps, self.tick_every, self.f0, self.target,
                                     checkpoint_every=self.checkpoint_every,
                                     flags=srs.ADJ_MEAN_TRACE if self.mean_trace else 0)

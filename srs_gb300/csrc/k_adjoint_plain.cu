@@ -17,7 +17,8 @@
 //     immobile buffer's lambda, their Kahan compensation);
 //   * lam: the full lambda at the segment boundaries.
 // The transposed diffusion operator gathers the four neighbours' slots with
-// the transposed coefficients aT; Dirichlet faces (kb) join the diagonal.
+// the transposed coefficients aT; Dirichlet faces (kb) join the diagonal, and
+// their sources of the mobile buffers add kon/koff gradient terms.
 //
 // Parameter gradients: each thread sums its elements' terms of the step in
 // FP32, the block reduces them (one realization per block), and the block's
@@ -111,6 +112,18 @@ __global__ void __launch_bounds__(ADJP_THREADS) k_adjp_step(AdjPlainArgs a) {
     const AdjTerms lt = adj_local(k, ak, x, ig.x, me, li, jsr, trpn, Sc, Sa, Sm, Sy, g);
     float oc = lt.oc, dG = lt.dG;
     const float c = lt.c;
+    if (a.kb) {
+      // the Dirichlet source of the mobile buffers (their resting bound level)
+      const float kbj = a.kb[j];
+      if (kbj != 0.0f) {
+        g[SRS_ADJ_K_ON_DYE] = fmaf(me.w * kbj, ak.kb_on[0], g[SRS_ADJ_K_ON_DYE]);
+        g[SRS_ADJ_K_OFF_DYE] = fmaf(me.w * kbj, ak.kb_off[0], g[SRS_ADJ_K_OFF_DYE]);
+        g[SRS_ADJ_K_ON_ATP] = fmaf(me.y * kbj, ak.kb_on[1], g[SRS_ADJ_K_ON_ATP]);
+        g[SRS_ADJ_K_OFF_ATP] = fmaf(me.y * kbj, ak.kb_off[1], g[SRS_ADJ_K_OFF_ATP]);
+        g[SRS_ADJ_K_ON_CMDN] = fmaf(me.z * kbj, ak.kb_on[2], g[SRS_ADJ_K_ON_CMDN]);
+        g[SRS_ADJ_K_OFF_CMDN] = fmaf(me.z * kbj, ak.kb_off[2], g[SRS_ADJ_K_OFF_CMDN]);
+      }
+    }
     if (a.flags[j] & 4u) {
       // release flux of this element's channels, with the gating of step n
       for (int q = a.ch_ptr[j]; q < a.ch_ptr[j + 1]; ++q) {

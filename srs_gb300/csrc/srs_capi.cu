@@ -2397,6 +2397,16 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     ak.serca_per_ap = 2e-3f;
     ak.v_cell = (float)s->p.reals[R_V_CELL];
     ak.inv_khi = (float)(1.0 / s->p.reals[R_K_D_SL_HI]);
+    // Dirichlet sources D kb Bv of dye, ATP, CMDN, Bv = c0 B / (Kd + c0)
+    const double* Rr = s->p.reals;
+    const int dq[3] = {R_D_DYE, R_D_ATP, R_D_CMDN}, onq[3] = {R_K_ON_DYE, R_K_ON_ATP, R_K_ON_CMDN},
+              offq[3] = {R_K_OFF_DYE, R_K_OFF_ATP, R_K_OFF_CMDN};
+    const double bv[3] = {rv.dye, rv.atp, rv.cmdn};
+    for (int q = 0; q < 3; ++q) {
+      const double kon = Rr[onq[q]], Kd = Rr[offq[q]] / kon, den = Kd + Rr[R_C_0_CA];
+      ak.kb_on[q] = (float)(Rr[dq[q]] * bv[q] * Kd / (kon * den));
+      ak.kb_off[q] = (float)(-Rr[dq[q]] * bv[q] / (kon * den));
+    }
   }
   SRS_CUDA(cudaMemsetAsync(lam, 0, sizeof(float4) * R * NE, s->st));
   SRS_CUDA(cudaMemsetAsync(lam_c4, 0, sizeof(float4) * R * NE, s->st));
@@ -2513,6 +2523,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     pa.aT = s->d_adjp_aT;
     pa.nb = s->a32.nb;
     pa.bs = s->d_adjp_bs;
+    pa.kb = s->a32.kb;
     pa.flags = s->a32.flags;
     pa.ch_ptr = s->a32.chan_ptr;
     pa.ch_list = s->a32.chan_list;

@@ -194,6 +194,12 @@ struct AdjConsts {
   float serca_per_ap;  // dF_Ca/dA_P = -serca_per_ap * v_cycle / B
   float v_cell;        // V_CELL
   float inv_khi;       // 1 / K_D_SL_HI
+  // Dirichlet faces hold the mobile buffers at their resting bound level
+  // c0 B / (Kd + c0), Kd = koff / kon, so their source D kb Bv depends on kon
+  // and koff: d(source)/dkon = kb * kb_on[q], d(source)/dkoff = kb * kb_off[q]
+  // (q: dye, ATP, CMDN)
+  float kb_on[3];
+  float kb_off[3];
 };
 
 struct AdjArgs {
@@ -261,6 +267,7 @@ struct AdjPlainArgs {
   const float4* aT;        // [N] coefficient of this element in each neighbour's row
   const int4* nb;          // [N] neighbours
   const float2* bs;        // [N] (bsl, TropC in the sign bit; sum a + kb, JSR in the sign bit)
+  const float* kb;         // [N] Dirichlet rate kb, or null when the mesh has none
   const uint32_t* flags;   // [N] bit 2: the element carries channel entries
   const int32_t* ch_ptr;
   const ChanEntry32* ch_list;

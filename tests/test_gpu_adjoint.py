@@ -51,7 +51,8 @@ def _check_against_oracle(srs, oracle, case, loss, grad, gs_all):
     from oracle import Mesh
     p, g = case["p"], case["g"]
     W, pad = linescan_weights(g)
-    m = Mesh(oracle, GOLDEN_MESH, 1, np.array(p.reals[:]))
+    noflux = int(p.ints[srs.I["FLAG_NO_FLUX_BOUNDARY"]])
+    m = Mesh(oracle, GOLDEN_MESH, noflux, np.array(p.reals[:]))
     ints = np.array(p.ints[:], np.int32)
     N = g.n_ele
     for r, seed in enumerate(SEEDS):
@@ -89,6 +90,20 @@ def plain_case(srs, case):
 
 def test_plain_engine_adjoint_matches_fp64_oracle(srs, oracle, case, plain_case):
     _check_against_oracle(srs, oracle, case, plain_case["loss"], plain_case["grad"], plain_case["gs"])
+
+
+def test_plain_engine_adjoint_with_dirichlet_faces_matches_fp64_oracle(srs, oracle, case):
+    """The plain engine also runs meshes with Dirichlet faces (on cytosolic
+    elements; the resident engine needs no-flux boundaries): their rate kb
+    joins the diagonal of the transposed operator and the diffusion
+    gradients."""
+    p = case["p"].copy()
+    p.ints[srs.I["FLAG_NO_FLUX_BOUNDARY"]] = 0
+    g, sim = _start(srs, p, srs.FP32, srs.ENGINE_PLAIN)
+    _, f0 = sim.linescan()
+    start = [sim.get_state(r) for r in range(len(SEEDS))]
+    loss, grad, gs = sim.adjoint(N_STEPS, TICK, f0, case["target"], checkpoint_every=K, grad_state=True)
+    _check_against_oracle(srs, oracle, dict(case, p=p, g=g, f0=f0, start=start), loss, grad, gs)
 
 
 def test_plain_engine_adjoint_agrees_with_resident(srs, case, plain_case):

@@ -8,14 +8,16 @@ from conftest import GOLDEN_MESH, LINESCAN_DESC, params_from_golden
 pytestmark = pytest.mark.gpu
 
 
-def test_autograd_gradient_matches_finite_differences(srs):
+@pytest.mark.parametrize("engine", ["RESIDENT", "PLAIN"])
+def test_autograd_gradient_matches_finite_differences(srs, engine):
     torch = pytest.importorskip("torch")
     from srs_gb300.autograd import AdjointProblem, LinescanLoss
     p, _ = params_from_golden(srs, "spark")
     p.ints[srs.I["FLAG_NO_FLUX_BOUNDARY"]] = 1
     rng = np.random.default_rng(5)
     prob = AdjointProblem(GOLDEN_MESH, p, [21, 22], LINESCAN_DESC, 400, 100,
-                          target=rng.standard_normal((2, 4, 20)) * 0.01, checkpoint_every=128)
+                          target=rng.standard_normal((2, 4, 20)) * 0.01, checkpoint_every=128,
+                          engine=getattr(srs, "ENGINE_" + engine))
     theta = prob.theta0().requires_grad_()
     loss = LinescanLoss.apply(theta, prob)
     (g,) = torch.autograd.grad(loss, theta)
