@@ -237,12 +237,10 @@ def reference_available():
     return os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libsrsref.so"))
 
 
-def cpu_sample(base, params, seconds, cores=None, prefer_reference=False):
+def cpu_sample(base, ints, reals, seconds, cores=None, prefer_reference=False):
     """Times RunSimulation on `cores` processes; returns (spark-ms/s, cores, kind, sample)."""
-    import numpy as np
     cores = cores or os.cpu_count() or 1
-    ints = list(params.ints)
-    reals = list(params.reals)
+    ints, reals = list(ints), list(reals)
     # calibrate: ~31M element-steps/s per core -> steps for the requested seconds
     kind = "reference" if (prefer_reference and reference_available()) else "port"
     worker = _ref_worker if kind == "reference" else _cpu_worker
@@ -262,22 +260,42 @@ def cpu_sample(base, params, seconds, cores=None, prefer_reference=False):
     return value, cores, kind, sample
 
 
+def write_config_mesh_host(directory):
+    """Writes the config-1 box dyad with the host-only mesh writer
+    (srs_gb300/bin/srs_meshgen, built from meshgen.cpp alone; compiled here
+    with g++ when absent), so that the CPU legs load no CUDA library."""
+    exe = os.path.join(ROOT, "srs_gb300", "bin", "srs_meshgen")
+    if not os.path.exists(exe):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location(
+            "_srs_build", os.path.join(ROOT, "srs_gb300", "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        exe = mod.build_meshgen(os.path.join(directory, "srs_meshgen"))
+    base = os.path.join(directory, "dyad12")
+    subprocess.run([exe, "-out", base], check=True, stdout=subprocess.DEVNULL)
+    return base
+
+
 # ---------------------------------------------------------------------------
 def run_reference(args):
+    """The reference arm: the reference's RunSimulation (oracle/_ref, built
+    from the reference sources where they are present, else the oracle's C
+    restatement of it, bit-exact with the reference) on the host cores.  It
+    loads only the oracle libraries: parameters from oracle/params.py, the
+    mesh from the host-only mesh writer."""
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    import __graft_entry__ as g
-    g.build()
-    import srs_gb300 as srs
-    from srs_gb300 import workloads as wl
+    subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    from oracle import params as op
     tmp = tempfile.mkdtemp(prefix="srs_bench_")
-    base, rep = wl.config_mesh(tmp)
-    p = wl.default_spark_params()
+    base = write_config_mesh_host(tmp)
+    ints, reals = op.default_spark()
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
     vals = []
     for i in range(args.warmup + args.steps):
-        v, cores, kind, sample = cpu_sample(base, p, per_step, prefer_reference=True)
+        v, cores, kind, sample = cpu_sample(base, ints, reals, per_step, prefer_reference=True)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
@@ -727,7 +745,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        v, cores, kind, sample = cpu_sample(base, p, args.cpu_seconds)
+        v, cores, kind, sample = cpu_sample(base, list(p.ints), list(p.reals), args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
     if rank == 0:
         line = {

@@ -350,6 +350,11 @@ int srs_adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, int* segment_steps, 
 /* WriteToGridFiles (cpu/OutputFuncs.cpp:42-220): legacy ASCII VTK of the
  * current state of realization r at time t. */
 int srs_write_grid_vtk(srs_sim* s, int r, const char* path, int run, int rank, int n, double t);
+/* The same file from host arrays (no device needed): states[6N] species-major
+ * in the grid's numbering (C_CA and C_DYE are written) and ryr_states[NR]
+ * (B_RYR marks open RyRs with 2); WriteToGridFiles (cpu/OutputFuncs.cpp:42-220). */
+int srs_grid_write_vtk(const srs_grid* g, const double* states, const int* ryr_states,
+                       const char* path, int run, int rank, int n, double t);
 
 /* ---- synthetic meshes (no reference counterpart beyond the file format of
  * mesh/main.cpp:1305-1364): box dyad, see the generator for the geometry. */
@@ -404,9 +409,10 @@ int srs_multisite_mesh_write(const srs_multisite_spec* spec, const char* base, i
 
 /* ---- allocation-free step ---------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory — a framework that owns every allocation through its own pool, code
- * running while a stream is captured into a CUDA graph, a real-time loop that
- * must not touch the allocator — srs_explicit_step_fp64_noalloc performs one
+ * memory — a host application that owns every device allocation through its
+ * own pool or budget, or a real-time loop in which cudaMalloc/cudaFree (which
+ * may synchronise the device) must not run — srs_explicit_step_fp64_noalloc
+ * performs one
  * ExplicitStep (cpu/RunSimulation.cpp:591-654, FP64, reference operation
  * order, followed by gating unless `nogating`) for up to
  * SRS_NOALLOC_MAX_REALIZATIONS realizations, reading states_in and writing
@@ -415,9 +421,10 @@ int srs_multisite_mesh_write(const srs_multisite_spec* spec, const char* base, i
  * compiled into the library (per GPU, held until the process exits, about
  * 22 KB), shared by all calls and reused without reallocation: each call
  * clears it first, and calls whose work overlaps on the GPU race on it, so
- * serialise them.  The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Arrays use the reference numbering and the layouts returned by
+ * serialise them.  The first call on a device, with that device current,
+ * looks up that array's device address (cudaGetSymbolAddress) and caches it;
+ * make that first call before any stream capture.  The cache is not
+ * refreshed, so cudaDeviceReset between calls is not supported.  Arrays use the reference numbering and the layouts returned by
  * srs_grid_get_operator / srs_grid_get_elements / srs_grid_get_channels:
  *   aij[5N], nij[4N]; br4[4N] = boundary rates of Ca, ATP, CMDN, dye;
  *   bhi[N] = TTArea*B_TOT_SL_HI/(V0*1e-15), blo[N] the same with B_TOT_SL_LO;

@@ -1,2 +1,3 @@
 """CPU oracle of the spark timestep (test infrastructure; see oracle.py)."""
-from .oracle import Oracle, Mesh, Reference, RNG_REFERENCE, RNG_PHILOX, build  # noqa: F401
+from .oracle import (Oracle, Mesh, Reference, RefIO, RefGrid, RNG_REFERENCE, RNG_PHILOX,  # noqa: F401
+                     build)

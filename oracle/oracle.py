@@ -213,6 +213,8 @@ class Reference:
         self.lib.ref_run_simulation.argtypes = [C.c_int] * 3 + [vp] * 14 + [C.c_int, C.c_int, vp,
                                                                              C.c_int64, C.c_int, vp]
         self.lib.ref_run_simulation.restype = C.c_int64
+        self.lib.ref_set_linescan.argtypes = [C.c_int] + [vp] * 5 + [C.c_int64]
+        self.lib.ref_linescan_rows.restype = C.c_int64
 
     @staticmethod
     def _mesh_args(m):
@@ -243,3 +245,126 @@ class Reference:
         if n < 0:
             raise ValueError("reference harness needs an explicit initial channel")
         return rows[:n].copy(), S
+
+    def run_simulation_linescan(self, m, ints, W, pad, rank=0, index=0, row_capacity=None, row_w=7,
+                                ls_capacity=None):
+        """run_simulation with the line scan F = pad + W @ [CaDye] (W dense,
+        [n_samples][N] in the mesh's numbering) taken at every grid-file call
+        of RunSimulation (t = 0, each grid-file step when OUTPUT_GRID_FLAG is
+        set, the end).  Returns (rows, final states, line-scan rows
+        [n_calls][1 + n_samples] = t, F_0 .. F_{n-1})."""
+        from oracle.linescan import to_csr
+        R = m.reals
+        if ls_capacity is None:
+            ls_capacity = int(R[0] / R[3]) + 8 if R[3] > 0 else 8
+        ptr, col, w = to_csr(np.asarray(W, np.float64))
+        pad = _f64(pad)
+        out = np.zeros((ls_capacity, len(pad) + 1))
+        self.lib.ref_set_linescan(len(pad), _p(ptr), _p(col), _p(w), _p(pad), _p(out), ls_capacity)
+        try:
+            rows, S = self.run_simulation(m, ints, rank, index, row_capacity, row_w)
+            n = int(self.lib.ref_linescan_rows())
+        finally:
+            self.lib.ref_set_linescan(0, None, None, None, None, None, 0)
+        return rows, S, out[:n].copy()
+
+
+REF_IO_SO = os.path.join(HERE, "_ref", "libsrsref_io.so")
+REF_LINESCAN = os.path.join(HERE, "_ref", "linescan")
+
+
+class RefIO:
+    """The reference's own cpu/InitFuncs.cpp and cpu/OutputFuncs.cpp
+    (oracle/_ref/libsrsref_io.so, driven by oracle/ref_io_harness.cpp)."""
+
+    def __init__(self):
+        if not os.path.exists(REF_IO_SO):
+            raise FileNotFoundError("reference sources unavailable: %s not built" % REF_IO_SO)
+        L = self.lib = C.CDLL(REF_IO_SO)
+        vp = C.c_void_p
+        L.refio_read_parameters.argtypes = [C.c_char_p, vp, vp, vp]
+        L.refio_load.argtypes = [C.c_char_p, vp, vp]
+        L.refio_load.restype = vp
+        for name in ("refio_counts", "refio_get_states", "refio_set_states", "refio_reset_states"):
+            getattr(L, name).argtypes = [vp, vp]
+        L.refio_operator.argtypes = [vp] * 4
+        L.refio_elements.argtypes = [vp] * 5
+        L.refio_channels.argtypes = [vp] * 5
+        L.refio_open_random_ryr.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.refio_open_random_ryr.restype = C.c_int
+        L.refio_write_grid.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.refio_free.argtypes = [vp]
+        L.refio_set_ryr.argtypes = [vp, vp]
+
+    def read_parameters(self, path):
+        """ReadParameters: (ints[19], reals[56], chars[4] as bytes)."""
+        ints = np.zeros(19, np.int32)
+        reals = np.zeros(56)
+        chars = C.create_string_buffer(4 * 255)
+        self.lib.refio_read_parameters(str(path).encode(), _p(ints), _p(reals), chars)
+        return ints, reals, [chars.raw[i * 255:(i + 1) * 255].split(b"\0")[0] for i in range(4)]
+
+    def load(self, base, ints, reals):
+        return RefGrid(self, base, ints, reals)
+
+
+class RefGrid:
+    """ReadGrid + InitializeDefaultGrid + InitializeDomainStruct of the
+    reference (cpu/main.cpp:170-189) for one mesh and parameter set."""
+
+    def __init__(self, io, base, ints, reals):
+        self.io, self.lib = io, io.lib
+        self.ints, self.reals = _i32(ints), _f64(reals)
+        self.h = self.lib.refio_load(str(base).encode(), _p(self.ints), _p(self.reals))
+        c = np.zeros(5, np.int32)
+        self.lib.refio_counts(self.h, _p(c))
+        self.N, self.NF, self.NN, self.NR, self.NL = (int(x) for x in c)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.refio_free(self.h)
+            self.h = None
+
+    def operator(self):
+        aij, nij, br = np.zeros(5 * self.N), np.zeros(4 * self.N, np.int32), np.zeros(6 * self.N)
+        self.lib.refio_operator(self.h, _p(aij), _p(nij), _p(br))
+        return aij, nij, br
+
+    def elements(self):
+        v0, tt = np.zeros(self.N), np.zeros(self.N)
+        dom, trop = np.zeros(self.N, np.int32), np.zeros(self.N, np.int32)
+        self.lib.refio_elements(self.h, _p(v0), _p(tt), _p(dom), _p(trop))
+        return dict(V0=v0, TT=tt, domain=dom, tropc=trop)
+
+    def channels(self):
+        a, b = np.zeros(self.NR, np.int32), np.zeros(self.NR, np.int32)
+        c, d = np.zeros(4 * self.NR, np.int32), np.zeros(self.NL, np.int32)
+        self.lib.refio_channels(self.h, _p(a), _p(b), _p(c), _p(d))
+        return dict(ryr_ele=a, ryr_jsr=b, ryr_nb=c, lcc_ele=d)
+
+    def states(self):
+        S = np.zeros(6 * self.N)
+        self.lib.refio_get_states(self.h, _p(S))
+        return S
+
+    def set_states(self, S):
+        self.lib.refio_set_states(self.h, _p(_f64(S)))
+
+    def reset_states(self):
+        S = np.zeros(6 * self.N)
+        self.lib.refio_reset_states(self.h, _p(S))
+        return S
+
+    def open_random_ryr(self, rank, index, ryr=None):
+        """OpenRandomRyR for (rank, ensemble index); returns (index opened, states)."""
+        r = _i32(ryr if ryr is not None else np.zeros(self.NR)).copy()
+        k = self.lib.refio_open_random_ryr(self.h, int(rank), int(index), _p(r))
+        return k, r
+
+    def write_grid(self, directory, ryr=None, rank=0, run=0, n=0, t=0.0):
+        """WriteToGridFiles of the current states (and the RyR states given);
+        returns the path <directory>/grid_<rank>_<run>_<n>.vtk."""
+        if ryr is not None:
+            self.lib.refio_set_ryr(self.h, _p(_i32(ryr)))
+        self.lib.refio_write_grid(self.h, str(directory).encode(), int(rank), int(run), int(n), float(t))
+        return os.path.join(str(directory), "grid_%d_%d_%d.vtk" % (rank, run, n))

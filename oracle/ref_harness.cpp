@@ -23,10 +23,36 @@ namespace {
 float* g_rows = nullptr;
 int64_t g_row_cap = 0, g_nrows = 0;
 int g_row_w = 0;
+
+// line scan of the bound dye taken at every grid-file call: F_i = pad_i +
+// sum_q w_q [CaDye]_{col_q} over row i of a CSR weight matrix (the PSF sum
+// of linescan/main.cpp:197-225 with the cell volumes folded into w)
+int g_ls_n = 0;
+const int* g_ls_ptr = nullptr;
+const int* g_ls_col = nullptr;
+const double* g_ls_w = nullptr;
+const double* g_ls_pad = nullptr;
+double* g_ls_out = nullptr;
+int64_t g_ls_cap = 0, g_ls_rows = 0;
 }  // namespace
 
 void CreateOutputFiles(int, int, ParamStruct*) {}
-void WriteToGridFiles(int, double, GridStruct*, SimData*, ParamStruct*) {}
+
+// Called by RunSimulation at t = 0, at every grid-file step when
+// OUTPUT_GRID_FLAG is set, and at the end (cpu/RunSimulation.cpp:421-586).
+// Writes one line-scan row [t, F_0 .. F_{n-1}] when a capture is set.
+void WriteToGridFiles(int, double t, GridStruct* g, SimData*, ParamStruct*) {
+  if (!g_ls_out || g_ls_rows >= g_ls_cap) return;
+  double* o = g_ls_out + g_ls_rows * (int64_t)(g_ls_n + 1);
+  o[0] = t;
+  const double* dye = g->States[INDEX_DYE];
+  for (int i = 0; i < g_ls_n; ++i) {
+    double acc = 0.0;
+    for (int q = g_ls_ptr[i]; q < g_ls_ptr[i + 1]; ++q) acc += g_ls_w[q] * dye[g_ls_col[q]];
+    o[1 + i] = g_ls_pad[i] + acc;
+  }
+  ++g_ls_rows;
+}
 void WriteToStateFiles(double t, SimData* sd, ParamStruct* ps) {
   if (g_nrows >= g_row_cap) return;
   float* row = g_rows + g_nrows * g_row_w;
@@ -223,9 +249,28 @@ int64_t ref_run_simulation(int N, int NR, int NL, const double* aij, const int* 
   g_row_cap = row_cap;
   g_row_w = row_w;
   g_nrows = 0;
+  g_ls_rows = 0;
   RunSimulation(&h.sd, &h.ps);
+  fflush(stdout);  // the reference's progress output, while the caller still captures it
   if (states_out) unload(&h, N, states_out);
   return g_nrows;
 }
+
+// Line-scan capture for the next ref_run_simulation calls (n_samples rows
+// of CSR weights in the reference's element numbering; out holds cap rows
+// of n_samples + 1 doubles).  n_samples = 0 switches it off.
+void ref_set_linescan(int n_samples, const int* ptr, const int* col, const double* w, const double* pad,
+                      double* out, int64_t cap) {
+  g_ls_n = n_samples;
+  g_ls_ptr = ptr;
+  g_ls_col = col;
+  g_ls_w = w;
+  g_ls_pad = pad;
+  g_ls_out = n_samples > 0 ? out : nullptr;
+  g_ls_cap = cap;
+  g_ls_rows = 0;
+}
+
+int64_t ref_linescan_rows() { return g_ls_rows; }
 
 }  // extern "C"

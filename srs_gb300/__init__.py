@@ -210,6 +210,7 @@ _SIGS = {
     "srs_sim_status": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "srs_sim_get_config": (C.c_int, [_P, C.POINTER(_SimConfig)]),
     "srs_write_grid_vtk": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "srs_grid_write_vtk": (C.c_int, [_P, _P, _P, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
     "srs_box_mesh_default": (None, [C.POINTER(BoxMeshSpec)]),
     "srs_box_mesh_write": (C.c_int, [C.POINTER(BoxMeshSpec), C.c_char_p, _P, _P]),
     "srs_multisite_mesh_write": (C.c_int, [C.POINTER(MultiSiteSpec), C.c_char_p, _P, _P]),
@@ -356,6 +357,14 @@ class Grid:
         d = np.zeros(self.n_lcc, np.int32)
         _check(_lib.srs_grid_get_channels(self._h, _ptr(a), _ptr(b), _ptr(c), _ptr(d)))
         return dict(ryr_ele=a, ryr_jsr=b, ryr_nb=c, lcc_ele=d)
+
+    def write_vtk(self, path, states, ryr_states=None, run=0, rank=0, n=0, t=0.0):
+        """WriteToGridFiles' VTK file from host arrays (states[6N], ryr_states[NR])."""
+        S = np.ascontiguousarray(states, dtype=np.float64)
+        ryr = np.ascontiguousarray(ryr_states if ryr_states is not None else np.zeros(self.n_ryr),
+                                   dtype=np.int32)
+        _check(_lib.srs_grid_write_vtk(self._h, _ptr(S), _ptr(ryr), str(path).encode(), run, rank, n,
+                                       float(t)))
 
     def initial_states(self, params):
         S = np.zeros(6 * self.n_ele, np.float64)

@@ -3,7 +3,7 @@
 Outputs (git-ignored, rebuilt on every box):
   srs_gb300/libsrs_gb300.so   C ABI of include/srs_gb300.h
   srs_gb300/bin/cru3d         drop-in replacement of the reference CLI
-  srs_gb300/bin/srs_meshgen   synthetic mesh writer
+  srs_gb300/bin/srs_meshgen   synthetic mesh writer (host code only)
 
 Translation units compile in parallel; the numerics files use -fmad=false so
 that every fused multiply-add is an explicit one (bit-reproducible results),
@@ -93,13 +93,24 @@ def build(verbose=False, force=False):
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-    for exe, src in (("cru3d", "cru3d_main.cpp"), ("srs_meshgen", "meshgen_main.cpp")):
-        cmd = ["g++", "-std=c++17", "-O2", "-I", CSRC, "-I", INC, os.path.join(CSRC, src), "-o",
-               os.path.join(BIN, exe), "-L", HERE, "-lsrs_gb300", "-Wl,-rpath,$ORIGIN/.."]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link of %s failed:\n%s\n%s" % (exe, r.stdout, r.stderr))
+    cmd = ["g++", "-std=c++17", "-O2", "-I", CSRC, "-I", INC, os.path.join(CSRC, "cru3d_main.cpp"),
+           "-o", os.path.join(BIN, "cru3d"), "-L", HERE, "-lsrs_gb300", "-Wl,-rpath,$ORIGIN/.."]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link of cru3d failed:\n%s\n%s" % (r.stdout, r.stderr))
+    build_meshgen(os.path.join(BIN, "srs_meshgen"))
     return LIB
+
+
+def build_meshgen(dest):
+    """The mesh writer as a host-only executable (meshgen.cpp alone, no CUDA
+    library), so that CPU-only runs can write their input files."""
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", CSRC, "-I", INC,
+           os.path.join(CSRC, "meshgen.cpp"), os.path.join(CSRC, "meshgen_main.cpp"), "-o", dest]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build of %s failed:\n%s\n%s" % (dest, r.stdout, r.stderr))
+    return dest
 
 
 if __name__ == "__main__":

@@ -1,11 +1,11 @@
 // k_noalloc.cu — an explicit step that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: a host framework that owns every
-// device allocation through its own pool, code that runs while a stream is
-// being captured into a CUDA graph, or a real-time loop that must not touch
-// the allocator.  srs_explicit_step_fp64_noalloc serves them.  The caller
-// passes every input and output as its own device buffer; the only memory
-// the step needs beyond those — the per-realization "blocks finished"
+// Some callers cannot call cudaMalloc: a host application that owns every
+// device allocation through its own pool or budget, or a real-time loop in
+// which cudaMalloc/cudaFree (which may synchronise the device and take an
+// unbounded time) must not run.  srs_explicit_step_fp64_noalloc serves them.
+// The caller passes every input and output as its own device buffer; the only
+// memory the step needs beyond those — the per-realization "blocks finished"
 // counters and control blocks of the FP64 step kernel — lives in the
 // fixed-size array below instead of in cudaMalloc'ed memory.
 //
@@ -14,6 +14,11 @@
 // of the last call, so each call clears what must start at zero before its
 // step.  Calls whose work overlaps on the GPU (different streams, or several
 // host threads) race on the array: serialise them.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address (cudaGetSymbolAddress) and caches it per device.
+// That cache is not refreshed: cudaDeviceReset between calls is not
+// supported (the cached address would belong to the destroyed context).
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -68,9 +73,14 @@ void* g_addr[128] = {};  // symbol address of the array, per device
 int scratch_address(void** out, std::string* err) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 128) {
+  if (e != cudaSuccess) {
     *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
     return SRS_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= 128) {
+    *err = "srs_explicit_step_fp64_noalloc supports devices 0..127, current device is " +
+           std::to_string(dev);
+    return SRS_ERR_UNSUPPORTED;
   }
   std::lock_guard<std::mutex> lock(g_mtx);
   if (!g_addr[dev]) {
@@ -106,6 +116,8 @@ extern "C" int srs_explicit_step_fp64_noalloc(const srs_noalloc_step* d) {
   if (d->n_ele <= 0 || d->n_ryr < 0 || d->n_lcc < 0 || !d->reals || !d->seeds || !d->aij ||
       !d->nij || !d->br4 || !d->v0 || !d->bhi || !d->blo || !d->flags || !d->chan_ptr ||
       !d->states_in || !d->states_out || !d->ryr_states || !d->residuals ||
+      !d->chan_list || (d->n_ryr > 0 && (!d->ryr_ele || !d->ryr_jsr)) ||
+      (d->n_ryr > 0 && d->reals[R_RYR_A_STAR] != 0 && !d->ryr_nb) ||
       (d->n_lcc > 0 && (!d->lcc_states || !d->lccv_states || !d->lcc_ele)))
     return set_last_error(SRS_ERR_INPUT, "missing input or output pointer");
   if (d->n_ryr > 1024 && d->reals[R_RYR_A_STAR] != 0)

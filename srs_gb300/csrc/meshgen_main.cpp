@@ -1,5 +1,7 @@
 // meshgen_main.cpp — writes a synthetic box-dyad mesh in the reference's
-// mesh file set (see meshgen.cpp for the geometry).
+// mesh file set (see meshgen.cpp for the geometry).  Host code only: it is
+// built from meshgen.cpp alone and loads no CUDA library, so CPU-only
+// callers (the CPU reference timings) can write their inputs with it.
 //
 //   srs_meshgen -out base [key value ...]
 // keys: box_x box_y box_z foot_half_x foot_half_y n_foot_x n_foot_y n_out_x
@@ -9,11 +11,11 @@
 #include <cstdlib>
 #include <cstring>
 
-#include "srs_gb300.h"
+#include "srs_host.h"
 
 int main(int argc, char** argv) {
-  srs_box_mesh_spec s;
-  srs_box_mesh_default(&s);
+  srs::MeshGenSpec s;
+  srs::meshgen_default_spec(&s);
   const char* out = nullptr;
   for (int i = 1; i + 1 < argc; i += 2) {
     const char* k = argv[i];
@@ -55,14 +57,13 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "usage: srs_meshgen -out base [key value ...]\n");
     return 1;
   }
-  int rep[6];
-  double a0;
-  int rc = srs_box_mesh_write(&s, out, rep, &a0);
+  srs::MeshGenReport rep;
+  int rc = srs::meshgen_box(s, out, &rep);
   if (rc) {
-    std::fprintf(stderr, "Error: %s (%s)\n", srs_status_string(rc), srs_last_error());
+    std::fprintf(stderr, "Error: mesh generation failed (status %d) for %s\n", rc, out);
     return 1;
   }
-  std::printf("tets %d faces %d nodes %d ryr %d lcc %d jsr_tets %d max_a0 %.6g\n", rep[0], rep[1],
-              rep[2], rep[3], rep[4], rep[5], a0);
+  std::printf("tets %d faces %d nodes %d ryr %d lcc %d jsr_tets %d max_a0 %.6g\n", rep.n_tets,
+              rep.n_faces, rep.n_nodes, rep.n_ryr, rep.n_lcc, rep.n_jsr_tets, rep.max_a0);
   return 0;
 }

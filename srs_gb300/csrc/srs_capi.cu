@@ -1817,7 +1817,8 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
   }
   const int ns = (int)((d->x_max - d->x_min) / d->res);
   if (ns <= 0) return fail(SRS_ERR_INPUT, "no line-scan samples");
-  const double alpha = 1.0 / std::pow(2 * 3.14159265358979323846, 1.5);
+  // normpdf3d with the tool's own constant (linescan/parameters.h: PI = 3.14159)
+  const double alpha = 1.0 / std::pow(2 * 3.14159, 1.5);
   auto pdf = [&](double rx, double ry, double rz) {
     return alpha * std::exp(-0.5 * ((rx * rx / (sx * sx)) + (ry * ry / (sy * sy)) + (rz * rz / (sz * sz)))) /
            (sx * sy * sz);
@@ -1828,20 +1829,26 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
     else if (d->axis == 1) { c[0] = d->offset1; c[1] = xi; c[2] = d->offset2; }
     else { c[0] = d->offset1; c[1] = d->offset2; c[2] = xi; }
   };
-  // element centroids from the node file (linescan/main.cpp:95-110)
+  // element centroids and volumes from the nodes (linescan/main.cpp:95-109:
+  // the mean of the four nodes, |(c1-c4) . ((c2-c4) x (c3-c4))| / 6)
   const Mesh& m = s->m;
-  std::vector<double> cx(m.N), cy(m.N), cz(m.N);
+  std::vector<double> cx(m.N), cy(m.N), cz(m.N), vol(m.N);
   for (int j = 0; j < m.N; ++j) {
-    double x = 0, y = 0, z = 0;
+    double px[4], py[4], pz[4];
     for (int k = 0; k < 4; ++k) {
       int v = m.ele_nodes[4 * (size_t)j + k];
-      x += m.node_x[v];
-      y += m.node_y[v];
-      z += m.node_z[v];
+      px[k] = m.node_x[v];
+      py[k] = m.node_y[v];
+      pz[k] = m.node_z[v];
     }
-    cx[j] = x / 4.0;
-    cy[j] = y / 4.0;
-    cz[j] = z / 4.0;
+    cx[j] = (px[0] + px[1] + px[2] + px[3]) / 4.0;
+    cy[j] = (py[0] + py[1] + py[2] + py[3]) / 4.0;
+    cz[j] = (pz[0] + pz[1] + pz[2] + pz[3]) / 4.0;
+    double ax = px[0] - px[3], ay = py[0] - py[3], az = pz[0] - pz[3];
+    double bx = px[1] - px[3], by = py[1] - py[3], bz = pz[1] - pz[3];
+    double qx = px[2] - px[3], qy = py[2] - py[3], qz = pz[2] - pz[3];
+    double nx = by * qz - bz * qy, ny = bz * qx - bx * qz, nz = bx * qy - by * qx;
+    vol[j] = std::fabs((ax * nx + ay * ny + az * nz) / 6.0);
   }
   // padding voxels at the resting fluorescence (AddPointGrid, :275-313)
   std::vector<double> px, py, pz, pv;
@@ -1883,7 +1890,7 @@ int srs_linescan_setup(srs_sim* s, const srs_linescan_desc* d, int* n_samples) {
     for (int j = 0; j < m.N; ++j) {
       double rx = cx[j] - c[0], ry = cy[j] - c[1], rz = cz[j] - c[2];
       if (rx * rx + ry * ry + rz * rz < d->r_thresh) {
-        double wj = m.V0[j] * pdf(rx, ry, rz);
+        double wj = vol[j] * pdf(rx, ry, rz);
         col.push_back(s->eng_of_ref[j]);
         w.push_back(wj);
         rest += wj * S6[SP_DYE * (size_t)m.N + j];
@@ -2795,6 +2802,13 @@ int srs_write_grid_vtk(srs_sim* s, int r, const char* path, int run, int rank, i
   std::vector<int32_t> ryr(s->NR);
   SRS_CUDA(cudaMemcpy(ryr.data(), s->d_ryr + (size_t)r * s->NR, s->NR * 4, cudaMemcpyDeviceToHost));
   return write_grid_vtk(path, s->m, run, rank, n, t, &S6[0], &S6[(size_t)SP_DYE * s->N], ryr.data());
+}
+
+int srs_grid_write_vtk(const srs_grid* g, const double* states, const int* ryr_states,
+                       const char* path, int run, int rank, int n, double t) {
+  if (!g || !states || !path || (g->m.NR > 0 && !ryr_states)) return fail(SRS_ERR_INPUT, "null argument");
+  int rc = write_grid_vtk(path, g->m, run, rank, n, t, states, states + (size_t)SP_DYE * g->m.N, ryr_states);
+  return rc ? fail(rc, std::string("cannot write ") + path) : SRS_OK;
 }
 
 void srs_box_mesh_default(srs_box_mesh_spec* spec) {

@@ -1,9 +1,10 @@
 """Autotuner of the resident engine.
 
-Chooses the cluster size (CTAs sharing one realization), the threads per CTA
-and the time steps per persistent launch for a given grid and batch by timing
-short trial launches of each candidate on the device (CUDA events on the
-engine's stream).  Results are cached per (element count, channel count,
+Chooses the cluster size (CTAs sharing one realization) and the threads per
+CTA for a given grid and batch by timing short trial launches of each
+candidate on the device (CUDA events on the engine's stream).  The time steps
+per persistent launch are not searched: they are the caller's output cadence
+(the launch ends at every states-row or grid-file tick).  Results are cached per (element count, channel count,
 realizations, device) in a JSON file next to the package, so later runs start
 with the tuned configuration.
 """

@@ -138,3 +138,36 @@ def test_ryr_with_swapped_domains_is_rejected_by_fp32_engines(srs, mesh_copy):
         with pytest.raises(srs.SrsError) as e:
             srs.Simulation(g, p, 1, srs.FP32, eng)
         assert e.value.status == -3
+
+
+NOALLOC_POINTERS = ("aij", "nij", "br4", "v0", "bhi", "blo", "flags", "chan_ptr", "chan_list",
+                    "ryr_ele", "ryr_jsr", "ryr_nb", "lcc_ele", "states_in", "states_out",
+                    "ryr_states", "lcc_states", "lccv_states", "residuals")
+
+
+@pytest.mark.parametrize("missing", NOALLOC_POINTERS + ("reals", "seeds"))
+def test_noalloc_step_rejects_null_pointers(srs, missing):
+    """Host-side validation of srs_explicit_step_fp64_noalloc: every array the
+    FP64 step reads for the given counts must be non-null (ryr_nb only with
+    coupled gating), and the call returns SRS_ERR_INPUT before any CUDA call.
+    The other pointers are placeholders that must never be dereferenced, so
+    the test runs only where no GPU is visible."""
+    import ctypes as C
+
+    import numpy as np
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("host-only validation test")
+    d = srs.NoallocStep()
+    d.n_ele, d.n_realizations, d.n_ryr, d.n_lcc = 10, 2, 3, 1
+    for k, name in enumerate(NOALLOC_POINTERS):
+        setattr(d, name, 0x1000 + 0x100 * k)
+    reals = np.zeros(56)
+    reals[srs.R["RYR_A_STAR"]] = 1.0 if missing == "ryr_nb" else 0.0
+    seeds = np.zeros(2, np.uint64)
+    d.reals = reals.ctypes.data_as(C.c_void_p).value
+    d.seeds = seeds.ctypes.data_as(C.c_void_p).value
+    setattr(d, missing, None)
+    with pytest.raises(srs.SrsError) as e:
+        srs.explicit_step_fp64_noalloc(d)
+    assert e.value.status == -1 and "pointer" in str(e.value)

@@ -29,3 +29,27 @@ def test_linescan_matches_restatement(srs, prec, eng):
     assert F.shape == (3, ns)
     assert np.allclose(F, want, rtol=1e-12, atol=0)
     assert (F > F0).any()  # the open RyR raised the bound dye somewhere on the line
+
+
+def test_linescan_matches_reference_tool_output(srs):
+    """The device line scan against the reference's own line-scan tool
+    (linescan/main.cpp) on three states of the golden mesh whose grid files
+    the reference wrote (tests/golden/linescan_tool.npz, from
+    tests/golden/gen_linescan_tool.py).  The tool prints %g (six significant
+    digits), so the bar is 5e-6 relative."""
+    import json
+    import os
+
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "linescan_tool.npz"))
+    desc = json.loads(str(d["desc"]))
+    states = d["states"]
+    p, _ = params_from_golden(srs, "spark")
+    g = srs.Grid(p, GOLDEN_MESH)
+    sim = srs.Simulation(g, p, len(states), srs.FP64, srs.ENGINE_PLAIN, seeds=[1, 2, 3])
+    for r, S in enumerate(states):
+        sim.set_state(r, states=S)
+    sim.linescan_setup(**desc)
+    F, _ = sim.linescan()
+    assert F.shape == d["tool_output"].shape
+    assert np.allclose(F, d["tool_output"], rtol=5e-6, atol=0), np.abs(F / d["tool_output"] - 1).max()

@@ -303,6 +303,29 @@ def test_fp32_resident_error_vs_fp64_on_config_mesh(srs, box_mesh):
     assert e <= TOL32, e
 
 
+def test_fp32_error_vs_fp64_over_2ms_on_config_mesh(srs, box_mesh):
+    """The deterministic part over a real horizon: 2 ms (222,224 steps at
+    dt = 9 ns) of the DefaultSpark source (RyR 24 held open, gating off) on
+    the config mesh.  Both FP32 engines stay within 1e-5 relative of the FP64
+    engine at every 0.5 ms checkpoint."""
+    base, _ = box_mesh
+    p = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24,
+                                     FLAG_NO_GATING=1)
+    g = srs.Grid(p, base)
+    s64 = srs.Simulation(g, p, 1, srs.FP64, srs.ENGINE_PLAIN)
+    s32 = srs.Simulation(g, p, 2, srs.FP32, srs.ENGINE_RESIDENT)
+    p32 = srs.Simulation(g, p, 1, srs.FP32, srs.ENGINE_PLAIN)
+    errs = []
+    for _ in range(4):
+        for s in (s64, s32, p32):
+            s.explicit_step(55556)
+        ref = s64.get_state(0)["states"]
+        errs.append((rel_err(s32.get_state(0)["states"], ref), rel_err(s32.get_state(1)["states"], ref),
+                     rel_err(p32.get_state(0)["states"], ref)))
+    assert max(max(e) for e in errs) <= TOL32, errs
+    assert not (s32.status() & 1) and not (p32.status() & 1)
+
+
 def test_nonfinite_state_is_reported(srs):
     p = golden_params(srs, "spark_nogating")
     g = srs.Grid(p, GOLDEN_MESH)

@@ -11,7 +11,9 @@ import pytest
 
 from conftest import GOLDEN_MESH, ROOT
 
-REF_PARAM_DIR = "/root/reference/param"
+# the reference's parameter files, where its source tree is present (the
+# same variable oracle/build_ref.sh reads)
+REF_PARAM_DIR = os.path.join(os.environ.get("SRS_REFERENCE_ROOT", "/root/reference"), "param")
 
 # XML symbol -> (kind, index, conversion) of cpu/InitFuncs.cpp:191-349
 FLAGS = {"flag_noflux": 9, "flag_nogating": 14, "flag_ffwd": 15, "flag_use_clock": 2,
@@ -262,3 +264,18 @@ def test_multisite_spec_errors(srs, tmp_path, field, value):
         srs.write_multisite_mesh(base, spec)
     assert e.value.status == -1
     assert not os.path.exists(base + ".ele")
+
+
+def test_oracle_parameter_vectors_match_product(srs):
+    """oracle/params.py (ReadParameters defaults and DefaultSpark, used by the
+    CPU-only reference leg of bench.py) equals the product's parameters."""
+    from oracle import params as op
+    from srs_gb300 import workloads as wl
+    p = srs.default_parameters()
+    assert list(p.ints) == list(op.DEFAULT_INTS)
+    assert list(p.reals) == [float(x) for x in op.DEFAULT_REALS]
+    assert op.INT_NAMES == tuple(sorted(srs.I, key=srs.I.get))
+    assert op.REAL_NAMES == tuple(sorted(srs.R, key=srs.R.get))
+    ints, reals = op.default_spark(T_FINAL=3.0)
+    q = wl.default_spark_params(T_FINAL=3.0)
+    assert list(q.ints) == ints and list(q.reals) == reals

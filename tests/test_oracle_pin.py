@@ -88,3 +88,19 @@ def test_own_log_exp_accuracy(oracle):
     us = np.random.default_rng(0).random(1000) + 1e-12
     got = np.array([L.or_log(float(u)) for u in us])
     assert np.max(np.abs(got - np.log(us)) / np.maximum(np.abs(np.log(us)), 1e-3)) < 1e-15
+
+
+def test_linescan_restatement_matches_tool_fixture():
+    """oracle/linescan.py against the reference line-scan tool's output
+    committed in tests/golden/linescan_tool.npz (%g: 5e-6 relative)."""
+    import json
+
+    from conftest import GOLDEN, GOLDEN_MESH
+    from oracle import Mesh, Oracle, linescan
+    d = np.load(os.path.join(GOLDEN, "linescan_tool.npz"))
+    desc = json.loads(str(d["desc"]))
+    N = d["states"].shape[1] // 6
+    m = Mesh(Oracle(), GOLDEN_MESH, 1, np.zeros(56))
+    W, pad = linescan.weights(GOLDEN_MESH, m.elements()["order"], desc)
+    got = np.array([pad + W @ S[5 * N:] for S in d["states"]])
+    assert np.allclose(got, d["tool_output"], rtol=5e-6, atol=0)

@@ -1,9 +1,10 @@
 """The allocation-free step, checked against the regular FP64 engine.
 
 srs_explicit_step_fp64_noalloc exists for callers that cannot allocate
-device memory themselves (a framework that owns every allocation, code
-running under stream capture, a real-time loop): they hand over their own
-device buffers and the library uses only a fixed array compiled into it.
+device memory themselves (a host application that owns every device
+allocation through its own pool, or a real-time loop in which cudaMalloc must
+not run): they hand over their own device buffers and the library uses only
+a fixed array compiled into it.
 This test builds those buffers with torch, runs two consecutive steps
 through the C ABI and requires bit-identical results to two steps of the
 regular FP64 engine (srs_explicit_step), whose arithmetic is the
@@ -96,6 +97,8 @@ def test_noalloc_step_matches_regular_engine(srs):
             assert np.array_equal(out[r], expect[k][r]["states"]), (k, r)
             assert np.array_equal(ryr.cpu().numpy().reshape(R, -1)[r], expect[k][r]["ryr"])
             assert np.array_equal(res.cpu().numpy().reshape(R, -1)[r], expect[k][r]["residuals"])
+            assert np.array_equal(lcc.cpu().numpy().reshape(R, -1)[r], expect[k][r]["lcc"])
+            assert np.array_equal(lccv.cpu().numpy().reshape(R, -1)[r], expect[k][r]["lccv"])
     assert int(status.item()) == 0
 
 
