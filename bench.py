@@ -75,7 +75,9 @@ def parse():
     ap.add_argument("--no-config2", action="store_true", help="skip the multi-mesh batch leg")
     ap.add_argument("--no-config4", action="store_true", help="skip the large-site leg")
     ap.add_argument("--no-config0", action="store_true", help="skip the single-spark leg")
-    ap.add_argument("--config0-ms", type=float, default=2.0)
+    ap.add_argument("--config0-ms", type=float, default=20.0)
+    ap.add_argument("--fp64-steps", type=int, default=22222,
+                    help="steps of the FP32-vs-FP64 error check of the config-1 engine")
     ap.add_argument("--config4-steps", type=int, default=4096)
     ap.add_argument("--config4-realizations", type=int, default=32,
                     help="realizations of the large-site leg (32: the workload; fewer for profiling)")
@@ -85,7 +87,10 @@ def parse():
                     help="run one secondary leg alone and print its JSON (profiling)")
     ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
-    ap.add_argument("--config2-steps", type=int, default=4000)
+    ap.add_argument("--config2-ms", type=float, default=2.0,
+                    help="simulated window of the multi-mesh batch leg (both protocols)")
+    ap.add_argument("--config2-launch-steps", type=int, default=0,
+                    help="steps per member launch in one graph replay (0: one states interval)")
     ap.add_argument("--adjoint-threads", type=int, default=0, help="reverse-sweep threads per CTA")
     ap.add_argument("--adjoint-flags", type=int, default=0, help="srs_adjoint_desc flags")
     ap.add_argument("--adjoint-partitions", type=int, default=0,
@@ -415,39 +420,122 @@ def plain_one_realization(srs, grid, p, n=4000):
 def config2_batch(srs, args):
     """Uneven multi-mesh batch: four box dyads (6k / 15k / 30k / 60k tets,
     Poisson-disk clusters of 10 / 25 / 60 / 100 RyRs, one LCC per 7 RyRs) x
-    two protocols (leak: clamped at rest, no trigger; LCC-triggered: clamped
-    at 0 mV) x 32 realizations = 256 realizations, each member at its tuned
-    resident configuration, advanced by one CUDA graph per 1000 steps.
-    Reported against the same members advanced one after another."""
+    two protocols (leak: clamped at rest, no trigger, 100 ms; LCC-triggered:
+    clamped at 0 mV, 30 ms, as param/Gain_0mV.xml) x 32 realizations = 256
+    realizations, each member at its tuned resident configuration, run by
+    srs_batch_run_simulation (the members' resident launches as branches of
+    one CUDA graph, the RunSimulation protocol on: LCC gating and clamp,
+    states rows on the device) over the first --config2-ms of both protocols
+    (a bounded sample of the 30 / 100 ms runs; the whole runs are projected
+    from it).  Reported against the same members run one after another
+    (srs_run_simulation each), with the roofline of the batch (algorithmic
+    48 + 44/R B per element-step of every member)."""
+    import numpy as np
     from srs_gb300 import tuner
     from srs_gb300 import workloads as wl
     tmp = tempfile.mkdtemp(prefix="srs_c2_")
-    sims, sim_ms = [], 0.0
-    seed0 = 1
+    W = args.config2_ms
+    members, seed0 = [], 1
     for base, rep_ in wl.config2_meshes(tmp):
-        for p in wl.config2_protocols(rep_["max_a0"]):
+        for k, p in enumerate(wl.config2_protocols(rep_["max_a0"])):
+            full = p.reals[srs.R["T_FINAL"]]
+            p.set(T_FINAL=W)
             g = srs.Grid(p, base)
             seeds = list(range(seed0, seed0 + 32))
             seed0 += 32
             t = tuner.tune_resident(g, p, 32, seeds=seeds)
-            sim = srs.Simulation(g, p, 32, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
-                                 cluster_size=t["cluster_size"], threads_per_cta=t["threads_per_cta"],
-                                 steps_per_launch=1000)
+            members.append(dict(grid=g, p=p, seeds=seeds, tune=t, n_tets=rep_["n_tets"],
+                                protocol=("leak", "lcc_trigger")[k], full_ms=full))
+
+    def make(S):
+        out = []
+        for m in members:
+            sim = srs.Simulation(m["grid"], m["p"], 32, srs.FP32, srs.ENGINE_RESIDENT, seeds=m["seeds"],
+                                 cluster_size=m["tune"]["cluster_size"],
+                                 threads_per_cta=m["tune"]["threads_per_cta"], steps_per_launch=S)
             sim.reset()
-            sims.append(sim)
-    n = args.config2_steps
-    spark_ms = sum(s.R * n * s.params.reals[srs.R["T_STEP"]] for s in sims)
-    for s in sims:  # members one after another
-        s.time_advance(1000)
-        sim_ms += s.time_advance(n)
-    b = srs.Batch(sims, steps_per_launch=1000)
-    b.time_advance(1000)
-    ms = b.time_advance(n)
+            out.append(sim)
+        return out
+
+    def launch_steps(m):
+        p = m["p"]
+        return int(round(p.reals[srs.R["OUTPUT_STATES_INTERVAL"]] / p.reals[srs.R["T_STEP"]]))
+
+    S = args.config2_launch_steps or max(launch_steps(m) for m in members)
+    # warm-up: one graph replay of every member
+    sims = make(S)
+    srs.Batch(sims, steps_per_launch=S).time_advance(S)
+    # members one after another
+    sims = make(S)
+    torch_sync()
+    one_rows, one_each = [], []
+    for sim in sims:
+        t0 = time.perf_counter()
+        one_rows.append(sim.run_simulation())
+        one_each.append(time.perf_counter() - t0)
+    one_s = sum(one_each)
+    # the batch
+    sims = make(S)
+    b = srs.Batch(sims, steps_per_launch=S)
+    torch_sync()
+    t0 = time.perf_counter()
+    outs = b.run_simulation()
+    batch_s = time.perf_counter() - t0
+    spark_ms, alg, per = 0.0, 0.0, []
+    for m, sim, (rows, t_end, n_steps), (rows1, _, n1), t1 in zip(members, sims, outs, one_rows, one_each):
+        dt = m["p"].reals[srs.R["T_STEP"]]
+        if not np.array_equal(n_steps, n1):
+            raise RuntimeError("batch and one-by-one runs differ in length")
+        spark_ms += float(n_steps.sum()) * dt
+        alg += float(n_steps.sum()) * m["n_tets"] * (48.0 + 44.0 / sim.R)
+        max_open = [float(r[:, 2].max()) for r in rows]
+        lcc_open = [float(r[:, 3].max()) for r in rows]
+        per.append({"tets": m["n_tets"], "protocol": m["protocol"],
+                    "cluster_size": sim.config()["cluster_size"], "steps": int(n_steps.max()),
+                    "alone_s": t1, "alone_ps_per_element_step":
+                        1e12 * t1 / (float(n_steps.sum()) * m["n_tets"]),
+                    "runs_with_lcc_opening": int(sum(x > 0 for x in lcc_open)),
+                    "runs_with_recruited_ryr": int(sum(x > 0 for x in max_open)),
+                    "mean_max_open_ryr": float(np.mean(max_open))})
+    peak, peak_kind = measured_peaks()
+    rate = spark_ms / batch_s
     return {"workload": "config2: 4 meshes (6000/15288/29478/60984 tets; 10/25/60/100 RyR) x "
-                        "2 protocols x 32 realizations, %d steps" % n,
-            "value": spark_ms / (ms / 1e3), "unit": UNIT, "batch_ms": ms,
-            "members_one_by_one_ms": sim_ms,
-            "cluster_sizes": [s.config()["cluster_size"] for s in sims]}
+                        "2 protocols x 32 realizations, RunSimulation protocol, first %.3g ms" % W,
+            "value": rate, "unit": UNIT, "batch_s": batch_s, "members_one_by_one_s": one_s,
+            "batch_over_one_by_one": one_s / batch_s, "steps_per_launch": S,
+            "roofline": {"bound": "hbm", "achieved": alg / batch_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / batch_s / 1e9 / peak,
+                         "note": "effective: algorithmic 48 + 44/R B per element-step of every "
+                                 "member, wall time of srs_batch_run_simulation; peak %s" % peak_kind},
+            # the whole runs (leak 100 ms, LCC-triggered 30 ms) at this window's rate
+            "projected_full_runs_s": sum(32 * m["full_ms"] for m in members) / rate,
+            "members": per}
+
+
+def torch_sync():
+    import torch
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def fp64_error(srs, grid, p, n, engine, **sim_kw):
+    """Error of an FP32 engine against the FP64 engine (the same per-element
+    arithmetic in FP64, bit-exact with the FP64 oracle) over the deterministic
+    part of the workload: n steps with gating off and the protocol's source
+    (RyR 24 held open) from rest, two FP32 realizations against one FP64 run.
+    Error: max over elements and species of |c32 - c64| / max(|c64|, 1e-3 uM)."""
+    import numpy as np
+    pd = p.copy().set(FLAG_NO_GATING=1)
+    s64 = srs.Simulation(grid, pd, 1, srs.FP64, srs.ENGINE_PLAIN, seeds=[1])
+    s32 = srs.Simulation(grid, pd, 2, srs.FP32, engine, seeds=[1, 2], **sim_kw)
+    s64.explicit_step(n)
+    s32.explicit_step(n)
+    ref = s64.get_state(0)["states"]
+    err = max(float(np.max(np.abs(s32.get_state(r)["states"] - ref) / np.maximum(np.abs(ref), 1e-3)))
+              for r in range(2))
+    return {"max_rel": err, "bar": 1e-5, "steps": n, "simulated_ms": n * DT_MS,
+            "engine": "resident" if engine == srs.ENGINE_RESIDENT else "plain",
+            "against": "FP64 plain engine, gating off"}
 
 
 def config0_spark(srs, args):
@@ -480,19 +568,17 @@ def config0_spark(srs, args):
             F.append(sim.linescan()[0][0] / f0)
 
     t0 = time.perf_counter()
-    _, _, n_steps, launch_ms = sim.run_simulation(timed=True, grid_callback=sample)
+    rows, _, n_steps, launch_ms = sim.run_simulation(timed=True, grid_callback=sample)
     wall = time.perf_counter() - t0
+    from srs_gb300.metrics import NAMES, spark_metrics
     F = np.array(F)
-    c = F[:, ns // 2] - 1.0
-    k = int(np.argmax(c))
-    half = c >= 0.5 * c[k]
-    fdhm = float(np.sum(half) * I)
+    K = min(len(F), len(rows[0]))
+    met = spark_metrics(F[:K, ns // 2], rows[0][:K, 2], I)
     return {"workload": "config0: config mesh, 1 realization, FP64 plain engine, DefaultSpark, "
                         "%.3g ms, line scan of %d samples every %.3g ms" % (T, ns, I),
             "steps": int(n_steps[0]), "device_s": float(launch_ms.sum()) / 1e3, "wall_s": wall,
             "value": T / wall, "unit": UNIT,
-            "spark": {"amplitude_dF_F0": float(c[k]), "time_to_peak_ms": float(ts[k]),
-                      "fdhm_ms": fdhm}}
+            "spark": dict(zip(NAMES, met)), "spark_metrics": "srs_gb300/metrics.py (centre sample)"}
 
 
 def config4_site(srs, args):
@@ -529,9 +615,10 @@ def config4_site(srs, args):
     n_el = rep_["n_tets"]
     alg = n_el * R * n * (48.0 + 44.0 / R)
     peak, peak_kind = measured_peaks()
+    del sim
+    err64 = fp64_error(srs, g, p, 2048, srs.ENGINE_PLAIN)
     adj = None
     if args.config4_adjoint_steps > 0:
-        del sim
         adj = config4_adjoint(srs, base, R, args.config4_adjoint_steps, ms / n)
     return {"adjoint": adj, "workload": "config4: multi-site release unit, %d tets (%d RyR in 5 clusters, %d LCC), "
                         "%d realizations, DefaultSpark protocol, FP32 plain engine, %d timed steps"
@@ -540,7 +627,7 @@ def config4_site(srs, args):
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
                          "note": "algorithmic 48 + 44/R B per element-step; peak %s" % peak_kind},
-            "mesh_generation_s": t_gen, "mesh_load_s": t_load,
+            "fp64_error": err64, "mesh_generation_s": t_gen, "mesh_load_s": t_load,
             "total_ca_start": np.asarray(tot0)[0].tolist(), "total_ca_end": np.asarray(tot1)[0].tolist()}
 
 
@@ -711,6 +798,14 @@ def run_ours(args):
                "reset_ms": reset_ms, "ms_per_step": 1e3 * e2e_s}
 
     # secondary legs: a failure is reported in the line, not fatal to it
+    err64 = None
+    if rank == 0 and args.fp64_steps > 0:
+        try:
+            err64 = fp64_error(srs, grid, p, args.fp64_steps, srs.ENGINE_RESIDENT,
+                               cluster_size=tuned["cluster_size"],
+                               threads_per_cta=tuned["threads_per_cta"])
+        except Exception as e:  # noqa: BLE001
+            err64 = {"error": "%s: %s" % (type(e).__name__, e)}
     adj = None
     if rank == 0 and not args.no_adjoint:
         try:
@@ -767,6 +862,7 @@ def run_ours(args):
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roof,
+            "fp64_error": err64,
             "cpu_baseline": cpu,
             "clocks": clk,
             "adjoint": adj,

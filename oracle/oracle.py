@@ -145,11 +145,14 @@ class Mesh:
                                     _p(st["CI"]), _p(S))
         return S
 
-    def steps_fp32(self, st, seed, step0, n, ryr, lcc, lccv, res, gating=True, globals_=None):
+    def steps_fp32(self, st, seed, step0, n, ryr, lcc, lccv, res, gating=True, globals_=None,
+                   compact=False):
+        """FP32 deviation-form steps; compact: the compensation terms are kept
+        in the 16-bit form of the large-mesh engine (srs_comp.h)."""
         g = _f64(globals_ if globals_ is not None else [self.reals[15], self.reals[16]])
         self.o.lib.or_steps_fp32(self.h, _p(self.reals), _p(g), _p(st["U"]), _p(st["Im"]), _p(st["CM"]),
                                  _p(st["CI"]), C.c_uint64(seed), step0, n, _p(ryr), _p(lcc), _p(lccv),
-                                 _p(res), int(gating))
+                                 _p(res), int(bool(gating)) | (2 if compact else 0))
 
     def adjoint(self, ints, S0, ch, seed, n_steps, tick_every, W, pad, f0, target, grad=True,
                 grad_state=False):

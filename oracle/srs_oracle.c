@@ -1214,9 +1214,25 @@ static void fp32_element(const or_k32* k, const float* o, float im, const float*
 }
 
 /* n FP32 steps (+ PHILOX gating on float Ca when `gating`), reference numbering. */
+/* Compact compensation (the large-mesh form of the plain FP32 engine,
+ * srs_gb300/csrc/srs_comp.h): after each update the compensation term c is
+ * kept as the IEEE half of c * 2^24 (clamped to +-65504, rounded to nearest
+ * even) and read back times 2^-24.  The conversion here is the compiler's
+ * _Float16 (IEEE binary16, round to nearest even), independent of the
+ * engine's. */
+static float comp_round_trip(float c) {
+  float v = c * 16777216.0f;
+  _Float16 h;
+  v = fminf(fmaxf(v, -65504.0f), 65504.0f);
+  h = (_Float16)v;
+  return (float)h * (1.0f / 16777216.0f);
+}
+
+/* flags: bit 0 gating, bit 1 compact compensation */
 void or_steps_fp32(const or_mesh* m, const double* R, const double* G, float* U, float* Im, float* CM,
                    float* CI, uint64_t seed, int64_t step0, int64_t n, int* ryr, int* lcc, int* lccv,
-                   double* res, int gating) {
+                   double* res, int flags) {
+  const int gating = flags & 1, compact = flags & 2;
   int N = m->N, j, q, i;
   or_k32 k;
   float* U2 = malloc(sizeof(float) * 4 * N);
@@ -1255,6 +1271,10 @@ void or_steps_fp32(const or_mesh* m, const double* R, const double* G, float* U,
       fp32_element(&k, &U[4 * j], Im[j], &U[4 * nb[0]], &U[4 * nb[1]], &U[4 * nb[2]], &U[4 * nb[3]],
                    &a[4 * j], m->domain[j] == 1, m->tropc[j], bsl[j], flux, &CM[4 * j], &CI[j],
                    &U2[4 * j], &I2[j]);
+      if (compact) {
+        for (q = 0; q < 4; ++q) CM[4 * j + q] = comp_round_trip(CM[4 * j + q]);
+        CI[j] = comp_round_trip(CI[j]);
+      }
     }
     memcpy(U, U2, sizeof(float) * 4 * N);
     memcpy(Im, I2, sizeof(float) * N);

@@ -74,10 +74,11 @@ int64_t or_run_simulation(const or_mesh* m, const int* ints, const double* reals
 void or_fp32_to_dev(const or_mesh* m, const double* reals, const double* states, float* U, float* Im);
 void or_fp32_from_dev(const or_mesh* m, const double* reals, const float* U, const float* Im,
                       const float* CM, const float* CI, double* states);
-/* CM (4N) and CI (N) hold the compensation terms of the Euler update. */
+/* CM (4N) and CI (N) hold the compensation terms of the Euler update.
+ * flags: bit 0 gating, bit 1 compact (16-bit) compensation terms. */
 void or_steps_fp32(const or_mesh* m, const double* reals, const double* globals, float* U, float* Im,
                    float* CM, float* CI, uint64_t seed, int64_t step0, int64_t n, int* ryr, int* lcc,
-                   int* lccv, double* res, int gating);
+                   int* lccv, double* res, int flags);
 
 /* Bit-reproducible arithmetic restated (for direct tests). */
 float or_logf(float x);

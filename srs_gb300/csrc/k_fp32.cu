@@ -70,27 +70,40 @@ __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int
       }
     }
     const int4 nb = a.nb[j];
-    float4 cm = a.CM[(size_t)r * N + j];
-    float ci = a.CI[(size_t)r * N + j];
+    const size_t o = (size_t)r * N + j;
+    const float4 x = M[j];
+    const float im = I[j];
+    float4 cm;
+    float ci;
+    if (a.CMq) {  // compact compensation (srs_comp.h)
+      cm = comp_load4(a.CMq[o]);
+      ci = comp_load1(a.CIq[o]);
+    } else {
+      cm = a.CM[o];
+      ci = a.CI[o];
+    }
     float4 out;
     float imo;
     if constexpr (TRAJ) {
       float g;
-      const float4 x = M[j];
-      const float im = I[j];
       tet_update(a.k, x, im, M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
                  a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo, &g);
-      a.traj_u[(size_t)r * N + j] = x;
-      a.traj_ig[(size_t)r * N + j] = make_float2(im, g);
-      a.traj_ib[(size_t)r * N + j] = sl_inv_factor(a.k, a.bsl[j], ((fl & 1u) ? a.k.c0j : a.k.c0) + x.x);
+      a.traj_u[o] = x;
+      a.traj_ig[o] = make_float2(im, g);
+      a.traj_ib[o] = sl_inv_factor(a.k, a.bsl[j], ((fl & 1u) ? a.k.c0j : a.k.c0) + x.x);
     } else {
-      tet_update(a.k, M[j], I[j], M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
+      tet_update(a.k, x, im, M[nb.x], M[nb.y], M[nb.z], M[nb.w], a.a[j], fl, a.bsl[j],
                  a.kb ? a.kb[j] : 0.0f, flux, cm, ci, &out, &imo);
     }
     Mo[j] = out;
     Io[j] = imo;
-    a.CM[(size_t)r * N + j] = cm;
-    a.CI[(size_t)r * N + j] = ci;
+    if (a.CMq) {
+      a.CMq[o] = comp_store4(cm);
+      a.CIq[o] = comp_store1(ci);
+    } else {
+      a.CM[o] = cm;
+      a.CI[o] = ci;
+    }
     if (!isfinite(out.x)) atomicOr(&ctlp->status, 1u);
   }
 }
@@ -179,9 +192,14 @@ __global__ void __launch_bounds__(256, 6) k_plain32_update(Plain32Args a) {
     const size_t n = min((size_t)blockDim.x, (size_t)a.N - e0);
     const size_t o = (size_t)r * a.N + e0;
     prefetch_span(a.M_in + o, n * sizeof(float4));
-    prefetch_span(a.CM + o, n * sizeof(float4));
     prefetch_span(a.I_in + o, n * sizeof(float));
-    prefetch_span(a.CI + o, n * sizeof(float));
+    if (a.CMq) {
+      prefetch_span(a.CMq + o, n * sizeof(ushort4));
+      prefetch_span(a.CIq + o, n * sizeof(uint16_t));
+    } else {
+      prefetch_span(a.CM + o, n * sizeof(float4));
+      prefetch_span(a.CI + o, n * sizeof(float));
+    }
   }
   const int j = blockIdx.y * blockDim.x + threadIdx.x;
   if (j < a.N) plain32_element<TRAJ>(a, r, j);

@@ -23,7 +23,9 @@ __global__ void k_linescan(LinescanArgs a) {
       dye = a.S64[(size_t)r * 6 * a.n_state + 5 * (size_t)a.n_state + e];
     } else {
       const size_t o = (size_t)r * a.n_state + e;
-      dye = a.rest_dye[e] + ((double)a.M[o].w - (double)a.CM[o].w);
+      const float u = a.M[o].w;
+      const float c = a.CMq ? comp_load1(a.CMq[o].w) : a.CM[o].w;
+      dye = a.rest_dye[e] + ((double)u - (double)c);
     }
     acc += a.w[q] * dye;
   }

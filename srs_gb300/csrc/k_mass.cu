@@ -27,12 +27,21 @@ __global__ void k_total_ca(MassArgs a) {
       bound = S[n + e] + S[2 * n + e] + S[3 * n + e] + S[4 * n + e] + S[5 * n + e];
     } else {
       const size_t o = (size_t)r * a.n_state + e;
-      const float4 m = a.M[o], cm = a.CM[o];
+      const float4 m = a.M[o];
+      const float im = a.I[o];
+      float4 cm;
+      float ci;
+      if (a.CMq) {  // compact compensation (srs_comp.h)
+        cm = comp_load4(a.CMq[o]);
+        ci = comp_load1(a.CIq[o]);
+      } else {
+        cm = a.CM[o];
+        ci = a.CI[o];
+      }
       const double* rs = a.rest4 + 4 * (size_t)e;
       c = rs[0] + ((double)m.x - (double)cm.x);
       bound = (rs[1] + ((double)m.y - (double)cm.y)) + (rs[2] + ((double)m.z - (double)cm.z)) +
-              (rs[3] + ((double)m.w - (double)cm.w)) +
-              (a.rest_imm[e] + ((double)a.I[o] - (double)a.CI[o]));
+              (rs[3] + ((double)m.w - (double)cm.w)) + (a.rest_imm[e] + ((double)im - (double)ci));
     }
     const double sl = a.bhi[e] * c / (a.khi + c) + a.blo[e] * c / (a.klo + c);
     acc[a.jsr[e] ? 1 : 0] += v0 * (c + bound + sl);

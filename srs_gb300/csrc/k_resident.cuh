@@ -3,6 +3,8 @@
 // per cluster size in the k_res_*.cu units (SRS_RESIDENT_DEFINE), which
 // compile in parallel; k_fp32.cu dispatches on the cluster size.
 #pragma once
+#include <type_traits>
+
 #include "srs_cluster.cuh"
 #include "srs_engine.h"
 #include "srs_fp32_update.cuh"
@@ -281,6 +283,7 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         const float4* src = cur ? buf1 : buf0;
         float4* dst = cur ? buf0 : buf1;
         const uint32_t* bs = tail->base[cur];
+        const uint32_t src_local = smem_addr(src);
         if constexpr (TRAJ) {
           if (chan_warp) {
             const int W = NR + 2 * NL + 1;
@@ -300,7 +303,10 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         // Elements lo + idx, lo + idx + stride, ... below hi; idx carries
         // over to the next range, so consecutive ranges are dealt out as
         // one sequence and every thread gets the same count.
-        auto update = [&](int& idx, int lo, int hi, int stride) {
+        // `local`: every neighbour of the range lies in this CTA's partition
+        // (the interior range), so its state is read from this CTA's shared
+        // memory directly, without the per-rank base lookup.
+        auto update = [&](int& idx, int lo, int hi, int stride, auto local) {
           const int first = lo + idx;
           // geometry of the next element is loaded one iteration ahead
           float4 ga_n = make_float4(0, 0, 0, 0), gb_n = ga_n;
@@ -344,6 +350,11 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
               n1 = ld_smem_f4(bs[0] + c1 * 16u);
               n2 = ld_smem_f4(bs[0] + c2 * 16u);
               n3 = ld_smem_f4(bs[0] + c3 * 16u);
+            } else if constexpr (decltype(local)::value) {
+              n0 = ld_smem_f4(src_local + (c0 & off_mask) * 16u);
+              n1 = ld_smem_f4(src_local + (c1 & off_mask) * 16u);
+              n2 = ld_smem_f4(src_local + (c2 & off_mask) * 16u);
+              n3 = ld_smem_f4(src_local + (c3 & off_mask) * 16u);
             } else {
               n0 = ld_dsmem_f4(bs[c0 >> a.off_bits] + (c0 & off_mask) * 16u);
               n1 = ld_dsmem_f4(bs[c1 >> a.off_bits] + (c1 & off_mask) * 16u);
@@ -377,13 +388,13 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
           if (split) {
             if (chan_group) {
               int idx = tid;
-              update(idx, 0, n_ch, ng);
+              update(idx, 0, n_ch, ng, std::false_type{});
               group_sync(ng);  // the group wrote the channel elements itself
               if (!P_.nogating) resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, cs, tid, ng);
             }
           } else {
             int idx = tid;
-            update(idx, 0, n_ch, nthr);
+            update(idx, 0, n_ch, nthr, std::false_type{});
             __syncthreads();
             if (chan_warp && !P_.nogating)
               resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, cs, lane, 32);
@@ -426,14 +437,14 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         }
         // interior elements: neighbours all in this partition
         int idx = wt;
-        if (worker) update(idx, n_ch, n_ch + n_int, wn);
+        if (worker) update(idx, n_ch, n_ch + n_int, wn, std::true_type{});
         if (a.ch_interior && rank == 0 && n_ch > 0) channels();
         if (spec) {  // no termination inside this launch: nothing to read
           cl_wait<C>();
           pending = false;
         }
         // boundary elements: some neighbour in another partition
-        if (worker) update(idx, n_ch + n_int, n_loc, wn);
+        if (worker) update(idx, n_ch + n_int, n_loc, wn, std::false_type{});
         if (!a.ch_interior && rank == 0 && n_ch > 0) channels();
         __syncthreads();
         cl_arrive<C>();

@@ -80,6 +80,10 @@ struct srs_sim {
   float* d_I[2] = {nullptr, nullptr};
   float4* d_CM = nullptr;  // FP32 engines: Euler compensation terms
   float* d_CI = nullptr;
+  // the large-mesh form of the plain FP32 engine keeps them compact
+  // (srs_comp.h) in these instead
+  ushort4* d_CMq = nullptr;
+  uint16_t* d_CIq = nullptr;
   int C = 1, threads = 0, n_clusters = 0, P_stride = 0, off_bits = 0;
   size_t smem = 0;
   std::vector<int> part_start, part_len, part_nch, part_nint;  // resident partitions
@@ -464,8 +468,13 @@ int setup_plain32(srs_sim* s) {
     SRS_TRY(dev_alloc(s, &s->d_M[b], (size_t)s->R * N));
     SRS_TRY(dev_alloc(s, &s->d_I[b], (size_t)s->R * N));
   }
-  SRS_TRY(dev_alloc(s, &s->d_CM, (size_t)s->R * N));
-  SRS_TRY(dev_alloc(s, &s->d_CI, (size_t)s->R * N));
+  if (N >= PLAIN32_SPLIT_N) {
+    SRS_TRY(dev_alloc(s, &s->d_CMq, (size_t)s->R * N));
+    SRS_TRY(dev_alloc(s, &s->d_CIq, (size_t)s->R * N));
+  } else {
+    SRS_TRY(dev_alloc(s, &s->d_CM, (size_t)s->R * N));
+    SRS_TRY(dev_alloc(s, &s->d_CI, (size_t)s->R * N));
+  }
   SRS_TRY(upload_channels_engine_order(s));
   return SRS_OK;
 }
@@ -790,8 +799,13 @@ int upload_state_range(srs_sim* s, int r0, int r1, const double* S6) {
                            cudaMemcpyHostToDevice, s->st));
   SRS_CUDA(cudaMemcpyAsync(s->d_I[0] + (size_t)r0 * NE, hI, NE * nr * sizeof(float),
                            cudaMemcpyHostToDevice, s->st));
-  SRS_CUDA(cudaMemsetAsync(s->d_CM + (size_t)r0 * NE, 0, NE * nr * sizeof(float4), s->st));
-  SRS_CUDA(cudaMemsetAsync(s->d_CI + (size_t)r0 * NE, 0, NE * nr * sizeof(float), s->st));
+  if (s->d_CMq) {  // q = 0 is c = 0
+    SRS_CUDA(cudaMemsetAsync(s->d_CMq + (size_t)r0 * NE, 0, NE * nr * sizeof(ushort4), s->st));
+    SRS_CUDA(cudaMemsetAsync(s->d_CIq + (size_t)r0 * NE, 0, NE * nr * sizeof(uint16_t), s->st));
+  } else {
+    SRS_CUDA(cudaMemsetAsync(s->d_CM + (size_t)r0 * NE, 0, NE * nr * sizeof(float4), s->st));
+    SRS_CUDA(cudaMemsetAsync(s->d_CI + (size_t)r0 * NE, 0, NE * nr * sizeof(float), s->st));
+  }
   SRS_CUDA(cudaStreamSynchronize(s->st));
   return SRS_OK;
 }
@@ -810,8 +824,20 @@ int download_state(srs_sim* s, int r, double* S6) {
   std::vector<float> I(NE), CIh(NE);
   SRS_CUDA(cudaMemcpy(M.data(), s->d_M[0] + r * NE, NE * sizeof(float4), cudaMemcpyDeviceToHost));
   SRS_CUDA(cudaMemcpy(I.data(), s->d_I[0] + r * NE, NE * sizeof(float), cudaMemcpyDeviceToHost));
-  SRS_CUDA(cudaMemcpy(CMh.data(), s->d_CM + r * NE, NE * sizeof(float4), cudaMemcpyDeviceToHost));
-  SRS_CUDA(cudaMemcpy(CIh.data(), s->d_CI + r * NE, NE * sizeof(float), cudaMemcpyDeviceToHost));
+  if (s->d_CMq) {
+    std::vector<ushort4> Q(NE);
+    std::vector<uint16_t> QI(NE);
+    SRS_CUDA(cudaMemcpy(Q.data(), s->d_CMq + r * NE, NE * sizeof(ushort4), cudaMemcpyDeviceToHost));
+    SRS_CUDA(cudaMemcpy(QI.data(), s->d_CIq + r * NE, NE * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    for (size_t e = 0; e < NE; ++e) {
+      CMh[e] = make_float4(comp_decode_host(Q[e].x), comp_decode_host(Q[e].y), comp_decode_host(Q[e].z),
+                           comp_decode_host(Q[e].w));
+      CIh[e] = comp_decode_host(QI[e]);
+    }
+  } else {
+    SRS_CUDA(cudaMemcpy(CMh.data(), s->d_CM + r * NE, NE * sizeof(float4), cudaMemcpyDeviceToHost));
+    SRS_CUDA(cudaMemcpy(CIh.data(), s->d_CI + r * NE, NE * sizeof(float), cudaMemcpyDeviceToHost));
+  }
   const RestValues& rv = s->rv;
   for (size_t e = 0; e < NE; ++e) {
     int j = s->ref_of_eng[e];
@@ -886,6 +912,8 @@ void refresh_args(srs_sim* s) {
     s->a32.k = make_consts32(s);
     s->a32.CM = s->d_CM;
     s->a32.CI = s->d_CI;
+    s->a32.CMq = s->d_CMq;
+    s->a32.CIq = s->d_CIq;
   } else {
     s->ar.P_ = s->P;
     s->ar.C = s->ch;
@@ -1638,6 +1666,7 @@ int srs_run_simulation_grid(srs_sim* s, srs_run_output* out, srs_grid_callback c
 // ---- multi-mesh batch ----------------------------------------------------------
 struct srs_batch {
   std::vector<srs_sim*> sims;
+  std::vector<size_t> order;  // enqueue order: decreasing elements x realizations
   int S = 1000;  // steps per member launch in one graph replay
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr;
@@ -1657,9 +1686,12 @@ void batch_drop_graph(srs_batch* b) {
 
 // One replay: every member advances S steps on its own stream; the members'
 // launches are branches of one graph forked from and joined into b->st.
+// Members are enqueued by decreasing work (elements x realizations), so the
+// longest clusters are dispatched first and the small members fill the SMs
+// around them.
 int batch_enqueue(srs_batch* b, int steps, int first) {
   SRS_CUDA(cudaEventRecord(b->fork, b->st));
-  for (size_t i = 0; i < b->sims.size(); ++i) {
+  for (size_t i : b->order) {
     srs_sim* s = b->sims[i];
     SRS_CUDA(cudaStreamWaitEvent(s->st, b->fork, 0));
     SRS_TRY(resident_launch(s, steps, first));
@@ -1710,6 +1742,11 @@ int srs_batch_create(srs_sim* const* sims, int n, int steps_per_launch, srs_batc
   }
   srs_batch* b = new srs_batch();
   b->sims.assign(sims, sims + n);
+  b->order.resize(n);
+  for (int i = 0; i < n; ++i) b->order[i] = (size_t)i;
+  std::stable_sort(b->order.begin(), b->order.end(), [&](size_t x, size_t y) {
+    return (int64_t)sims[x]->N * sims[x]->R > (int64_t)sims[y]->N * sims[y]->R;
+  });
   b->S = steps_per_launch > 0 ? steps_per_launch : 1000;
   b->join.assign(n, nullptr);
   bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1939,6 +1976,7 @@ int srs_linescan(srs_sim* s, double* out, double* rest) {
   } else {
     a.M = s->d_M[0];
     a.CM = s->d_CM;
+    a.CMq = s->d_CMq;
   }
   if (launch_linescan(a, s->R, s->st)) return fail(SRS_ERR_CUDA, "line-scan launch failed");
   s->launches++;
@@ -2051,13 +2089,15 @@ int adjoint_setup(srs_sim* s) {
 
 // Device copies of the complete engine state of all realizations.
 struct StateSnap {
-  float4* M;
-  float* I;
-  float4* CM;
-  float* CI;
-  int32_t *ryr, *lcc, *lccv;
-  double* res;
-  RealCtl* ctl;
+  float4* M = nullptr;
+  float* I = nullptr;
+  float4* CM = nullptr;  // compensation: float, or compact (srs_comp.h) in CMq / CIq
+  float* CI = nullptr;
+  ushort4* CMq = nullptr;
+  uint16_t* CIq = nullptr;
+  int32_t *ryr = nullptr, *lcc = nullptr, *lccv = nullptr;
+  double* res = nullptr;
+  RealCtl* ctl = nullptr;
 };
 
 // Reverse-sweep records with neighbour codes for CTAs that each hold m
@@ -2176,8 +2216,9 @@ int adjoint_plan(srs_sim* s, const srs_adjoint_desc* d, AdjPlan* pl) {
   const int64_t n_steps = d->n_steps, n_ticks = n_steps / te;
   // bytes: one recorded step, one snapshot of the whole state, lambda
   const size_t step_b = (size_t)R * (NE * (plain ? 28 : 24) + (size_t)W * 4);
-  const size_t snap_b = (size_t)R * NE * 40 + (size_t)R * (NR + 2 * NL) * 4 + (size_t)R * s->NCH * 8 +
-                        (size_t)R * sizeof(RealCtl);
+  // state 20 B per element, compensation 20 B (10 B compact)
+  const size_t snap_b = (size_t)R * NE * (s->d_CMq ? 30 : 40) + (size_t)R * (NR + 2 * NL) * 4 +
+                        (size_t)R * s->NCH * 8 + (size_t)R * sizeof(RealCtl);
   const size_t lam_b = (size_t)R * NE * (plain ? 76 : 44);
   size_t free_b = 0, total_b = 0, held = 0;
   for (auto& b : s->adj_bufs) held += b.second;
@@ -2230,8 +2271,13 @@ int snap_alloc(srs_sim* s, Scratch& sc, StateSnap* o) {
   const size_t n = (size_t)s->R * eng_count(s);
   SRS_TRY(sc.get(&o->M, n));
   SRS_TRY(sc.get(&o->I, n));
-  SRS_TRY(sc.get(&o->CM, n));
-  SRS_TRY(sc.get(&o->CI, n));
+  if (s->d_CMq) {
+    SRS_TRY(sc.get(&o->CMq, n));
+    SRS_TRY(sc.get(&o->CIq, n));
+  } else {
+    SRS_TRY(sc.get(&o->CM, n));
+    SRS_TRY(sc.get(&o->CI, n));
+  }
   SRS_TRY(sc.get(&o->ryr, (size_t)s->R * s->NR));
   SRS_TRY(sc.get(&o->lcc, (size_t)s->R * s->NL));
   SRS_TRY(sc.get(&o->lccv, (size_t)s->R * s->NL));
@@ -2248,8 +2294,13 @@ int snap_copy(srs_sim* s, const StateSnap& o, bool save) {
   };
   SRS_CUDA(cp(o.M, s->d_M[0], n * sizeof(float4)));
   SRS_CUDA(cp(o.I, s->d_I[0], n * sizeof(float)));
-  SRS_CUDA(cp(o.CM, s->d_CM, n * sizeof(float4)));
-  SRS_CUDA(cp(o.CI, s->d_CI, n * sizeof(float)));
+  if (s->d_CMq) {
+    SRS_CUDA(cp(o.CMq, s->d_CMq, n * sizeof(ushort4)));
+    SRS_CUDA(cp(o.CIq, s->d_CIq, n * sizeof(uint16_t)));
+  } else {
+    SRS_CUDA(cp(o.CM, s->d_CM, n * sizeof(float4)));
+    SRS_CUDA(cp(o.CI, s->d_CI, n * sizeof(float)));
+  }
   SRS_CUDA(cp(o.ryr, s->d_ryr, (size_t)s->R * s->NR * 4));
   SRS_CUDA(cp(o.lcc, s->d_lcc, (size_t)s->R * s->NL * 4));
   SRS_CUDA(cp(o.lccv, s->d_lccv, (size_t)s->R * s->NL * 4));
@@ -2786,6 +2837,8 @@ int srs_sim_total_ca(srs_sim* s, double* out) {
     m.CM = s->d_CM;
     m.I = s->d_I[0];
     m.CI = s->d_CI;
+    m.CMq = s->d_CMq;
+    m.CIq = s->d_CIq;
   }
   SRS_CUDA(cudaStreamSynchronize(s->st));
   if (launch_total_ca(m, s->R, s->st)) return fail(SRS_ERR_CUDA, "total-Ca launch failed");

@@ -1,6 +1,7 @@
 // srs_engine.h — host-side declarations of the kernel launchers and the
 // argument blocks they take (definitions in k_plain64.cu and k_fp32.cu).
 #pragma once
+#include "srs_comp.h"
 #include <cuda_runtime.h>
 
 #include "../../include/srs_gb300.h"
@@ -70,6 +71,10 @@ struct Plain32Args {
   float* I_out;
   float4* CM;  // [R][N] compensation of the Euler update (mobile species)
   float* CI;   // [R][N] compensation (immobile buffer)
+  // compact compensation (srs_comp.h; large meshes): when set, these hold
+  // the compensation and CM / CI are unused
+  ushort4* CMq;  // [R][N]
+  uint16_t* CIq;  // [R][N]
   Consts32 k;
   Protocol P;
   Channels C;
@@ -162,6 +167,7 @@ struct LinescanArgs {
   const double* S64;     // FP64 engine state [R][6][N] (or null)
   const float4* M;       // FP32 engines: deviations [R][n_state]
   const float4* CM;      //   and their compensation terms
+  const ushort4* CMq;    //   (or in compact form, srs_comp.h)
   const double* rest_dye;  // [n_state] resting bound dye per element
   double* out;           // [R][n_samples]
 };
@@ -180,6 +186,8 @@ struct MassArgs {
   const float4* CM;
   const float* I;
   const float* CI;
+  const ushort4* CMq;     // compact compensation (srs_comp.h), when set
+  const uint16_t* CIq;
   const double* rest4;    // [n_state][4] rest of Ca, ATP, CMDN, dye
   const double* rest_imm; // [n_state]
   double* out;            // [R][2]: cytosol, JSR

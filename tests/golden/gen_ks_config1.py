@@ -15,8 +15,8 @@ the states rows give the RyR open counts.  Metrics per run: ks_metrics.py.
 
 Per-run results go to DIR (one small .npz per run, so an interrupted job
 resumes where it stopped); when all runs are there the script writes
-tests/golden/ks_config1.npz (metrics, RyR open counts per tick, the centre
-dF/F0 traces, the parameter vectors).  A run takes about 110 s on one core of
+tests/golden/ks_config1.npz (metrics, RyR open counts per tick, the most
+LCCs open at any tick, the centre dF/F0 traces, the parameter vectors).  A run takes about 110 s on one core of
 a 2.7 GHz x86 host.
 """
 import argparse
@@ -82,7 +82,7 @@ def assemble(work, n_runs, dest):
     from ks_metrics import NAMES, spark_metrics
     p = params()
     ns = int((LINESCAN["x_max"] - LINESCAN["x_min"]) / LINESCAN["res"])
-    centre, opens, metrics = [], [], []
+    centre, opens, lccs, metrics = [], [], [], []
     for i in range(n_runs):
         d = np.load(os.path.join(work, "run%05d.npz" % i))
         ls, rows = d["ls"], d["rows"]
@@ -92,9 +92,11 @@ def assemble(work, n_runs, dest):
         n = rows[:N_TICKS + 1, 2]
         centre.append((c / c[0] - 1.0).astype(np.float32))
         opens.append(n.astype(np.int8))
+        lccs.append(int(rows[:N_TICKS + 1, 3].max()))
         metrics.append(spark_metrics(c, n, TICK_MS))
     np.savez_compressed(dest, metrics=np.array(metrics), names=np.array(NAMES),
                         dff0_centre=np.array(centre), n_open=np.array(opens),
+                        max_lcc_open=np.array(lccs, np.int8),
                         ints=np.array(list(p.ints)), reals=np.array(list(p.reals)),
                         window_ms=WINDOW_MS, tick_ms=TICK_MS)
     print("wrote", dest, "from", n_runs, "runs")

@@ -2,17 +2,18 @@
 
 tests/golden/ks_reference.npz holds 1000 runs of the reference's own
 cpu/RunSimulation.cpp (glibc rand() gating; written by
-tests/golden/gen_ks_reference.py).  The same protocol runs here as 1000
-realizations of the FP32 resident engine (Philox gating, seeds 1..1000),
-and every metric must pass a two-sample Kolmogorov-Smirnov test at
-p > 0.01: peak cleft Ca, time to peak, FDHM, maximum open RyRs, RyR open time.
+tests/golden/gen_ks_reference.py) of a short recruiting protocol on the
+golden mesh.  The same protocol runs here as 1000 realizations of the FP32
+resident engine (Philox gating, seeds 1..1000), and the metrics are
+compared: peak cleft Ca, time to peak, FDHM, maximum open RyRs, RyR open
+time.
 
-The metric distributions have atoms: about a fifth of the runs reach their
-peak at the first output tick with no other RyR open, so their peak is one
-deterministic number.  The FP32 engine reproduces it within the deterministic
-tolerance (1e-5 relative), not bit for bit, and a KS test would count the two
-copies of the atom as different values.  Engine values within that tolerance
-of a reference value are therefore taken as that value before the test.
+Runs in which RyR 4 stays open through the window and no other RyR opens
+(about a fifth) share one deterministic trajectory: the distributions are a
+mixture of that atom and a continuous part, compared in parts
+(tests/ks_mixture.py): the atom's mass (Fisher's exact test), every metric
+of the other runs (KS, p > 0.01), and the atom's value against the
+reference's at the deterministic tolerance (1e-5 relative).
 """
 import importlib.util
 import os
@@ -21,6 +22,8 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, GOLDEN_MESH
+from ks_mixture import mixture_ks, plain_ks
+
 
 def _gen_module():
     spec = importlib.util.spec_from_file_location(
@@ -33,27 +36,16 @@ def _gen_module():
 REL_TOL = 1e-5  # deterministic-part tolerance of the FP32 engine
 
 
-def snap_to_reference(ref, x, rel=REL_TOL):
-    """Replace each value of x by the nearest value of ref when they agree
-    within rel (relative); other values are left as they are."""
-    u = np.unique(ref)
-    j = np.clip(np.searchsorted(u, x), 1, len(u) - 1)
-    lo, hi = u[j - 1], u[j]
-    near = np.where(np.abs(x - lo) <= np.abs(hi - x), lo, hi)
-    ok = np.abs(near - x) <= rel * np.maximum(np.abs(near), 1e-12)
-    return np.where(ok, near, x)
-
-
-def test_snap_to_reference_only_merges_within_tolerance():
-    ref = np.array([1.0, 2.0, 8.3652])
-    x = np.array([8.36520005, 8.3660, 1.0, 0.5])
-    out = snap_to_reference(ref, x)
-    assert out[0] == 8.3652 and out[1] == 8.3660 and out[2] == 1.0 and out[3] == 0.5
+def atom_mask(m):
+    """RyR 4 open at every output tick and no other RyR open: one open RyR
+    at most and the whole window's open time (both exact tick counts)."""
+    full = m[m[:, 3] == 1, 4].max()
+    return (m[:, 3] == 1) & (m[:, 4] == full)
 
 
 @pytest.mark.gpu
 def test_spark_metric_distributions_match_reference(srs):
-    stats = pytest.importorskip("scipy.stats")
+    pytest.importorskip("scipy.stats")
     d = np.load(os.path.join(GOLDEN, "ks_reference.npz"))
     ref = d["metrics"]
     names = [str(x) for x in d["names"]]
@@ -69,9 +61,12 @@ def test_spark_metric_distributions_match_reference(srs):
     rows, t_end, n_steps = sim.run_simulation()
     metrics = _gen_module().metrics
     gpu = np.array([metrics(r) for r in rows])
-    report = {}
-    for k, name in enumerate(names):
-        res = stats.ks_2samp(ref[:, k], snap_to_reference(ref[:, k], gpu[:, k]))
-        report[name] = (float(res.pvalue), float(ref[:, k].mean()), float(gpu[:, k].mean()))
-    bad = {n: v for n, v in report.items() if not v[0] > 0.01}
+    ref_atom, gpu_atom = atom_mask(ref), atom_mask(gpu)
+    report, bad = mixture_ks(ref, gpu, ref_atom, gpu_atom, names)
     assert not bad, report
+    # the atom's value: the reference's (FP64) and the engine's (FP32) peak
+    v_ref = np.unique(ref[ref_atom, 0], return_counts=True)
+    v_gpu = np.unique(gpu[gpu_atom, 0], return_counts=True)
+    a_ref, a_gpu = v_ref[0][np.argmax(v_ref[1])], v_gpu[0][np.argmax(v_gpu[1])]
+    assert abs(a_gpu - a_ref) <= REL_TOL * abs(a_ref), (a_gpu, a_ref)
+    print("golden-mesh KS:", report, "plain KS (atoms included):", plain_ks(ref, gpu, names))
