@@ -39,6 +39,8 @@ LINESCAN = dict(axis=0, offset1=0.0, offset2=0.1, x_min=-1.0, x_max=1.0, res=0.0
 
 def test_config1_spark_distributions_match_reference(srs, box_mesh):
     pytest.importorskip("scipy.stats")
+    if not os.path.exists(FIXTURE):
+        pytest.skip("reference ensemble tests/golden/ks_config1.npz not generated")
     from srs_gb300.metrics import NAMES, spark_metrics
     d = np.load(FIXTURE)
     ref = d["metrics"]
