@@ -287,11 +287,11 @@ int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, s
 }
 
 // Largest number of co-resident clusters for a configuration (0: does not fit).
-int resident_max_clusters(int C, int threads, size_t smem, int geo_smem) {
+int resident_max_clusters(int C, int threads, size_t smem) {
   switch (C) {
 #define SRS_M(CC) \
   case CC:        \
-    return resident_max_clusters_c##CC(threads, smem, geo_smem);
+    return resident_max_clusters_c##CC(threads, smem);
     SRS_RESIDENT_SIZES(SRS_M)
 #undef SRS_M
     default: return 0;

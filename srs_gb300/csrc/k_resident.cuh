@@ -154,10 +154,7 @@ static __device__ void resident_prestep(const ResidentArgs& a, RealCtl& ctl, con
 // TRAJ: also record, for every step of the launch, the state the step starts
 // from, its Ca rate before the rapid-buffer factor and the channel states it
 // uses (the trajectory the adjoint is conditioned on).
-// GEO: the partition's geometry records are staged in shared memory once per
-// launch (configurations with one CTA per SM) instead of read from L2 every
-// step.
-template <int C, bool TRAJ, bool GEO>
+template <int C, bool TRAJ>
 // At most 640 threads per CTA: two CTAs of up to 320 threads share an SM
 // with up to 96 registers per thread (the tuned configurations), and
 // single-CTA configurations keep the same budget.
@@ -207,8 +204,7 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
   const bool chan_group = split && tid < ng;
   const bool chan_warp = (rank == 0) && (warp == 0);
   const int n_int = a.n_int[rank];  // interior elements follow the channel elements
-  const TetRec* geo_g = a.geo + (size_t)rank * P;
-  TetRec* geo_s = reinterpret_cast<TetRec*>(smem + a.geo_off);  // GEO only
+  const TetRec* geo = a.geo + (size_t)rank * P;
   const uint32_t off_mask = (1u << a.off_bits) - 1u;
   const Consts32& k = a.k;
   const Protocol& P_ = a.P_;
@@ -226,11 +222,6 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
     }
   }
 
-  if constexpr (GEO) {
-    const float4* gsrc = reinterpret_cast<const float4*>(geo_g);
-    float4* gdst = reinterpret_cast<float4*>(geo_s);
-    for (int i = tid; i < 2 * n_loc; i += nthr) gdst[i] = __ldg(gsrc + i);
-  }
   if (tid < 32) {
     for (int q = lane; q < C; q += 32) {
       tail->base[0][q] = (C > 1) ? map_rank(smem_addr(buf0), q) : smem_addr(buf0);
@@ -318,23 +309,20 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         auto update = [&](int& idx, int lo, int hi, int stride, auto local) {
           const int first = lo + idx;
           // geometry of the next element is loaded one iteration ahead
-          auto geo_load = [&](int e, float4& ga_, float4& gb_) {
-            if constexpr (GEO) {
-              const float4* gp = reinterpret_cast<const float4*>(geo_s + e);
-              ga_ = gp[0];
-              gb_ = gp[1];
-            } else {
-              const float4* gp = reinterpret_cast<const float4*>(geo_g + e);
-              ga_ = __ldg(gp);
-              gb_ = __ldg(gp + 1);
-            }
-          };
           float4 ga_n = make_float4(0, 0, 0, 0), gb_n = ga_n;
-          if (first < hi) geo_load(first, ga_n, gb_n);
+          if (first < hi) {
+            const float4* gp = reinterpret_cast<const float4*>(geo + first);
+            ga_n = __ldg(gp);
+            gb_n = __ldg(gp + 1);
+          }
           int i = first;
           for (; i < hi; i += stride) {
             const float4 ga = ga_n, gb = gb_n;
-            if (i + stride < hi) geo_load(i + stride, ga_n, gb_n);
+            if (i + stride < hi) {
+              const float4* gp = reinterpret_cast<const float4*>(geo + i + stride);
+              ga_n = __ldg(gp);
+              gb_n = __ldg(gp + 1);
+            }
             uint32_t w0 = __float_as_uint(gb.x), w1 = __float_as_uint(gb.y);
             uint32_t c0 = w0 & 0xffffu, c1 = w0 >> 16, c2 = w1 & 0xffffu, c3 = w1 >> 16;
             const uint32_t fl = __float_as_uint(gb.w);
@@ -502,21 +490,21 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
   step_barrier<C>();  // no CTA leaves while others may read its shared memory
 }
 
-template <int C, bool TRAJ, bool GEO>
+template <int C, bool TRAJ>
 static cudaError_t set_attrs(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_resident32<C, TRAJ, GEO>,
+  cudaError_t e = cudaFuncSetAttribute(k_resident32<C, TRAJ>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (C > 8)
-    e = cudaFuncSetAttribute(k_resident32<C, TRAJ, GEO>,
-                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    e = cudaFuncSetAttribute(k_resident32<C, TRAJ>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                             1);
   return e;
 }
 
-template <int C, bool TRAJ, bool GEO>
+template <int C, bool TRAJ>
 static int launch_resident_t(const ResidentArgs& a, int n_clusters, int threads, size_t smem,
                              cudaStream_t st) {
-  if (set_attrs<C, TRAJ, GEO>(smem) != cudaSuccess) return -1;
+  if (set_attrs<C, TRAJ>(smem) != cudaSuccess) return -1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n_clusters * C);
   cfg.blockDim = dim3(threads);
@@ -529,13 +517,13 @@ static int launch_resident_t(const ResidentArgs& a, int n_clusters, int threads,
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, k_resident32<C, TRAJ, GEO>, a);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_resident32<C, TRAJ>, a);
   return e == cudaSuccess ? 0 : -1;
 }
 
-template <int C, bool GEO>
+template <int C>
 static int max_clusters_t(int threads, size_t smem) {
-  if (set_attrs<C, false, GEO>(smem) != cudaSuccess || set_attrs<C, true, false>(smem) != cudaSuccess) {
+  if (set_attrs<C, false>(smem) != cudaSuccess || set_attrs<C, true>(smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -552,8 +540,8 @@ static int max_clusters_t(int threads, size_t smem) {
   cfg.numAttrs = 1;
   int n = 0;
   int n2 = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_resident32<C, false, GEO>, &cfg) != cudaSuccess ||
-      cudaOccupancyMaxActiveClusters(&n2, k_resident32<C, true, false>, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, k_resident32<C, false>, &cfg) != cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&n2, k_resident32<C, true>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -567,12 +555,10 @@ static int max_clusters_t(int threads, size_t smem) {
   namespace srs {                                                                        \
   int launch_resident_c##CC(const ResidentArgs& a, int n_clusters, int threads, size_t smem, \
                             cudaStream_t st) {                                           \
-    if (a.traj_u) return launch_resident_t<CC, true, false>(a, n_clusters, threads, smem, st); \
-    return a.geo_smem ? launch_resident_t<CC, false, true>(a, n_clusters, threads, smem, st) \
-                      : launch_resident_t<CC, false, false>(a, n_clusters, threads, smem, st); \
+    return a.traj_u ? launch_resident_t<CC, true>(a, n_clusters, threads, smem, st)      \
+                    : launch_resident_t<CC, false>(a, n_clusters, threads, smem, st);    \
   }                                                                                      \
-  int resident_max_clusters_c##CC(int threads, size_t smem, int geo_smem) {              \
-    return geo_smem ? max_clusters_t<CC, true>(threads, smem)                            \
-                    : max_clusters_t<CC, false>(threads, smem);                          \
+  int resident_max_clusters_c##CC(int threads, size_t smem) {                            \
+    return max_clusters_t<CC>(threads, smem);                                            \
   }                                                                                      \
   }

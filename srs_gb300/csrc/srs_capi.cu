@@ -707,23 +707,8 @@ int setup_resident(srs_sim* s, int C, int threads) {
   if (!resident_cluster_supported(C)) return fail(SRS_ERR_UNSUPPORTED, "unsupported cluster size");
   s->C = C;
   s->threads = threads;
-  const size_t base = resident_smem_bytes(s->P_stride, s->NR, s->NL, s->part_nch[0], 2 * s->NR + s->NL);
-  // Geometry in shared memory when only one CTA fits on an SM anyway (more
-  // than half the thread budget, or more than half the SM's shared memory)
-  // and the records fit next to the state.
-  {
-    int dev = 0, smem_sm = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const size_t off = (base + 15) & ~(size_t)15;
-    const size_t with_geo = off + (size_t)s->P_stride * sizeof(TetRec);
-    const bool two_per_sm = 2 * threads <= SRS_RESIDENT_MAX_THREADS && 2 * (base + 1024) <= (size_t)smem_sm;
-    s->ar.geo_smem = (!two_per_sm && with_geo <= (size_t)optin) ? 1 : 0;
-    s->ar.geo_off = (int32_t)off;
-    s->smem = s->ar.geo_smem ? with_geo : base;
-  }
-  int maxc = resident_max_clusters(C, threads, s->smem, s->ar.geo_smem);
+  s->smem = resident_smem_bytes(s->P_stride, s->NR, s->NL, s->part_nch[0], 2 * s->NR + s->NL);
+  int maxc = resident_max_clusters(C, threads, s->smem);
   if (maxc <= 0) return fail(SRS_ERR_UNSUPPORTED, "resident configuration does not fit on the device");
   s->n_clusters = std::min(maxc, s->R);
   return SRS_OK;

@@ -122,11 +122,6 @@ struct ResidentArgs {
   int32_t off_bits;
   int32_t steps;
   const TetRec* geo;
-  // geometry staged in shared memory at byte offset geo_off of the dynamic
-  // block (configurations with one CTA per SM, where it fits); else read from
-  // global memory (L2) every step
-  int32_t geo_smem;
-  int32_t geo_off;
   int32_t prestep_first;  // run the protocol of the first step before it
   int32_t initial_row;    // ... and write the t = 0 states row
   const int32_t* n_local; // [C] elements in each partition
@@ -330,7 +325,7 @@ size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries);
 #define SRS_RESIDENT_DECLARE(CC)                                                            \
   int launch_resident_c##CC(const ResidentArgs& a, int n_clusters, int threads, size_t smem, \
                             cudaStream_t st);                                              \
-  int resident_max_clusters_c##CC(int threads, size_t smem, int geo_smem);
+  int resident_max_clusters_c##CC(int threads, size_t smem);
 SRS_RESIDENT_DECLARE(1)
 SRS_RESIDENT_DECLARE(2)
 SRS_RESIDENT_DECLARE(3)
@@ -342,7 +337,7 @@ SRS_RESIDENT_DECLARE(16)
 #undef SRS_RESIDENT_DECLARE
 int launch_resident(const ResidentArgs& a, int C, int n_clusters, int threads, size_t smem,
                     cudaStream_t st);
-int resident_max_clusters(int C, int threads, size_t smem, int geo_smem);
+int resident_max_clusters(int C, int threads, size_t smem);
 bool resident_cluster_supported(int C);
 
 }  // namespace srs
