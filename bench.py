@@ -538,6 +538,26 @@ def fp64_error(srs, grid, p, n, engine, **sim_kw):
             "against": "FP64 plain engine, gating off"}
 
 
+def mass_balance(srs, grid, p, n, engine, **sim_kw):
+    """Mass balance of an FP32 engine with every Ca source and sink across the
+    compartment boundary off (SERCA A_P = 0, JSR refill V_REFILL = 0, LCCs
+    closed and gating off, no-flux boundaries), RyR 24 held open so Ca moves
+    from the JSR into the cytosol: over n steps the total Ca of cytosol + JSR
+    (free, bound and rapid-buffer Ca, FP64 sums of the state: srs_sim_total_ca)
+    must stay constant.  Returns the relative change of the total and the
+    moved fraction (the JSR's loss relative to the total)."""
+    import numpy as np
+    pm = p.copy().set(A_P=0.0, V_REFILL=0.0, FLAG_NO_GATING=1, FLAG_NO_FLUX_BOUNDARY=1)
+    sim = srs.Simulation(grid, pm, 2, srs.FP32, engine, seeds=[1, 2], **sim_kw)
+    t0 = np.asarray(sim.total_ca())
+    sim.explicit_step(n)
+    t1 = np.asarray(sim.total_ca())
+    tot0, tot1 = t0.sum(1), t1.sum(1)
+    return {"steps": n, "total_rel_change": float(np.max(np.abs(tot1 - tot0) / tot0)),
+            "moved_rel": float(np.max((t0[:, 1] - t1[:, 1]) / tot0)),
+            "sources": "SERCA, refill, LCC and boundary fluxes off; RyR 24 open"}
+
+
 def config0_spark(srs, args):
     """Plain single spark (config 0, the reference's CPU-runnable case): the
     config mesh, one realization in FP64 on the plain engine under the
@@ -604,7 +624,10 @@ def config4_site(srs, args):
     g = srs.Grid(p, base)
     t_load = time.perf_counter() - t0
     R = args.config4_realizations
+    from srs_gb300 import tuner
+    tuned = tuner.tune_plain(g, p, R, seeds=list(range(1, R + 1)))
     sim = srs.Simulation(g, p, R, srs.FP32, srs.ENGINE_PLAIN, seeds=list(range(1, R + 1)))
+    sim.set_prefetch(tuned["prefetch_blocks"])
     sim.reset()
     tot0 = sim.total_ca()
     _, _, n_run, launch_ms = sim.run_simulation(timed=True)
@@ -617,6 +640,7 @@ def config4_site(srs, args):
     peak, peak_kind = measured_peaks()
     del sim
     err64 = fp64_error(srs, g, p, 2048, srs.ENGINE_PLAIN)
+    mass = mass_balance(srs, g, p, 2048, srs.ENGINE_PLAIN)
     adj = None
     if args.config4_adjoint_steps > 0:
         adj = config4_adjoint(srs, base, R, args.config4_adjoint_steps, ms / n)
@@ -627,7 +651,10 @@ def config4_site(srs, args):
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
                          "note": "algorithmic 48 + 44/R B per element-step; peak %s" % peak_kind},
-            "fp64_error": err64, "mesh_generation_s": t_gen, "mesh_load_s": t_load,
+            "prefetch_blocks": tuned["prefetch_blocks"],
+            "prefetch_trials": [(t["prefetch_blocks"], t["ms_per_step"]) for t in tuned["trials"]],
+            "fp64_error": err64, "mass_balance": mass, "mesh_generation_s": t_gen,
+            "mesh_load_s": t_load,
             "total_ca_start": np.asarray(tot0)[0].tolist(), "total_ca_end": np.asarray(tot1)[0].tolist()}
 
 
@@ -806,6 +833,14 @@ def run_ours(args):
                                threads_per_cta=tuned["threads_per_cta"])
         except Exception as e:  # noqa: BLE001
             err64 = {"error": "%s: %s" % (type(e).__name__, e)}
+    mass = None
+    if rank == 0 and args.fp64_steps > 0:
+        try:
+            mass = mass_balance(srs, grid, p, args.fp64_steps, srs.ENGINE_RESIDENT,
+                                cluster_size=tuned["cluster_size"],
+                                threads_per_cta=tuned["threads_per_cta"])
+        except Exception as e:  # noqa: BLE001
+            mass = {"error": "%s: %s" % (type(e).__name__, e)}
     adj = None
     if rank == 0 and not args.no_adjoint:
         try:
@@ -863,6 +898,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "roofline": roof,
             "fp64_error": err64,
+            "mass_balance": mass,
             "cpu_baseline": cpu,
             "clocks": clk,
             "adjoint": adj,

@@ -191,6 +191,12 @@ typedef struct srs_sim_config {
   int64_t engine_elements;  /* element slots per realization in the engine layout */
 } srs_sim_config;
 int srs_sim_get_config(const srs_sim* s, srs_sim_config* c);
+/* Plain FP32 engine on meshes of 65,536 elements and more (the split form):
+ * how many element blocks of 256 ahead each update block asks L2 to prefetch
+ * (0: none; negative: the default, one wave of blocks).  A tuning knob of
+ * this implementation, no counterpart in the reference; srs_gb300/tuner.py
+ * searches it. */
+int srs_sim_set_prefetch(srs_sim* s, int element_blocks);
 
 /* ---- line scan (linescan/main.cpp:160-225) --------------------------------
  * PSF-weighted bound-dye fluorescence at sample points on a line, from the

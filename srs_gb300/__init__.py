@@ -209,6 +209,7 @@ _SIGS = {
     "srs_sim_time_advance": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
     "srs_sim_status": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "srs_sim_get_config": (C.c_int, [_P, C.POINTER(_SimConfig)]),
+    "srs_sim_set_prefetch": (C.c_int, [_P, C.c_int]),
     "srs_write_grid_vtk": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
     "srs_grid_write_vtk": (C.c_int, [_P, _P, _P, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
     "srs_box_mesh_default": (None, [C.POINTER(BoxMeshSpec)]),
@@ -406,6 +407,11 @@ class Simulation:
 
     def reset(self):
         _check(_lib.srs_sim_reset(self._h))
+
+    def set_prefetch(self, element_blocks):
+        """srs_sim_set_prefetch: L2 prefetch distance of the large-mesh plain
+        FP32 engine, in element blocks (negative: the default)."""
+        _check(_lib.srs_sim_set_prefetch(self._h, int(element_blocks)))
 
     def set_state(self, r, states=None, ryr=None, lcc=None, lccv=None, residuals=None):
         conv = lambda a, t: None if a is None else np.ascontiguousarray(a, dtype=t)

@@ -85,6 +85,7 @@ struct srs_sim {
   ushort4* d_CMq = nullptr;
   uint16_t* d_CIq = nullptr;
   int C = 1, threads = 0, n_clusters = 0, P_stride = 0, off_bits = 0;
+  int pf_override = -1;  // plain FP32 split form: L2 prefetch distance (-1: one wave)
   size_t smem = 0;
   std::vector<int> part_start, part_len, part_nch, part_nint;  // resident partitions
   int ch_interior = 0;
@@ -907,7 +908,7 @@ void refresh_args(srs_sim* s) {
       int dev = 0, n_sm = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-      s->a32.pf_rows = std::max(1, (n_sm * 6 + s->R - 1) / s->R);
+      s->a32.pf_rows = s->pf_override >= 0 ? s->pf_override : std::max(1, (n_sm * 6 + s->R - 1) / s->R);
     }
     s->a32.k = make_consts32(s);
     s->a32.CM = s->d_CM;
@@ -1290,6 +1291,15 @@ void srs_sim_destroy(srs_sim* s) {
 int srs_sim_get_desc(const srs_sim* s, srs_sim_desc* d) {
   if (!s || !d) return fail(SRS_ERR_INPUT, "null argument");
   *d = s->d;
+  return SRS_OK;
+}
+
+int srs_sim_set_prefetch(srs_sim* s, int element_blocks) {
+  if (!s) return fail(SRS_ERR_INPUT, "null argument");
+  if (s->d.engine != SRS_ENGINE_PLAIN || s->d.precision != SRS_FP32 || s->N < PLAIN32_SPLIT_N)
+    return fail(SRS_ERR_UNSUPPORTED, "the prefetch distance applies to the plain FP32 engine's large-mesh form");
+  s->pf_override = element_blocks < 0 ? -1 : element_blocks;
+  refresh_args(s);
   return SRS_OK;
 }
 

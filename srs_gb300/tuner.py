@@ -1,10 +1,13 @@
-"""Autotuner of the resident engine.
+"""Autotuners of the FP32 engines.
 
-Chooses the cluster size (CTAs sharing one realization) and the threads per
-CTA for a given grid and batch by timing short trial launches of each
-candidate on the device (CUDA events on the engine's stream).  The time steps
-per persistent launch are not searched: they are the caller's output cadence
-(the launch ends at every states-row or grid-file tick).  Results are cached per (element count, channel count,
+tune_resident: the resident engine's cluster size (CTAs sharing one
+realization) and threads per CTA for a given grid and batch, by timing short
+trial launches of each candidate on the device (CUDA events on the engine's
+stream).  The time steps per persistent launch are not searched: they are
+the caller's output cadence (the launch ends at every states-row or
+grid-file tick).
+
+tune_plain: the L2 prefetch distance of the plain engine's large-mesh form.  Results are cached per (element count, channel count,
 realizations, device) in a JSON file next to the package, so later runs start
 with the tuned configuration.
 """
@@ -65,6 +68,48 @@ def tune_resident(grid, params, R, seeds=None, clusters=(1, 2, 3, 4, 5, 6, 8),
         raise RuntimeError("no resident configuration fits this grid")
     best = min(trials, key=lambda d: d["ms_per_step"])
     out = dict(best, trials=trials)
+    if use_cache:
+        cache[key] = out
+        try:
+            json.dump(cache, open(CACHE, "w"), indent=1)
+        except OSError:
+            pass
+    return out
+
+
+def tune_plain(grid, params, R, seeds=None, waves=(0.0, 0.5, 1.0, 2.0, 4.0), trial_steps=32,
+               repeats=2, use_cache=True, verbose=False):
+    """Prefetch distance of the plain FP32 engine's large-mesh form (meshes of
+    65,536 elements and more): each update block asks L2 for the state of the
+    element block `distance` blocks ahead.  Candidates are fractions of one
+    wave (six blocks per SM over the realizations); each is timed over short
+    trial advances.  Returns dict(prefetch_blocks, ms_per_step, trials)."""
+    import torch
+    n_sm = torch.cuda.get_device_properties(0).multi_processor_count
+    wave = max(1, (n_sm * 6 + R - 1) // R)
+    key = "plain|" + _key(grid, R)
+    cache = {}
+    if use_cache and os.path.exists(CACHE):
+        try:
+            cache = json.load(open(CACHE))
+        except ValueError:
+            cache = {}
+        if key in cache:
+            return cache[key]
+    sim = srs.Simulation(grid, params, R, srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
+    sim.advance_async(trial_steps)
+    sim.synchronize()
+    trials = []
+    for w in sorted(set(int(round(f * wave)) for f in waves)):
+        sim.set_prefetch(w)
+        sim.time_advance(trial_steps)  # new graph for this distance
+        ms = min(sim.time_advance(trial_steps) for _ in range(repeats))
+        trials.append(dict(prefetch_blocks=w, ms_per_step=ms / trial_steps))
+        if verbose:
+            print("tuner: prefetch %d blocks %.4f ms/step" % (w, ms / trial_steps))
+    del sim
+    best = min(trials, key=lambda d: d["ms_per_step"])
+    out = dict(best, trials=trials, wave_blocks=wave)
     if use_cache:
         cache[key] = out
         try:
