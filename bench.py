@@ -443,16 +443,22 @@ def config2_batch(srs, args):
             g = srs.Grid(p, base)
             seeds = list(range(seed0, seed0 + 32))
             seed0 += 32
+            # alone, a member's 32 realizations leave SMs idle, so its best
+            # configuration buys parallelism with larger clusters; in the
+            # batch the other members fill those SMs, so there the
+            # configuration that is fastest per element-step on a full GPU
+            # (tuned on 256 realizations) is used
             t = tuner.tune_resident(g, p, 32, seeds=seeds)
-            members.append(dict(grid=g, p=p, seeds=seeds, tune=t, n_tets=rep_["n_tets"],
+            tb = tuner.tune_resident(g, p, 256, seeds=list(range(1, 257)))
+            members.append(dict(grid=g, p=p, seeds=seeds, tune=t, tune_batch=tb, n_tets=rep_["n_tets"],
                                 protocol=("leak", "lcc_trigger")[k], full_ms=full))
 
-    def make(S):
+    def make(S, which):
         out = []
         for m in members:
             sim = srs.Simulation(m["grid"], m["p"], 32, srs.FP32, srs.ENGINE_RESIDENT, seeds=m["seeds"],
-                                 cluster_size=m["tune"]["cluster_size"],
-                                 threads_per_cta=m["tune"]["threads_per_cta"], steps_per_launch=S)
+                                 cluster_size=m[which]["cluster_size"],
+                                 threads_per_cta=m[which]["threads_per_cta"], steps_per_launch=S)
             sim.reset()
             out.append(sim)
         return out
@@ -463,10 +469,10 @@ def config2_batch(srs, args):
 
     S = args.config2_launch_steps or max(launch_steps(m) for m in members)
     # warm-up: one graph replay of every member
-    sims = make(S)
+    sims = make(S, "tune_batch")
     srs.Batch(sims, steps_per_launch=S).time_advance(S)
-    # members one after another
-    sims = make(S)
+    # members one after another, each at its own tuned configuration
+    sims = make(S, "tune")
     torch_sync()
     one_rows, one_each = [], []
     for sim in sims:
@@ -475,7 +481,7 @@ def config2_batch(srs, args):
         one_each.append(time.perf_counter() - t0)
     one_s = sum(one_each)
     # the batch
-    sims = make(S)
+    sims = make(S, "tune_batch")
     b = srs.Batch(sims, steps_per_launch=S)
     torch_sync()
     t0 = time.perf_counter()
@@ -491,7 +497,10 @@ def config2_batch(srs, args):
         max_open = [float(r[:, 2].max()) for r in rows]
         lcc_open = [float(r[:, 3].max()) for r in rows]
         per.append({"tets": m["n_tets"], "protocol": m["protocol"],
-                    "cluster_size": sim.config()["cluster_size"], "steps": int(n_steps.max()),
+                    "cluster_size": sim.config()["cluster_size"],
+                    "threads_per_cta": sim.config()["threads_per_cta"],
+                    "alone_cluster_size": m["tune"]["cluster_size"],
+                    "alone_threads_per_cta": m["tune"]["threads_per_cta"], "steps": int(n_steps.max()),
                     "alone_s": t1, "alone_ps_per_element_step":
                         1e12 * t1 / (float(n_steps.sum()) * m["n_tets"]),
                     "runs_with_lcc_opening": int(sum(x > 0 for x in lcc_open)),
@@ -625,7 +634,10 @@ def config4_site(srs, args):
     t_load = time.perf_counter() - t0
     R = args.config4_realizations
     from srs_gb300 import tuner
-    tuned = tuner.tune_plain(g, p, R, seeds=list(range(1, R + 1)))
+    if args.no_tune:  # the default distance: one wave of blocks
+        tuned = dict(prefetch_blocks=-1, trials=[])
+    else:
+        tuned = tuner.tune_plain(g, p, R, seeds=list(range(1, R + 1)))
     sim = srs.Simulation(g, p, R, srs.FP32, srs.ENGINE_PLAIN, seeds=list(range(1, R + 1)))
     sim.set_prefetch(tuned["prefetch_blocks"])
     sim.reset()

@@ -306,7 +306,9 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         // `local`: every neighbour of the range lies in this CTA's partition
         // (the interior range), so its state is read from this CTA's shared
         // memory directly, without the per-rank base lookup.
-        auto update = [&](int& idx, int lo, int hi, int stride, auto local) {
+        // `chan`: the range of channel elements (head of partition 0), which add
+        // the release flux of their channels
+        auto update = [&](int& idx, int lo, int hi, int stride, auto local, auto chan) {
           const int first = lo + idx;
           // geometry of the next element is loaded one iteration ahead
           float4 ga_n = make_float4(0, 0, 0, 0), gb_n = ga_n;
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
             uint32_t c0 = w0 & 0xffffu, c1 = w0 >> 16, c2 = w1 & 0xffffu, c3 = w1 >> 16;
             const uint32_t fl = __float_as_uint(gb.w);
             float flux = 0.0f;
-            if (i < n_ch) {
+            if constexpr (decltype(chan)::value) {
               for (int q = s_cptr[i]; q < s_cptr[i + 1]; ++q) {
                 ChanEntry32 e = s_clist[q];
                 float J = 0.0f;
@@ -388,13 +390,13 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
           if (split) {
             if (chan_group) {
               int idx = tid;
-              update(idx, 0, n_ch, ng, std::false_type{});
+              update(idx, 0, n_ch, ng, std::false_type{}, std::true_type{});
               group_sync(ng);  // the group wrote the channel elements itself
               if (!P_.nogating) resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, cs, tid, ng);
             }
           } else {
             int idx = tid;
-            update(idx, 0, n_ch, nthr, std::false_type{});
+            update(idx, 0, n_ch, nthr, std::false_type{}, std::true_type{});
             __syncthreads();
             if (chan_warp && !P_.nogating)
               resident_gate(a, tail->ctl, dst, s_ryr, s_lcc, s_lccv, s_res, s_nb, cs, lane, 32);
@@ -437,14 +439,14 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         }
         // interior elements: neighbours all in this partition
         int idx = wt;
-        if (worker) update(idx, n_ch, n_ch + n_int, wn, std::true_type{});
+        if (worker) update(idx, n_ch, n_ch + n_int, wn, std::true_type{}, std::false_type{});
         if (a.ch_interior && rank == 0 && n_ch > 0) channels();
         if (spec) {  // no termination inside this launch: nothing to read
           cl_wait<C>();
           pending = false;
         }
         // boundary elements: some neighbour in another partition
-        if (worker) update(idx, n_ch + n_int, n_loc, wn, std::false_type{});
+        if (worker) update(idx, n_ch + n_int, n_loc, wn, std::false_type{}, std::false_type{});
         if (!a.ch_interior && rank == 0 && n_ch > 0) channels();
         __syncthreads();
         cl_arrive<C>();
