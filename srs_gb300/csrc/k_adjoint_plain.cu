@@ -14,7 +14,8 @@
 //     buffered; lambda_ATP/CMDN/dye have no other owner storage inside a
 //     segment;
 //   * lam_c, lam_im, lam_c4, lam_cim: the owner state (lambda_Ca, the
-//     immobile buffer's lambda, their Kahan compensation);
+//     immobile buffer's lambda, their Kahan compensation; on large meshes
+//     the compensation is kept as halves, lam_c4q / lam_cimq, srs_comp.h);
 //   * lam: the full lambda at the segment boundaries.
 // The transposed diffusion operator gathers the four neighbours' slots with
 // the transposed coefficients aT; Dirichlet faces (kb) join the diagonal, and
@@ -58,8 +59,10 @@ __global__ void __launch_bounds__(ADJP_THREADS) k_adjp_publish(AdjPlainArgs a) {
 
 // One reverse step t of the segment (x_{n-1} -> x_n, n = s0 + t): reads the
 // slots of step n (pub), writes those of step n - 1 (nxt), or the boundary
-// lambda when t == 1 (a.last).
-__global__ void __launch_bounds__(ADJP_THREADS) k_adjp_step(AdjPlainArgs a) {
+// lambda when t == 1 (a.last).  Four blocks per SM (64 registers, a few
+// spilled): the step waits on memory, and 32 warps per SM hide more of it
+// than 24 (1.11 against 0.84 ms per step on the config-4 mesh).
+__global__ void __launch_bounds__(ADJP_THREADS, 4) k_adjp_step(AdjPlainArgs a) {
   const int r = blockIdx.x;
   const Consts32& k = a.k;
   const AdjConsts& ak = a.ak;
@@ -85,8 +88,16 @@ __global__ void __launch_bounds__(ADJP_THREADS) k_adjp_step(AdjPlainArgs a) {
     const float2 ig = a.tig[o];
     const float4 me = pub[j];
     const float4 n0 = pub[nb.x], n1 = pub[nb.y], n2 = pub[nb.z], n3 = pub[nb.w];
-    float lx = a.lam_c[o], li = a.lam_im[o], ci = a.lam_cim[o];
-    float4 cm = a.lam_c4[o];
+    float lx = a.lam_c[o], li = a.lam_im[o];
+    float ci;
+    float4 cm;
+    if (a.lam_c4q) {
+      cm = comp_load4(a.lam_c4q[o]);
+      ci = comp_load1(a.lam_cimq[o]);
+    } else {
+      cm = a.lam_c4[o];
+      ci = a.lam_cim[o];
+    }
     // transposed diffusion: S = sum_k aT_k lambda(nb_k) - (sum_k a_k + kb) lambda(self)
     float Sc = at.x * n0.x;
     Sc = fmaf(at.y, n1.x, Sc);
@@ -157,8 +168,13 @@ __global__ void __launch_bounds__(ADJP_THREADS) k_adjp_step(AdjPlainArgs a) {
     kadd(L.w, cm.w, k.dt * lt.oy);
     kadd(li, ci, k.dt * lt.oi);
     a.lam_im[o] = li;
-    a.lam_cim[o] = ci;
-    a.lam_c4[o] = cm;
+    if (a.lam_c4q) {
+      a.lam_c4q[o] = comp_store4(cm);
+      a.lam_cimq[o] = comp_store1(ci);
+    } else {
+      a.lam_cim[o] = ci;
+      a.lam_c4[o] = cm;
+    }
     if (!a.last) {
       const float inj = coef ? plain_injection(a, coef, j) : 0.0f;
       a.nxt[o] = make_float4(L.x * a.ib[o], L.y, L.z, L.w + inj);

@@ -2606,6 +2606,10 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     pa.lam_im = lam_im;
     pa.lam_cim = lam_cim;
     pa.lam_c4 = lam_c4;
+    if (s->d_CMq) {  // large mesh: lambda's compensation as halves (the buffers are big enough)
+      pa.lam_c4q = reinterpret_cast<ushort4*>(lam_c4);
+      pa.lam_cimq = reinterpret_cast<uint16_t*>(lam_cim);
+    }
     pa.lam = lam;
     pa.part = part;
     pa.k = s->a32.k;
@@ -2742,9 +2746,22 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     hi.resize((size_t)R * NE);
     hci.resize((size_t)R * NE);
     SRS_CUDA(cudaMemcpyAsync(hl.data(), lam, sizeof(float4) * R * NE, cudaMemcpyDeviceToHost, s->st));
-    SRS_CUDA(cudaMemcpyAsync(hc.data(), lam_c4, sizeof(float4) * R * NE, cudaMemcpyDeviceToHost, s->st));
     SRS_CUDA(cudaMemcpyAsync(hi.data(), lam_im, sizeof(float) * R * NE, cudaMemcpyDeviceToHost, s->st));
-    SRS_CUDA(cudaMemcpyAsync(hci.data(), lam_cim, sizeof(float) * R * NE, cudaMemcpyDeviceToHost, s->st));
+    if (plain && s->d_CMq) {
+      std::vector<ushort4> q4((size_t)R * NE);
+      std::vector<uint16_t> q1((size_t)R * NE);
+      SRS_CUDA(cudaMemcpyAsync(q4.data(), lam_c4, sizeof(ushort4) * R * NE, cudaMemcpyDeviceToHost, s->st));
+      SRS_CUDA(cudaMemcpyAsync(q1.data(), lam_cim, sizeof(uint16_t) * R * NE, cudaMemcpyDeviceToHost, s->st));
+      SRS_CUDA(cudaStreamSynchronize(s->st));
+      for (size_t e = 0; e < q4.size(); ++e) {
+        hc[e] = make_float4(comp_decode_host(q4[e].x), comp_decode_host(q4[e].y), comp_decode_host(q4[e].z),
+                            comp_decode_host(q4[e].w));
+        hci[e] = comp_decode_host(q1[e]);
+      }
+    } else {
+      SRS_CUDA(cudaMemcpyAsync(hc.data(), lam_c4, sizeof(float4) * R * NE, cudaMemcpyDeviceToHost, s->st));
+      SRS_CUDA(cudaMemcpyAsync(hci.data(), lam_cim, sizeof(float) * R * NE, cudaMemcpyDeviceToHost, s->st));
+    }
   }
   SRS_CUDA(cudaStreamSynchronize(s->st));
   SRS_CUDA(cudaGetLastError());

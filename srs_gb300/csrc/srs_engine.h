@@ -299,6 +299,11 @@ struct AdjPlainArgs {
   float* lam_im;
   float* lam_cim;
   float4* lam_c4;
+  // compact compensation of lambda (srs_comp.h; meshes of PLAIN32_SPLIT_N
+  // elements and more, like the forward state): when set, these replace
+  // lam_c4 / lam_cim
+  ushort4* lam_c4q;
+  uint16_t* lam_cimq;
   float4* lam;             // boundary lambda (Ca, ATP, CMDN, dye)
   double* part;            // [R][blocks][SRS_N_ADJ] FP64 gradient rows of the blocks
   Consts32 k;

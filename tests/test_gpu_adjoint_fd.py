@@ -76,3 +76,63 @@ def test_adjoint_matches_finite_differences_over_20000_steps(srs):
     for name in ("A_P", "K_ON_CMDN", "K_OFF_CMDN", "K_ON_TRPN", "K_OFF_TRPN", "B_TOT_SL_HI",
                  "K_D_SL_HI"):
         assert report[name][1] != 0.0, name
+
+
+def test_large_mesh_plain_adjoint_matches_finite_differences(srs, tmp_path):
+    """The plain engine's adjoint on a mesh of 65,536 elements and more, where
+    the forward state and lambda keep their compensation terms as halves:
+    1024 steps of the spark source with gating off against central
+    differences of the FP64 engine (h = 1e-4 |theta|), 1e-3 relative on every
+    parameter the horizon resolves."""
+    base = str(tmp_path / "big")
+    rep = srs.write_box_mesh(base, box_x=3.0, box_y=3.0, box_z=3.0, foot_half_x=0.3,
+                             foot_half_y=0.3, n_foot_x=10, n_foot_y=10, n_out_x=6, n_out_y=6,
+                             n_above_z=22)
+    assert rep["n_tets"] >= 65536
+    n, te = 1024, 128
+    desc = dict(axis=0, offset1=0.0, offset2=0.1, x_min=-1.0, x_max=1.0, res=0.05, var_x=0.0289,
+                var_y=0.1154, var_z=0.0289, r_thresh=1.0, f0_pad=0.0, pad_res=0.0, pad_min=0.0,
+                pad_max=0.0, domain=(0, 0, 0, 0, 0, 0))
+    p0 = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24, FLAG_NO_GATING=1)
+
+    def make(p, prec):
+        s = srs.Simulation(srs.Grid(p, base), p, 1, prec, srs.ENGINE_PLAIN, seeds=[3])
+        s.reset()
+        s.linescan_setup(**desc)
+        return s
+
+    sim = make(p0, srs.FP32)
+    _, f0 = sim.linescan()
+    start = sim.get_state(0)
+    target = np.random.default_rng(9).standard_normal((n // te, len(f0))) * 0.01
+    loss, grad, _ = sim.adjoint(n, te, f0, target[None], checkpoint_every=256)
+
+    def loss_of(p):
+        s = make(p, srs.FP64)
+        s.set_state(0, start["states"], start["ryr"], start["lcc"], start["lccv"], start["residuals"])
+        L = 0.0
+        for k in range(n // te):
+            s.explicit_step(te)
+            F, _ = s.linescan()
+            e = F[0] / f0 - 1.0 - target[k]
+            L += 0.5 * float((e * e).sum())
+        return L
+
+    L0 = loss_of(p0)
+    assert abs(loss[0] - L0) <= 1e-5 * L0
+    checked, bad = [], {}
+    for k, name in enumerate(srs.ADJ_PARAMS):
+        idx = srs.R[name]
+        h = 1e-4 * abs(p0.reals[idx])
+        hi, lo = p0.copy(), p0.copy()
+        hi.reals[idx] += h
+        lo.reals[idx] -= h
+        Lp, Lm = loss_of(hi), loss_of(lo)
+        if abs(Lp - Lm) < 1e-9 * L0:
+            continue  # below the loss's rounding over this horizon
+        fd = (Lp - Lm) / (2 * h)
+        if not abs(grad[0, k] - fd) <= 1e-3 * abs(fd):
+            bad[name] = (float(grad[0, k]), fd)
+        checked.append(name)
+    assert not bad, bad
+    assert {"D_CA", "K_ON_DYE", "K_OFF_DYE", "V_RYR"} <= set(checked), checked
