@@ -65,6 +65,8 @@ class Oracle:
         L.or_logf.restype = C.c_float
         L.or_exp2f.argtypes = [C.c_float]
         L.or_exp2f.restype = C.c_float
+        L.or_comp_round_trip.argtypes = [C.c_float]
+        L.or_comp_round_trip.restype = C.c_float
         L.or_log.argtypes = [C.c_double]
         L.or_log.restype = C.c_double
         L.or_philox4x32_10.argtypes = [vp, C.c_uint32, C.c_uint32, vp]

@@ -1228,6 +1228,9 @@ static float comp_round_trip(float c) {
   return (float)h * (1.0f / 16777216.0f);
 }
 
+/* the round trip alone, for tests */
+float or_comp_round_trip(float c) { return comp_round_trip(c); }
+
 /* flags: bit 0 gating, bit 1 compact compensation */
 void or_steps_fp32(const or_mesh* m, const double* R, const double* G, float* U, float* Im, float* CM,
                    float* CI, uint64_t seed, int64_t step0, int64_t n, int* ryr, int* lcc, int* lccv,

@@ -74,6 +74,8 @@ int64_t or_run_simulation(const or_mesh* m, const int* ints, const double* reals
 void or_fp32_to_dev(const or_mesh* m, const double* reals, const double* states, float* U, float* Im);
 void or_fp32_from_dev(const or_mesh* m, const double* reals, const float* U, const float* Im,
                       const float* CM, const float* CI, double* states);
+/* The compact compensation term's round trip: float(half(clamp(c 2^24))) 2^-24. */
+float or_comp_round_trip(float c);
 /* CM (4N) and CI (N) hold the compensation terms of the Euler update.
  * flags: bit 0 gating, bit 1 compact (16-bit) compensation terms. */
 void or_steps_fp32(const or_mesh* m, const double* reals, const double* globals, float* U, float* Im,
