@@ -17,8 +17,6 @@ Together these test that the two mixtures are the same distribution.  Atom
 runs are identified by the same exact criterion in both ensembles (counts of
 open channels at the output ticks, which both report exactly).
 """
-import numpy as np
-
 
 def mixture_ks(ref, gpu, ref_atom, gpu_atom, names, p_min=0.01):
     """ref, gpu: [runs][metrics]; *_atom: boolean masks.  Returns

@@ -9,12 +9,10 @@ Bars:
   * FP32 engines vs FP64: relative error <= 1e-5 on concentrations
     (|c32 - c64| / max(|c64|, 1e-3 uM)) over the deterministic part.
 """
-import os
-
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, GOLDEN_MESH, params_from_golden
+from conftest import GOLDEN_MESH, params_from_golden
 
 pytestmark = pytest.mark.gpu
 TOL32 = 1e-5
