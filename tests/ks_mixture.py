@@ -18,6 +18,7 @@ runs are identified by the same exact criterion in both ensembles (counts of
 open channels at the output ticks, which both report exactly).
 """
 
+
 def mixture_ks(ref, gpu, ref_atom, gpu_atom, names, p_min=0.01):
     """ref, gpu: [runs][metrics]; *_atom: boolean masks.  Returns
     (report, failures): report[name] = (p, ref mean, gpu mean) over the
