@@ -813,8 +813,10 @@ def run_ours(args):
                                threads_per_cta=tuned["threads_per_cta"])
         cfg_e = sim_e.config()
         sim_e.run_simulation()  # warm
+        clocks_e = Clocks(local)
         barrier(dist)
         torch.cuda.synchronize()
+        clocks_e.start()
         t0 = time.perf_counter()
         rows_bytes = 0
         t_reset = 0.0
@@ -826,6 +828,7 @@ def run_ours(args):
             rows_bytes = sum(r.nbytes for r in rows)
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.e2e_steps)
+        clk_e = clocks_e.stop()
         reset_ms = 1e3 * t_reset / args.e2e_steps
         e2e_val = ws * R * S * DT_MS / e2e_s
         row_cap = int(pe.reals[0] / pe.reals[2]) + 8
@@ -834,7 +837,7 @@ def run_ours(args):
         e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": cfg_e["reset_h2d_bytes"],
                "d2h_bytes_per_step": d2h,
                "call": "srs_sim_reset + srs_run_simulation (%d steps, rows %d B)" % (S, rows_bytes),
-               "reset_ms": reset_ms, "ms_per_step": 1e3 * e2e_s}
+               "reset_ms": reset_ms, "ms_per_step": 1e3 * e2e_s, "clocks": clk_e}
 
     # secondary legs: a failure is reported in the line, not fatal to it
     err64 = None

@@ -370,11 +370,11 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
               float g;
               a.traj_u[o] = src[i];
               const float im0 = immb[i];
-              tet_update(k, src[i], im0, n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
+              tet_update_x2(k, src[i], im0, n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
                          &out, &imo, &g);
               a.traj_ig[o] = make_float2(im0, g);
             } else {
-              tet_update(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
+              tet_update_x2(k, src[i], immb[i], n0, n1, n2, n3, ga, fl, gb.z, 0.0f, flux, cm, ci,
                          &out, &imo);
             }
             dst[i] = out;
