@@ -123,7 +123,7 @@ __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); 
 // tet_update with the four mobile species as two packed pairs, (Ca, ATP)
 // and (CMDN, dye): every lane performs the scalar operations of tet_update
 // in the same order, so the two give bit-identical results.  The resident
-// engine uses it (fewer issued instructions: 250.2 -> 248.0 ms per bench
+// engine uses it (fewer issued instructions: 251.4 -> 249.3 ms per bench
 // launch); the plain engine keeps the scalar form, which measured faster at
 // its 40-register budget (0.442 against 0.492 ms per large-mesh step).
 __device__ __forceinline__ void tet_update_x2(const Consts32& k, float4 o, float im, float4 s1,
