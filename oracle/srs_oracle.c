@@ -1223,7 +1223,7 @@ static void fp32_element(const or_k32* k, const float* o, float im, const float*
 static float comp_round_trip(float c) {
   float v = c * 16777216.0f;
   _Float16 h;
-  v = fminf(fmaxf(v, -65504.0f), 65504.0f);
+  if (v == v) v = fminf(fmaxf(v, -65504.0f), 65504.0f); /* a NaN stays a NaN */
   h = (_Float16)v;
   return (float)h * (1.0f / 16777216.0f);
 }

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(ADJP_THREADS, 4) k_adjp_step(AdjPlainArgs a) {
     float ci;
     float4 cm;
     if (a.lam_c4q) {
-      cm = comp_load4(a.lam_c4q[o]);
+      cm = comp_load4_x2(a.lam_c4q + o);
       ci = comp_load1(a.lam_cimq[o]);
     } else {
       cm = a.lam_c4[o];
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(ADJP_THREADS, 4) k_adjp_step(AdjPlainArgs a) {
     kadd(li, ci, k.dt * lt.oi);
     a.lam_im[o] = li;
     if (a.lam_c4q) {
-      a.lam_c4q[o] = comp_store4(cm);
+      comp_store4_x2(a.lam_c4q + o, cm);
       a.lam_cimq[o] = comp_store1(ci);
     } else {
       a.lam_cim[o] = ci;

@@ -76,7 +76,7 @@ __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int
     float4 cm;
     float ci;
     if (a.CMq) {  // compact compensation (srs_comp.h)
-      cm = comp_load4(a.CMq[o]);
+      cm = comp_load4(a.CMq + o);
       ci = comp_load1(a.CIq[o]);
     } else {
       cm = a.CM[o];
@@ -98,7 +98,7 @@ __device__ __forceinline__ void plain32_element(const Plain32Args& a, int r, int
     Mo[j] = out;
     Io[j] = imo;
     if (a.CMq) {
-      a.CMq[o] = comp_store4(cm);
+      comp_store4(a.CMq + o, cm);
       a.CIq[o] = comp_store1(ci);
     } else {
       a.CM[o] = cm;

@@ -32,7 +32,7 @@ __global__ void k_total_ca(MassArgs a) {
       float4 cm;
       float ci;
       if (a.CMq) {  // compact compensation (srs_comp.h)
-        cm = comp_load4(a.CMq[o]);
+        cm = comp_load4(a.CMq + o);
         ci = comp_load1(a.CIq[o]);
       } else {
         cm = a.CM[o];

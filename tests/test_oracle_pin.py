@@ -110,14 +110,15 @@ def test_compact_compensation_round_trip_matches_numpy_float16(oracle):
     """The large-mesh engines keep Euler compensation terms as IEEE halves of
     c * 2^24 (srs_gb300/csrc/srs_comp.h); the oracle's restatement (the
     compiler's _Float16) against numpy's float16 rounding on values across
-    the whole range, subnormal halves and the clamp included."""
+    the whole range, subnormal halves, the clamp and a NaN included."""
     rng = np.random.default_rng(1)
     c = np.concatenate([rng.standard_normal(4000) * 10.0 ** rng.uniform(-14, -6, 4000),
-                        [0.0, -0.0, 2.0 ** -40, -2.0 ** -30, 2.0 ** -25, 1e-3, -1.0]]).astype(np.float32)
+                        [0.0, -0.0, 2.0 ** -40, -2.0 ** -30, 2.0 ** -25, 1e-3, -1.0, np.inf, -np.inf,
+                         np.nan]]).astype(np.float32)
     want = (np.clip(c * np.float32(2 ** 24), -65504, 65504).astype(np.float16).astype(np.float32)
             * np.float32(2.0 ** -24))
     got = np.array([oracle.lib.or_comp_round_trip(float(x)) for x in c], np.float32)
-    assert np.array_equal(got, want)
+    assert np.array_equal(got, want, equal_nan=True)
     # 11 significant bits kept where c * 2^24 is a normal half below the clamp
     big = (np.abs(c) * 2 ** 24 >= 2 ** -14) & (np.abs(c) * 2 ** 24 <= 65504)
     assert np.all(np.abs(got[big] - c[big]) <= np.abs(c[big]) * 2.0 ** -11)
