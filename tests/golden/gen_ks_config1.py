@@ -16,8 +16,9 @@ the states rows give the RyR open counts.  Metrics per run: ks_metrics.py.
 Per-run results go to DIR (one small .npz per run, so an interrupted job
 resumes where it stopped); when all runs are there the script writes
 tests/golden/ks_config1.npz (metrics, RyR open counts per tick, the most
-LCCs open at any tick, the centre dF/F0 traces, the parameter vectors).  A run takes about 110 s on one core of
-a 2.7 GHz x86 host.
+LCCs open at any tick, the centre dF/F0 trace shared by the runs that
+recruit no channel, the parameter vectors).  A run takes about 115 s on one
+core of a 2.7 GHz x86 host.
 """
 import argparse
 import multiprocessing as mp
@@ -94,9 +95,14 @@ def assemble(work, n_runs, dest):
         opens.append(n.astype(np.int8))
         lccs.append(int(rows[:N_TICKS + 1, 3].max()))
         metrics.append(spark_metrics(c, n, TICK_MS))
-    np.savez_compressed(dest, metrics=np.array(metrics), names=np.array(NAMES),
-                        dff0_centre=np.array(centre), n_open=np.array(opens),
-                        max_lcc_open=np.array(lccs, np.int8),
+    # the runs that recruit no RyR and open no LCC share one deterministic
+    # trajectory: keep its trace once, with the spread among those runs
+    metrics, lccs, centre = np.array(metrics), np.array(lccs, np.int8), np.array(centre)
+    atom = (metrics[:, NAMES.index("max_open")] == 1) & (lccs == 0)
+    first = int(np.nonzero(atom)[0][0])
+    spread = float(np.abs(centre[atom] - centre[first][None, :]).max())
+    np.savez_compressed(dest, metrics=metrics, names=np.array(NAMES), n_open=np.array(opens),
+                        max_lcc_open=lccs, atom_trace=centre[first], atom_spread=spread,
                         ints=np.array(list(p.ints)), reals=np.array(list(p.reals)),
                         window_ms=WINDOW_MS, tick_ms=TICK_MS)
     print("wrote", dest, "from", n_runs, "runs")

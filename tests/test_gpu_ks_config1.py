@@ -73,7 +73,8 @@ def test_config1_spark_distributions_match_reference(srs, box_mesh):
     report, bad = mixture_ks(ref, gpu, ref_atom, gpu_atom, NAMES)
     assert not bad, report
     # the atom: one deterministic trajectory, the same as the reference's
-    ref_trace = d["dff0_centre"][np.nonzero(ref_atom)[0][0]].astype(np.float64)
+    assert float(d["atom_spread"]) == 0.0  # one trajectory in the reference too
+    ref_trace = d["atom_trace"].astype(np.float64)
     dff0 = C / C[:, :1] - 1.0
     err = np.abs(dff0[gpu_atom] - ref_trace[None, :]).max()
     assert err <= 2e-5, err
