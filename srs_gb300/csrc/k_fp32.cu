@@ -10,7 +10,8 @@
 // element keeps the rounding error of its last update and feeds it back, so
 // the tiny per-step increments (dt = 9 ns) do not accumulate a rounding bias
 // over millions of steps.  Compensation terms are private to the element's
-// owner thread and never travel to neighbours.
+// owner thread and never travel to neighbours; both engines keep them as
+// halves of c * 2^24 (srs_comp.h), rounded after every update.
 //
 // Two engines share the per-element update `tet_update`:
 //   * k_plain32_step: one launch per time step, state in HBM, grid.y over
@@ -260,7 +261,10 @@ int launch_plain32_prestep(const Plain32Args& a, int write_initial_row, cudaStre
 // Resident FP32 engine: kernel in k_resident.cuh, instantiated in k_res_*.cu
 // ===========================================================================
 size_t resident_smem_bytes(int P, int NR, int NL, int n_chtet, int n_entries) {
-  size_t b = (size_t)P * (3 * sizeof(float4) + 2 * sizeof(float));
+  // per element: two state buffers, the compact compensation terms of the
+  // mobile species, the immobile buffer and its compact compensation term
+  size_t b = (size_t)P * (2 * sizeof(float4) + sizeof(ushort4) + sizeof(float) + sizeof(uint16_t));
+  b = (b + 15) & ~(size_t)15;
   b += sizeof(ResidentSmemTail);
   b += (size_t)(NR + 2 * NL + NR) * sizeof(int32_t);  // ryr, lcc, lccv, lattice counts
   b += (size_t)(2 * NR + 2 * NL) * sizeof(uint32_t);  // channel element offsets, LCC rest

@@ -6,6 +6,7 @@
 #include <type_traits>
 
 #include "srs_cluster.cuh"
+#include "srs_comp.h"
 #include "srs_engine.h"
 #include "srs_fp32_update.cuh"
 #include "srs_protocol.cuh"
@@ -16,8 +17,10 @@ namespace srs {
 // Resident FP32 engine
 // ===========================================================================
 // Shared-memory layout of one CTA (dynamic):
-//   float4 buf[2][P]; float4 cm[P]; float imm[P]; float ci[P]; then this
-//   tail, then the channel block (used by rank 0).
+//   float4 buf[2][P]; ushort4 cm[P]; float imm[P]; ushort ci[P] (the
+//   compensation terms as halves, srs_comp.h: 46 instead of 56 bytes per
+//   element, so that three CTAs of an 8-CTA cluster fit on one SM); then this
+//   tail (16-byte aligned), then the channel block (used by rank 0).
 struct ResidentSmemTail {
   RealCtl ctl;
   uint32_t base[2][16];  // cluster addresses of buf[b] in CTA rank q
@@ -163,11 +166,12 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
   const int P = a.P;
   float4* buf0 = reinterpret_cast<float4*>(smem);
   float4* buf1 = buf0 + P;
-  float4* cmb = buf1 + P;
-  float* immb = reinterpret_cast<float*>(cmb + P);
-  float* cib = immb + P;
+  ushort4* cmq = reinterpret_cast<ushort4*>(buf1 + P);
+  float* immb = reinterpret_cast<float*>(cmq + P);
+  uint16_t* ciq = reinterpret_cast<uint16_t*>(immb + P);
   const int NR = a.C.NR, NL = a.C.NL, NCH = NR + NL;
-  ResidentSmemTail* tail = reinterpret_cast<ResidentSmemTail*>(cib + P);
+  ResidentSmemTail* tail = reinterpret_cast<ResidentSmemTail*>(
+      (reinterpret_cast<uintptr_t>(ciq + P) + 15) & ~(uintptr_t)15);
   int32_t* s_ryr = reinterpret_cast<int32_t*>(tail + 1);
   int32_t* s_lcc = s_ryr + NR;
   int32_t* s_lccv = s_lcc + NL;
@@ -241,8 +245,8 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
     for (int i = tid; i < n_loc; i += nthr) {
       buf0[i] = a.M[roff + i];
       immb[i] = a.I[roff + i];
-      cmb[i] = a.CM[roff + i];
-      cib[i] = a.CI[roff + i];
+      comp_store4(cmq + i, a.CM[roff + i]);
+      ciq[i] = comp_store1(a.CI[roff + i]);
     }
     if (rank == 0) {
       if (tid == 0) tail->ctl = a.CS.ctl[r];
@@ -363,8 +367,8 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
               n2 = ld_dsmem_f4(bs[c2 >> a.off_bits] + (c2 & off_mask) * 16u);
               n3 = ld_dsmem_f4(bs[c3 >> a.off_bits] + (c3 & off_mask) * 16u);
             }
-            float4 out, cm = cmb[i];
-            float imo, ci = cib[i];
+            float4 out, cm = comp_load4(cmq + i);
+            float imo, ci = comp_load1(ciq[i]);
             if constexpr (TRAJ) {
               const size_t o = ((size_t)s * a.R + r) * ((size_t)C * P) + (size_t)rank * P + i;
               float g;
@@ -379,8 +383,8 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
             }
             dst[i] = out;
             immb[i] = imo;
-            cmb[i] = cm;
-            cib[i] = ci;
+            comp_store4(cmq + i, cm);
+            ciq[i] = comp_store1(ci);
           }
           idx = i - hi;
         };
@@ -465,8 +469,8 @@ __global__ void __launch_bounds__(SRS_RESIDENT_MAX_THREADS, 1) k_resident32(Resi
         bad |= !isfinite(fin[i].x);
         a.M[roff + i] = fin[i];
         a.I[roff + i] = immb[i];
-        a.CM[roff + i] = cmb[i];
-        a.CI[roff + i] = cib[i];
+        a.CM[roff + i] = comp_load4(cmq + i);
+        a.CI[roff + i] = comp_load1(ciq[i]);
         if constexpr (TRAJ) {
           const size_t o = ((size_t)a.steps * a.R + r) * ((size_t)C * P) + (size_t)rank * P + i;
           a.traj_u[o] = fin[i];

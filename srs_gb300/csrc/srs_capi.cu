@@ -78,10 +78,9 @@ struct srs_sim {
   double* d_S[2] = {nullptr, nullptr};
   float4* d_M[2] = {nullptr, nullptr};
   float* d_I[2] = {nullptr, nullptr};
-  float4* d_CM = nullptr;  // FP32 engines: Euler compensation terms
+  float4* d_CM = nullptr;  // resident FP32 engine: Euler compensation terms
   float* d_CI = nullptr;
-  // the large-mesh form of the plain FP32 engine keeps them compact
-  // (srs_comp.h) in these instead
+  // the plain FP32 engine keeps them compact (srs_comp.h) in these instead
   ushort4* d_CMq = nullptr;
   uint16_t* d_CIq = nullptr;
   int C = 1, threads = 0, n_clusters = 0, P_stride = 0, off_bits = 0;
@@ -469,13 +468,9 @@ int setup_plain32(srs_sim* s) {
     SRS_TRY(dev_alloc(s, &s->d_M[b], (size_t)s->R * N));
     SRS_TRY(dev_alloc(s, &s->d_I[b], (size_t)s->R * N));
   }
-  if (N >= PLAIN32_SPLIT_N) {
-    SRS_TRY(dev_alloc(s, &s->d_CMq, (size_t)s->R * N));
-    SRS_TRY(dev_alloc(s, &s->d_CIq, (size_t)s->R * N));
-  } else {
-    SRS_TRY(dev_alloc(s, &s->d_CM, (size_t)s->R * N));
-    SRS_TRY(dev_alloc(s, &s->d_CI, (size_t)s->R * N));
-  }
+  // compensation terms as halves (srs_comp.h), as in the resident engine
+  SRS_TRY(dev_alloc(s, &s->d_CMq, (size_t)s->R * N));
+  SRS_TRY(dev_alloc(s, &s->d_CIq, (size_t)s->R * N));
   SRS_TRY(upload_channels_engine_order(s));
   return SRS_OK;
 }
@@ -2606,7 +2601,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     pa.lam_im = lam_im;
     pa.lam_cim = lam_cim;
     pa.lam_c4 = lam_c4;
-    if (s->d_CMq) {  // large mesh: lambda's compensation as halves (the buffers are big enough)
+    if (s->d_CMq) {  // lambda's compensation as halves, like the forward's (the buffers are big enough)
       pa.lam_c4q = reinterpret_cast<ushort4*>(lam_c4);
       pa.lam_cimq = reinterpret_cast<uint16_t*>(lam_cim);
     }

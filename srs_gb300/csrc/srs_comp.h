@@ -2,8 +2,10 @@
 //
 // The FP32 engines keep, per element and species, the rounding error c of
 // the last compensated Euler update t = u + y (Kahan: c = (t - u) - y), and
-// subtract it from the next increment.  |c| <= ulp(t) / 2.  The large-mesh
-// form of the plain FP32 engine stores c as an IEEE half of c * 2^24
+// subtract it from the next increment.  |c| <= ulp(t) / 2.  The FP32
+// engines store c as an IEEE half of c * 2^24 (the plain engine in HBM, the
+// resident engine in shared memory, where it frees the room for a third CTA
+// per SM)
 // (round to nearest even, saturated to the largest finite half; a NaN stays
 // a NaN), 10 bytes per element for the five species instead of 20:
 //   q = half(clamp(c * 2^24, +-65504)),   c' = float(q) * 2^-24.

@@ -29,8 +29,8 @@ def _key(grid, R):
 
 
 def tune_resident(grid, params, R, seeds=None, clusters=(1, 2, 3, 4, 5, 6, 8, 16),
-                  threads=(256, 288, 320, 352, 384, 448, 512, 640), trial_steps=200, repeats=2, use_cache=True,
-                  verbose=False):
+                  threads=(160, 192, 224, 256, 288, 320, 352, 384, 448, 512, 640), trial_steps=200,
+                  repeats=2, use_cache=True, verbose=False):
     """Returns dict(cluster_size, threads_per_cta, ms_per_step, trials).
     Clusters of 16 CTAs (non-portable) are among the candidates: they halve
     the partition of meshes that fit eight CTAs only one CTA per SM."""

@@ -79,8 +79,9 @@ def test_adjoint_matches_finite_differences_over_20000_steps(srs):
 
 
 def test_large_mesh_plain_adjoint_matches_finite_differences(srs, tmp_path):
-    """The plain engine's adjoint on a mesh of 65,536 elements and more, where
-    the forward state and lambda keep their compensation terms as halves:
+    """The plain engine's adjoint on a mesh of 65,536 elements and more (the
+    split forward form; the forward state and lambda keep their compensation
+    terms as halves on every mesh):
     1024 steps of the spark source with gating off against central
     differences of the FP64 engine (h = 1e-4 |theta|), 1e-3 relative on every
     parameter the horizon resolves."""

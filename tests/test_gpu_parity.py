@@ -107,6 +107,9 @@ def test_fp64_deterministic_run_equals_reference_golden(srs):
 
 
 def test_fp32_plain_bit_exact_with_fp32_oracle(srs, oracle):
+    """The plain FP32 engine (Euler compensation terms kept as halves,
+    srs_comp.h) against the oracle's FP32 restatement with the same compact
+    compensation."""
     p = golden_params(srs)
     g = srs.Grid(p, GOLDEN_MESH)
     seeds = [51, 52, 53]
@@ -120,7 +123,7 @@ def test_fp32_plain_bit_exact_with_fp32_oracle(srs, oracle):
         st = m.to_fp32(s0["states"])
         ryr, lcc, lccv, res = (s0["ryr"].copy(), s0["lcc"].copy(), s0["lccv"].copy(),
                                s0["residuals"].copy())
-        m.steps_fp32(st, sd, 0, n, ryr, lcc, lccv, res, gating=True)
+        m.steps_fp32(st, sd, 0, n, ryr, lcc, lccv, res, gating=True, compact=True)
         got = sim.get_state(r)
         assert np.array_equal(got["states"], m.from_fp32(st))
         assert np.array_equal(got["ryr"], ryr) and np.array_equal(got["residuals"], res)
@@ -129,9 +132,8 @@ def test_fp32_plain_bit_exact_with_fp32_oracle(srs, oracle):
 
 def test_fp32_plain_split_form_bit_exact_with_fp32_oracle(srs, oracle, tmp_path):
     """Meshes of 65,536 elements and more take the split form of the plain
-    FP32 step (element update and gating as two launches) and keep the Euler
-    compensation terms in 16-bit form (srs_comp.h): the same results as the
-    oracle's FP32 restatement with compact compensation."""
+    FP32 step (element update and gating as two launches): the same results
+    as the oracle's FP32 restatement with compact compensation."""
     base = str(tmp_path / "big")
     rep = srs.write_box_mesh(base, box_x=3.0, box_y=3.0, box_z=3.0, foot_half_x=0.3,
                              foot_half_y=0.3, n_foot_x=10, n_foot_y=10, n_out_x=6, n_out_y=6,
@@ -158,7 +160,7 @@ def test_fp32_plain_split_form_bit_exact_with_fp32_oracle(srs, oracle, tmp_path)
 
 
 def test_fp32_split_form_error_vs_fp64_over_2ms(srs, tmp_path):
-    """The large-mesh form (compact compensation) over 2 ms (222,224 steps)
+    """The large-mesh (split) form over 2 ms (222,224 steps)
     of the DefaultSpark source with gating off: within 1e-5 relative of the
     FP64 engine at every 0.5 ms checkpoint."""
     base = str(tmp_path / "big")

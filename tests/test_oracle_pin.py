@@ -107,7 +107,7 @@ def test_linescan_restatement_matches_tool_fixture():
 
 
 def test_compact_compensation_round_trip_matches_numpy_float16(oracle):
-    """The large-mesh engines keep Euler compensation terms as IEEE halves of
+    """The FP32 engines keep Euler compensation terms as IEEE halves of
     c * 2^24 (srs_gb300/csrc/srs_comp.h); the oracle's restatement (the
     compiler's _Float16) against numpy's float16 rounding on values across
     the whole range, subnormal halves, the clamp and a NaN included."""
