@@ -21,12 +21,6 @@
 #include <stdint.h>
 #include <string.h>
 
-#ifdef __CUDACC__
-#define SRS_COMP_FN __host__ __device__ __forceinline__
-#else
-#define SRS_COMP_FN inline
-#endif
-
 namespace srs {
 
 constexpr float kCompScale = 16777216.0f;          // 2^24
@@ -51,18 +45,12 @@ inline float comp_half_to_float_host(uint16_t h) {
   return v;
 }
 
-// The clamp of the encoding; a NaN stays a NaN.
-SRS_COMP_FN float comp_clamp(float v) {
-  return v != v ? v : fminf(fmaxf(v, -65504.0f), 65504.0f);
-}
-
 // Host side: the compensation term held in the stored 16 bits.
 inline float comp_decode_host(uint16_t q) { return comp_half_to_float_host(q) * kCompInvScale; }
 
 #ifdef __CUDACC__
-// Device side, the same values.  cvt.rn.satfinite rounds to nearest even and
-// saturates to +-65504 (a NaN stays a NaN), which is the clamp above followed
-// by the rounding; two species per conversion (the scalings are exact:
+// Device side.  cvt.rn.satfinite rounds to nearest even and saturates to
+// +-65504 (a NaN stays a NaN): the clamp of the encoding, then the rounding; two species per conversion (the scalings are exact:
 // powers of two).
 __device__ __forceinline__ uint32_t comp_encode2(float lo, float hi) {
   uint32_t q;
