@@ -50,8 +50,8 @@ inline float comp_decode_host(uint16_t q) { return comp_half_to_float_host(q) * 
 
 #ifdef __CUDACC__
 // Device side.  cvt.rn.satfinite rounds to nearest even and saturates to
-// +-65504 (a NaN stays a NaN): the clamp of the encoding, then the rounding; two species per conversion (the scalings are exact:
-// powers of two).
+// +-65504 (a NaN stays a NaN): the clamp of the encoding, then the rounding;
+// two species per conversion (the scalings are exact: powers of two).
 __device__ __forceinline__ uint32_t comp_encode2(float lo, float hi) {
   uint32_t q;
   asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(q) : "f"(hi * kCompScale), "f"(lo * kCompScale));
