@@ -299,14 +299,18 @@ def test_grid_snapshots_during_run(srs, engine, prec):
         assert np.array_equal(sim.get_state(r)["states"], ref.get_state(r)["states"])
 
 
-def test_resident_on_config_mesh_matches_plain(srs, box_mesh):
+@pytest.mark.parametrize("cluster,threads", [(0, 0), (5, 320), (6, 256), (8, 192)])
+def test_resident_on_config_mesh_matches_plain(srs, box_mesh, cluster, threads):
+    """The default placement and the bench's tuned ones (two CTAs of a
+    5-CTA cluster per SM, three of an 8-CTA cluster)."""
     base, _ = box_mesh
     p = srs.default_parameters().set(T_STEP=9e-6, FLAG_CLOCK_SEED=0, INIT_RYR=24,
                                      INIT_RYR_HOLD=10.0)
     g = srs.Grid(p, base)
     seeds = list(range(1, 5))
     pl = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_PLAIN, seeds=seeds)
-    rs = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds)
+    rs = srs.Simulation(g, p, len(seeds), srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                        cluster_size=cluster, threads_per_cta=threads)
     cfg = rs.config()
     assert cfg["cluster_size"] >= 2  # 10,368 elements do not fit one CTA's shared memory
     pl.explicit_step(600)
