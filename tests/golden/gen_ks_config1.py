@@ -15,9 +15,9 @@ the states rows give the RyR open counts.  Metrics per run: ks_metrics.py.
 
 Per-run results go to DIR (one small .npz per run, so an interrupted job
 resumes where it stopped); when all runs are there the script writes
-tests/golden/ks_config1.npz (metrics, RyR open counts per tick, the most
-LCCs open at any tick, the centre dF/F0 trace shared by the runs that
-recruit no channel, the parameter vectors).  A run takes about 115 s on one
+tests/golden/ks_config1.npz (metrics, the most LCCs open at any tick, which
+runs open no channel besides the held RyR and the centre dF/F0 trace they
+share, the parameter vectors).  A run takes about 115 s on one
 core of a 2.7 GHz x86 host.
 """
 import argparse
@@ -31,6 +31,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, HERE)
 
 WINDOW_MS = 3.0
@@ -81,9 +82,10 @@ def _run(args):
 
 def assemble(work, n_runs, dest):
     from ks_metrics import NAMES, spark_metrics
+    from ks_mixture import atom_mask
     p = params()
     ns = int((LINESCAN["x_max"] - LINESCAN["x_min"]) / LINESCAN["res"])
-    centre, opens, lccs, metrics = [], [], [], []
+    centre, lccs, metrics = [], [], []
     for i in range(n_runs):
         d = np.load(os.path.join(work, "run%05d.npz" % i))
         ls, rows = d["ls"], d["rows"]
@@ -91,18 +93,19 @@ def assemble(work, n_runs, dest):
             raise SystemExit("run %d: %d line-scan rows, %d states rows" % (i, len(ls), len(rows)))
         c = ls[:N_TICKS + 1, 1 + ns // 2]
         n = rows[:N_TICKS + 1, 2]
-        centre.append((c / c[0] - 1.0).astype(np.float32))
-        opens.append(n.astype(np.int8))
+        centre.append(c.astype(np.float64))
         lccs.append(int(rows[:N_TICKS + 1, 3].max()))
         metrics.append(spark_metrics(c, n, TICK_MS))
-    # the runs that recruit no RyR and open no LCC share one deterministic
-    # trajectory: keep its trace once, with the spread among those runs
+    # The runs in which no channel opens besides the held RyR share one
+    # deterministic trajectory, so their line-scan traces are bit-identical:
+    # the atom is the set of runs whose trace equals the most frequent one.
+    # (The open counts at the ticks cannot tell: a RyR or an LCC may open and
+    # close again between two ticks.)
     metrics, lccs, centre = np.array(metrics), np.array(lccs, np.int8), np.array(centre)
-    atom = (metrics[:, NAMES.index("max_open")] == 1) & (lccs == 0)
-    first = int(np.nonzero(atom)[0][0])
-    spread = float(np.abs(centre[atom] - centre[first][None, :]).max())
-    np.savez_compressed(dest, metrics=metrics, names=np.array(NAMES), n_open=np.array(opens),
-                        max_lcc_open=lccs, atom_trace=centre[first], atom_spread=spread,
+    atom = atom_mask(centre)
+    mode = centre[np.nonzero(atom)[0][0]]
+    np.savez_compressed(dest, metrics=metrics, names=np.array(NAMES), max_lcc_open=lccs, atom=atom,
+                        atom_dff0=(mode / mode[0] - 1.0),
                         ints=np.array(list(p.ints)), reals=np.array(list(p.reals)),
                         window_ms=WINDOW_MS, tick_ms=TICK_MS)
     print("wrote", dest, "from", n_runs, "runs")

@@ -14,9 +14,24 @@ reason that is not stochastic.  The mixture is compared in parts instead:
               checks it at the deterministic tolerance)
 
 Together these test that the two mixtures are the same distribution.  Atom
-runs are identified by the same exact criterion in both ensembles (counts of
-open channels at the output ticks, which both report exactly).
+runs are identified by the same exact criterion in both ensembles: counts of
+open channels at the output ticks (golden-mesh test), or a recorded trace
+bit-identical to the ensemble's most frequent one (atom_mask; config-1 test,
+where a channel may open and close again between two ticks).
 """
+
+
+def atom_mask(traces):
+    """Runs whose trace is bit-identical to the most frequent trace.  The runs
+    in which no channel opens besides the held RyR follow one deterministic
+    trajectory, which an engine computes the same way in every run."""
+    import numpy as np
+    keys = [t.tobytes() for t in np.ascontiguousarray(traces)]
+    counts = {}
+    for k in keys:
+        counts[k] = counts.get(k, 0) + 1
+    mode = max(counts, key=counts.get)
+    return np.array([k == mode for k in keys])
 
 
 def mixture_ks(ref, gpu, ref_atom, gpu_atom, names, p_min=0.01):
