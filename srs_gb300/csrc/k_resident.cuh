@@ -19,8 +19,9 @@ namespace srs {
 // Shared-memory layout of one CTA (dynamic):
 //   float4 buf[2][P]; ushort4 cm[P]; float imm[P]; ushort ci[P] (the
 //   compensation terms as halves, srs_comp.h: 46 instead of 56 bytes per
-//   element, so that three CTAs of an 8-CTA cluster fit on one SM); then this
-//   tail (16-byte aligned), then the channel block (used by rank 0).
+//   element, so that more CTAs share an SM -- for the 10,368-element dyad two
+//   of a 5-CTA cluster, or three of an 8-CTA one); then this tail (16-byte
+//   aligned), then the channel block (used by rank 0).
 struct ResidentSmemTail {
   RealCtl ctl;
   uint32_t base[2][16];  // cluster addresses of buf[b] in CTA rank q

@@ -4,8 +4,8 @@
 // the last compensated Euler update t = u + y (Kahan: c = (t - u) - y), and
 // subtract it from the next increment.  |c| <= ulp(t) / 2.  The FP32
 // engines store c as an IEEE half of c * 2^24 (the plain engine in HBM, the
-// resident engine in shared memory, where it frees the room for a third CTA
-// per SM)
+// resident engine in shared memory, where the smaller footprint lets more
+// CTAs share an SM)
 // (round to nearest even, saturated to the largest finite half; a NaN stays
 // a NaN), 10 bytes per element for the five species instead of 20:
 //   q = half(clamp(c * 2^24, +-65504)),   c' = float(q) * 2^-24.
