@@ -4,8 +4,9 @@ tests/golden/ks_config1.npz holds 1000 runs of the reference's own
 cpu/RunSimulation.cpp (glibc rand() gating, ensemble indices 0..999) on the
 10,368-element box dyad with the DefaultSpark parameters (RyR 24 opened at
 t = 0 and held for 10 ms), the first 3 ms of each spark, written by
-tests/golden/gen_ks_config1.py: per run the Fluo-4 line scan through the
-cluster centre and the RyR open counts at every 0.01 ms tick.  Here the
+tests/golden/gen_ks_config1.py: per run the spark metrics of the Fluo-4
+line scan through the cluster centre and of the RyR open counts, both taken
+at every 0.01 ms tick.  Here the
 same workload runs as 1000 realizations of the FP32 resident engine
 (Philox gating, seeds 1..1000), the line scan taken on the device at the
 same grid-file ticks, and the same metrics (srs_gb300/metrics.py) are
