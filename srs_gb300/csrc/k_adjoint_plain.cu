@@ -13,9 +13,9 @@
 //     lambda_ATP, lambda_CMDN, lambda_dye + tick injection), double
 //     buffered; lambda_ATP/CMDN/dye have no other owner storage inside a
 //     segment;
-//   * lam_c, lam_im, lam_c4, lam_cim: the owner state (lambda_Ca, the
-//     immobile buffer's lambda, their Kahan compensation; on large meshes
-//     the compensation is kept as halves, lam_c4q / lam_cimq, srs_comp.h);
+//   * lam_c, lam_im, lam_c4q, lam_cimq: the owner state (lambda_Ca, the
+//     immobile buffer's lambda, their Kahan compensation as halves,
+//     srs_comp.h);
 //   * lam: the full lambda at the segment boundaries.
 // The transposed diffusion operator gathers the four neighbours' slots with
 // the transposed coefficients aT; Dirichlet faces (kb) join the diagonal, and
@@ -89,15 +89,8 @@ __global__ void __launch_bounds__(ADJP_THREADS, 4) k_adjp_step(AdjPlainArgs a) {
     const float4 me = pub[j];
     const float4 n0 = pub[nb.x], n1 = pub[nb.y], n2 = pub[nb.z], n3 = pub[nb.w];
     float lx = a.lam_c[o], li = a.lam_im[o];
-    float ci;
-    float4 cm;
-    if (a.lam_c4q) {
-      cm = comp_load4_x2(a.lam_c4q + o);
-      ci = comp_load1(a.lam_cimq[o]);
-    } else {
-      cm = a.lam_c4[o];
-      ci = a.lam_cim[o];
-    }
+    float4 cm = comp_load4_x2(a.lam_c4q + o);
+    float ci = comp_load1(a.lam_cimq[o]);
     // transposed diffusion: S = sum_k aT_k lambda(nb_k) - (sum_k a_k + kb) lambda(self)
     float Sc = at.x * n0.x;
     Sc = fmaf(at.y, n1.x, Sc);
@@ -168,13 +161,8 @@ __global__ void __launch_bounds__(ADJP_THREADS, 4) k_adjp_step(AdjPlainArgs a) {
     kadd(L.w, cm.w, k.dt * lt.oy);
     kadd(li, ci, k.dt * lt.oi);
     a.lam_im[o] = li;
-    if (a.lam_c4q) {
-      comp_store4_x2(a.lam_c4q + o, cm);
-      a.lam_cimq[o] = comp_store1(ci);
-    } else {
-      a.lam_cim[o] = ci;
-      a.lam_c4[o] = cm;
-    }
+    comp_store4_x2(a.lam_c4q + o, cm);
+    a.lam_cimq[o] = comp_store1(ci);
     if (!a.last) {
       const float inj = coef ? plain_injection(a, coef, j) : 0.0f;
       a.nxt[o] = make_float4(L.x * a.ib[o], L.y, L.z, L.w + inj);

@@ -2599,12 +2599,10 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     pa.wt_w = s->d_wt_w;
     pa.lam_c = lam_c;
     pa.lam_im = lam_im;
-    pa.lam_cim = lam_cim;
-    pa.lam_c4 = lam_c4;
-    if (s->d_CMq) {  // lambda's compensation as halves, like the forward's (the buffers are big enough)
-      pa.lam_c4q = reinterpret_cast<ushort4*>(lam_c4);
-      pa.lam_cimq = reinterpret_cast<uint16_t*>(lam_cim);
-    }
+    // lambda's compensation as halves, like the forward's (the buffers are
+    // big enough)
+    pa.lam_c4q = reinterpret_cast<ushort4*>(lam_c4);
+    pa.lam_cimq = reinterpret_cast<uint16_t*>(lam_cim);
     pa.lam = lam;
     pa.part = part;
     pa.k = s->a32.k;
@@ -2742,7 +2740,7 @@ int srs_adjoint(srs_sim* s, const srs_adjoint_desc* d, srs_adjoint_out* out) {
     hci.resize((size_t)R * NE);
     SRS_CUDA(cudaMemcpyAsync(hl.data(), lam, sizeof(float4) * R * NE, cudaMemcpyDeviceToHost, s->st));
     SRS_CUDA(cudaMemcpyAsync(hi.data(), lam_im, sizeof(float) * R * NE, cudaMemcpyDeviceToHost, s->st));
-    if (plain && s->d_CMq) {
+    if (plain) {
       std::vector<ushort4> q4((size_t)R * NE);
       std::vector<uint16_t> q1((size_t)R * NE);
       SRS_CUDA(cudaMemcpyAsync(q4.data(), lam_c4, sizeof(ushort4) * R * NE, cudaMemcpyDeviceToHost, s->st));
