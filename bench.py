@@ -83,8 +83,10 @@ def parse():
                     help="realizations of the large-site leg (32: the workload; fewer for profiling)")
     ap.add_argument("--config4-adjoint-steps", type=int, default=1024,
                     help="steps of the large-site adjoint sample (0: skip it)")
-    ap.add_argument("--only", choices=["adjoint", "config0", "config2", "config4"], default=None,
-                    help="run one secondary leg alone and print its JSON (profiling)")
+    ap.add_argument("--only", choices=["adjoint", "config0", "config2", "config4", "blocking"],
+                    default=None,
+                    help="run one secondary leg alone and print its JSON (profiling; 'blocking': "
+                         "the temporal-blocking measurement of the large site)")
     ap.add_argument("--adjoint-checkpoint", type=int, default=-1,
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
     ap.add_argument("--config2-ms", type=float, default=2.0,
@@ -610,6 +612,115 @@ def config0_spark(srs, args):
             "spark": dict(zip(NAMES, met)), "spark_metrics": "srs_gb300/metrics.py (centre sample)"}
 
 
+def rcb_tiles(cen, max_tile):
+    """Recursive coordinate bisection of the element centroids cen[N][3]:
+    index arrays of compact tiles of at most max_tile elements."""
+    import numpy as np
+    out, todo = [], [np.arange(len(cen))]
+    while todo:
+        idx = todo.pop()
+        if len(idx) <= max_tile:
+            out.append(idx)
+            continue
+        c = cen[idx]
+        ax = int(np.argmax(c.max(0) - c.min(0)))
+        order = idx[np.argsort(c[:, ax], kind="stable")]
+        h = len(order) // 2
+        todo += [order[:h], order[h:]]
+    return out
+
+
+def blocking_probe(srs, args):
+    """Temporal blocking of the large release site, measured by emulation.
+
+    A blocked scheme loads a tile of the mesh plus a halo k elements deep,
+    runs k time steps on chip (recomputing the halo, whose outer layers go
+    stale one per step) and writes the tile back.  Its two factors are
+    measured separately:
+      halo  the config-4 mesh cut into compact tiles of at most 16,384
+            elements (recursive coordinate bisection of the centroids) and
+            k-hop halos over the face graph: at step s of a block the
+            elements within k - s hops of the tile are updated, so a block
+            updates update_factor times the elements it advances;
+      chip  the resident engine, which is such a blocked step without a
+            halo: each launch loads every realization's state, runs k steps
+            on chip and writes the state back.  It runs the 15,288-element
+            box of the multi-mesh batch (a tile-sized mesh that one cluster
+            holds) with 2016 realizations in flight, the 63 tiles x 32
+            realizations of the site, at k steps per launch.
+    The blocked cost per advanced element-step is chip x update_factor (the
+    halo's extra loads not counted); the plain engine's streaming split form
+    on the site is timed alongside."""
+    import numpy as np
+    from scipy import sparse
+    from srs_gb300 import tuner
+    from srs_gb300 import workloads as wl
+    tmp = tempfile.mkdtemp(prefix="srs_blk_")
+    base4, rep4 = wl.config4_mesh(tmp)
+    p = wl.default_spark_params()
+    g4 = srs.Grid(p, base4)
+    N = g4.n_ele
+    _, nij, _ = g4.operator()
+    fidx = g4.elements()["order"]
+    nodes = np.loadtxt(base4 + ".node", skiprows=1, usecols=(1, 2, 3))
+    ele = np.loadtxt(base4 + ".ele", skiprows=1, usecols=(1, 2, 3, 4), dtype=np.int64) - 1
+    cen = nodes[ele[fidx]].mean(axis=1)
+    rows = np.repeat(np.arange(N), 4)
+    cols = nij.astype(np.int64)
+    ok = (cols >= 0) & (cols < N) & (cols != rows)
+    A = sparse.csr_matrix((np.ones(int(ok.sum()), np.float32), (rows[ok], cols[ok])), shape=(N, N))
+    tiles = rcb_tiles(cen, 16384)
+    K = (1, 2, 4, 8)
+    reach = {k: 0 for k in range(max(K) + 1)}  # elements within k hops of a tile, summed over tiles
+    for t in tiles:
+        v = np.zeros(N, bool)
+        v[t] = True
+        reach[0] += len(t)
+        for k in range(1, max(K) + 1):
+            v = v | (A @ v.astype(np.float32) > 0)
+            reach[k] += int(v.sum())
+    halo = {}
+    for k in K:
+        upd = sum(reach[k - s] for s in range(1, k + 1)) / (k * reach[0])
+        halo[k] = {"halo_elements": reach[k] / reach[0] - 1.0, "update_factor": upd}
+    # streaming split form on the site (32 realizations)
+    s4 = srs.Simulation(g4, p, 32, srs.FP32, srs.ENGINE_PLAIN, seeds=list(range(1, 33)))
+    s4.advance_async(64)
+    s4.synchronize()
+    n4 = 512
+    stream_ps = s4.time_advance(n4) * 1e9 / (n4 * 32 * N)
+    del s4
+    # the on-chip factor on a tile-sized mesh
+    spec = wl.config2_mesh_specs()[1]
+    base1 = os.path.join(tmp, "tile")
+    rep1 = srs.write_box_mesh(base1, **spec)
+    p1 = wl.default_spark_params(T_STEP=wl.stable_dt(p, rep1["max_a0"]))
+    g1 = srs.Grid(p1, base1)
+    R = 2016
+    seeds = list(range(1, R + 1))
+    t = tuner.tune_resident(g1, p1, R, seeds=seeds, clusters=(4, 5, 6, 8),
+                            threads=(192, 256, 320, 384, 512), use_cache=False)
+    chip = {}
+    for k in K:
+        sim = srs.Simulation(g1, p1, R, srs.FP32, srs.ENGINE_RESIDENT, seeds=seeds,
+                             cluster_size=t["cluster_size"], threads_per_cta=t["threads_per_cta"],
+                             steps_per_launch=k)
+        sim.advance_async(8 * k)
+        sim.synchronize()
+        n = 64
+        chip[k] = sim.time_advance(n) * 1e9 / (n * R * g1.n_ele)
+        del sim
+    return {"workload": "temporal blocking of the config-4 site (%d tets) emulated: halo factors from "
+                        "its mesh, the on-chip step from the resident engine on a %d-tet box with %d "
+                        "realizations at k steps per launch" % (N, g1.n_ele, R),
+            "tiles": len(tiles), "tile_elements": reach[0] / len(tiles),
+            "halo": {str(k): halo[k] for k in K},
+            "chip_ps_per_element_step": {str(k): chip[k] for k in K},
+            "chip_config": {"cluster_size": t["cluster_size"], "threads_per_cta": t["threads_per_cta"]},
+            "blocked_ps_per_advanced_element_step": {str(k): chip[k] * halo[k]["update_factor"] for k in K},
+            "streaming_ps_per_element_step": stream_ps}
+
+
 def config4_site(srs, args):
     """Large release site: the multi-site mesh of about a million tets (five
     clusters of 20 / 40 / 60 / 100 / 150 RyRs, one LCC per 7 RyRs), 32
@@ -750,7 +861,8 @@ def run_ours(args):
         if rank == 0:
             legs = {"adjoint": adjoint_cost, "config2": lambda srs_, g_, p_, a_: config2_batch(srs_, a_),
                     "config4": lambda srs_, g_, p_, a_: config4_site(srs_, a_),
-                    "config0": lambda srs_, g_, p_, a_: config0_spark(srs_, a_)}
+                    "config0": lambda srs_, g_, p_, a_: config0_spark(srs_, a_),
+                    "blocking": lambda srs_, g_, p_, a_: blocking_probe(srs_, a_)}
             leg = legs[args.only](srs, grid, p, args)
             print(json.dumps(dict(leg, leg=args.only)))
         return 0
