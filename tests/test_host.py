@@ -279,3 +279,19 @@ def test_oracle_parameter_vectors_match_product(srs):
     ints, reals = op.default_spark(T_FINAL=3.0)
     q = wl.default_spark_params(T_FINAL=3.0)
     assert list(q.ints) == ints and list(q.reals) == reals
+
+
+def test_rcb_tiles_cover_every_element_once_within_the_size():
+    """The tiling of the temporal-blocking measurement (bench.py): recursive
+    coordinate bisection gives disjoint tiles that cover every element, none
+    larger than the bound, each spatially compact along the split axes."""
+    import bench
+    rng = np.random.default_rng(4)
+    cen = rng.random((10000, 3)) * np.array([3.0, 1.0, 1.0])
+    tiles = bench.rcb_tiles(cen, 700)
+    allidx = np.concatenate(tiles)
+    assert len(allidx) == len(cen) and len(np.unique(allidx)) == len(cen)
+    assert max(len(t) for t in tiles) <= 700 and min(len(t) for t in tiles) >= 300
+    # the first cut is along the longest axis (x): every tile lies on one side of it
+    xm = np.median(cen[:, 0])
+    assert all((cen[t, 0] <= xm).all() or (cen[t, 0] >= xm).all() for t in tiles)
