@@ -753,8 +753,10 @@ def config4_site(srs, args):
     sim.set_prefetch(tuned["prefetch_blocks"])
     sim.reset()
     tot0 = sim.total_ca()
-    _, _, n_run, launch_ms = sim.run_simulation(timed=True)
+    rows4, _, n_run, launch_ms = sim.run_simulation(timed=True)
     tot1 = sim.total_ca()
+    # RyR open counts at the states rows (column 2): how far the sparks spread
+    max_open = np.array([float(r[:, 2].max()) if len(r) else 0.0 for r in rows4])
     if len(launch_ms) < 2 or int(n_run.min()) != warm + n:
         raise RuntimeError("config4 run: %d chunks, %d steps" % (len(launch_ms), int(n_run.min())))
     ms = float(launch_ms[1:].sum())
@@ -776,6 +778,8 @@ def config4_site(srs, args):
                          "note": "algorithmic 48 + 44/R B per element-step; peak %s" % peak_kind},
             "prefetch_blocks": tuned["prefetch_blocks"],
             "prefetch_trials": [(t["prefetch_blocks"], t["ms_per_step"]) for t in tuned["trials"]],
+            "ryr_open_max": {"mean": float(max_open.mean()), "max": float(max_open.max()),
+                             "runs_recruiting": int((max_open > 1).sum())},
             "fp64_error": err64, "mass_balance": mass, "mesh_generation_s": t_gen,
             "mesh_load_s": t_load,
             "total_ca_start": np.asarray(tot0)[0].tolist(), "total_ca_end": np.asarray(tot1)[0].tolist()}
