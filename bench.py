@@ -91,6 +91,8 @@ def parse():
                     help="with --only adjoint: one checkpoint interval (0: whole trajectory)")
     ap.add_argument("--config2-ms", type=float, default=2.0,
                     help="simulated window of the multi-mesh batch leg (both protocols)")
+    ap.add_argument("--config2-no-alone", action="store_true",
+                    help="config2: skip the members-one-after-another comparison (long windows)")
     ap.add_argument("--config2-launch-steps", type=int, default=0,
                     help="steps per member launch in one graph replay (0: one states interval)")
     ap.add_argument("--adjoint-threads", type=int, default=0, help="reverse-sweep threads per CTA")
@@ -428,8 +430,8 @@ def config2_batch(srs, args):
     srs_batch_run_simulation (the members' resident launches as branches of
     one CUDA graph, the RunSimulation protocol on: LCC gating and clamp,
     states rows on the device) over the first --config2-ms of both protocols
-    (a bounded sample of the 30 / 100 ms runs; the whole runs are projected
-    from it).  Reported against the same members run one after another
+    (a bounded sample of the 30 / 100 ms runs, each protocol capped at its own
+    length; the whole runs are projected from it).  Reported against the same members run one after another
     (srs_run_simulation each), with the roofline of the batch (algorithmic
     48 + 44/R B per element-step of every member)."""
     import numpy as np
@@ -441,7 +443,7 @@ def config2_batch(srs, args):
     for base, rep_ in wl.config2_meshes(tmp):
         for k, p in enumerate(wl.config2_protocols(rep_["max_a0"])):
             full = p.reals[srs.R["T_FINAL"]]
-            p.set(T_FINAL=W)
+            p.set(T_FINAL=min(W, full))
             g = srs.Grid(p, base)
             seeds = list(range(seed0, seed0 + 32))
             seed0 += 32
@@ -474,14 +476,15 @@ def config2_batch(srs, args):
     sims = make(S, "tune_batch")
     srs.Batch(sims, steps_per_launch=S).time_advance(S)
     # members one after another, each at its own tuned configuration
-    sims = make(S, "tune")
-    torch_sync()
     one_rows, one_each = [], []
-    for sim in sims:
-        t0 = time.perf_counter()
-        one_rows.append(sim.run_simulation())
-        one_each.append(time.perf_counter() - t0)
-    one_s = sum(one_each)
+    if not args.config2_no_alone:
+        sims = make(S, "tune")
+        torch_sync()
+        for sim in sims:
+            t0 = time.perf_counter()
+            one_rows.append(sim.run_simulation())
+            one_each.append(time.perf_counter() - t0)
+    one_s = sum(one_each) if one_each else None
     # the batch
     sims = make(S, "tune_batch")
     b = srs.Batch(sims, steps_per_launch=S)
@@ -490,9 +493,10 @@ def config2_batch(srs, args):
     outs = b.run_simulation()
     batch_s = time.perf_counter() - t0
     spark_ms, alg, per = 0.0, 0.0, []
-    for m, sim, (rows, t_end, n_steps), (rows1, _, n1), t1 in zip(members, sims, outs, one_rows, one_each):
+    alone = list(zip(one_rows, one_each)) if one_each else [((None, None, None), None)] * len(members)
+    for m, sim, (rows, t_end, n_steps), ((rows1, _, n1), t1) in zip(members, sims, outs, alone):
         dt = m["p"].reals[srs.R["T_STEP"]]
-        if not np.array_equal(n_steps, n1):
+        if n1 is not None and not np.array_equal(n_steps, n1):
             raise RuntimeError("batch and one-by-one runs differ in length")
         spark_ms += float(n_steps.sum()) * dt
         alg += float(n_steps.sum()) * m["n_tets"] * (48.0 + 44.0 / sim.R)
@@ -504,7 +508,7 @@ def config2_batch(srs, args):
                     "alone_cluster_size": m["tune"]["cluster_size"],
                     "alone_threads_per_cta": m["tune"]["threads_per_cta"], "steps": int(n_steps.max()),
                     "alone_s": t1, "alone_ps_per_element_step":
-                        1e12 * t1 / (float(n_steps.sum()) * m["n_tets"]),
+                        1e12 * t1 / (float(n_steps.sum()) * m["n_tets"]) if t1 is not None else None,
                     "runs_with_lcc_opening": int(sum(x > 0 for x in lcc_open)),
                     "runs_with_recruited_ryr": int(sum(x > 0 for x in max_open)),
                     "mean_max_open_ryr": float(np.mean(max_open))})
@@ -513,7 +517,7 @@ def config2_batch(srs, args):
     return {"workload": "config2: 4 meshes (6000/15288/29478/60984 tets; 10/25/60/100 RyR) x "
                         "2 protocols x 32 realizations, RunSimulation protocol, first %.3g ms" % W,
             "value": rate, "unit": UNIT, "batch_s": batch_s, "members_one_by_one_s": one_s,
-            "batch_over_one_by_one": one_s / batch_s, "steps_per_launch": S,
+            "batch_over_one_by_one": one_s / batch_s if one_s else None, "steps_per_launch": S,
             "roofline": {"bound": "hbm", "achieved": alg / batch_s / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": alg / batch_s / 1e9 / peak,
                          "note": "effective: algorithmic 48 + 44/R B per element-step of every "
