@@ -119,6 +119,16 @@ def test_compact_compensation_round_trip_matches_numpy_float16(oracle):
             * np.float32(2.0 ** -24))
     got = np.array([oracle.lib.or_comp_round_trip(float(x)) for x in c], np.float32)
     assert np.array_equal(got, want, equal_nan=True)
+    # every finite half value and every midpoint between neighbours (the
+    # round-to-nearest-even ties), scaled back by 2^-24
+    h = np.arange(0, 0x7C00, dtype=np.uint16).view(np.float16).astype(np.float32)
+    mid = (h[:-1] + h[1:]) / np.float32(2.0)  # exact in float32
+    for v in (h, mid, -mid):
+        c = v * np.float32(2.0 ** -24)
+        want = (np.clip(c * np.float32(2 ** 24), -65504, 65504).astype(np.float16).astype(np.float32)
+                * np.float32(2.0 ** -24))
+        got = np.array([oracle.lib.or_comp_round_trip(float(x)) for x in c], np.float32)
+        assert np.array_equal(got, want)
     # 11 significant bits kept where c * 2^24 is a normal half below the clamp
     big = (np.abs(c) * 2 ** 24 >= 2 ** -14) & (np.abs(c) * 2 ** 24 <= 65504)
     assert np.all(np.abs(got[big] - c[big]) <= np.abs(c[big]) * 2.0 ** -11)
