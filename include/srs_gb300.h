@@ -362,6 +362,15 @@ int srs_write_grid_vtk(srs_sim* s, int r, const char* path, int run, int rank, i
 int srs_grid_write_vtk(const srs_grid* g, const double* states, const int* ryr_states,
                        const char* path, int run, int rank, int n, double t);
 
+/* ---- numerics check (no reference counterpart) ------------------------------
+ * The FP32 engines keep their Euler compensation terms as IEEE halves of
+ * c * 2^24 (round to nearest even, saturated to +-65504, a NaN stays a NaN).
+ * out[i] = in[i] after that round trip on the device, through the
+ * four-species form of the forward engines (packed = 0) or of the plain
+ * engine's adjoint (packed = 1); every fifth value through the single form.
+ * For tests of the device codec against a restatement. */
+int srs_comp_round_trip(const float* in, float* out, int64_t n, int packed);
+
 /* ---- synthetic meshes (no reference counterpart beyond the file format of
  * mesh/main.cpp:1305-1364): box dyad, see the generator for the geometry. */
 typedef struct srs_box_mesh_spec {

@@ -219,6 +219,7 @@ _SIGS = {
     "srs_linescan_setup": (C.c_int, [_P, C.POINTER(LinescanDesc), C.POINTER(C.c_int)]),
     "srs_linescan": (C.c_int, [_P, _P, _P]),
     "srs_sim_total_ca": (C.c_int, [_P, _P]),
+    "srs_comp_round_trip": (C.c_int, [_P, _P, C.c_int64, C.c_int]),
     "srs_batch_create": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P)]),
     "srs_batch_destroy": (None, [_P]),
     "srs_batch_advance": (C.c_int, [_P, C.c_int64]),
@@ -263,6 +264,15 @@ def library():
 def explicit_step_fp64_noalloc(desc):
     """srs_explicit_step_fp64_noalloc on a filled NoallocStep."""
     _check(_lib.srs_explicit_step_fp64_noalloc(C.byref(desc)))
+
+
+def comp_round_trip(values, packed=False):
+    """The device's round trip of FP32 compensation terms through their stored
+    halves (srs_comp_round_trip); returns float32."""
+    x = np.ascontiguousarray(values, dtype=np.float32)
+    out = np.empty_like(x)
+    _check(_lib.srs_comp_round_trip(_ptr(x), _ptr(out), int(x.size), int(bool(packed))))
+    return out
 
 
 def default_parameters():

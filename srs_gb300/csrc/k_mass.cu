@@ -9,6 +9,7 @@
 // of the reaction and diffusion terms.  Per realization the kernel returns
 // sum_j V0_j total_j (uM um^3) over the cytosol and over the JSR, summed in
 // double precision whatever the precision of the state.
+#include "srs_comp.h"
 #include "srs_engine.h"
 
 namespace srs {
@@ -65,6 +66,38 @@ __global__ void k_total_ca(MassArgs a) {
 
 int launch_total_ca(const MassArgs& a, int R, cudaStream_t st) {
   k_total_ca<<<R, 256, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// The compact compensation codec of srs_comp.h on the device: out[i] is in[i]
+// after its round trip through the stored half.  Each thread takes five
+// consecutive values, the first four through the four-species form (packed
+// scalings when `packed`, as the plain adjoint stores them), the fifth
+// through the single form.
+__global__ void k_comp_round_trip(const float* in, float* out, int64_t n, int packed) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 5;
+  if (i >= n) return;
+  float v[5];
+  for (int k = 0; k < 5; ++k) v[k] = i + k < n ? in[i + k] : 0.0f;
+  ushort4 q;
+  float4 c4;
+  if (packed) {
+    comp_store4_x2(&q, make_float4(v[0], v[1], v[2], v[3]));
+    c4 = comp_load4_x2(&q);
+  } else {
+    comp_store4(&q, make_float4(v[0], v[1], v[2], v[3]));
+    c4 = comp_load4(&q);
+  }
+  const float r[5] = {c4.x, c4.y, c4.z, c4.w, comp_load1(comp_store1(v[4]))};
+  for (int k = 0; k < 5; ++k)
+    if (i + k < n) out[i + k] = r[k];
+}
+
+int launch_comp_round_trip(const float* in, float* out, int64_t n, int packed, cudaStream_t st) {
+  const int64_t groups = (n + 4) / 5;
+  const int64_t blocks = (groups + 255) / 256;
+  if (blocks > 0x7fffffff) return -1;
+  k_comp_round_trip<<<(unsigned)blocks, 256, 0, st>>>(in, out, n, packed);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

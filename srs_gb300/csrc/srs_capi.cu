@@ -2928,6 +2928,25 @@ int srs_multisite_mesh_write(const srs_multisite_spec* spec, const char* base, i
   return SRS_OK;
 }
 
+int srs_comp_round_trip(const float* in, float* out, int64_t n, int packed) {
+  if (!in || !out || n < 0) return fail(SRS_ERR_INPUT, "bad argument");
+  if (n == 0) return SRS_OK;
+  struct Bufs {  // freed on every return path
+    float* d[2] = {nullptr, nullptr};
+    ~Bufs() {
+      for (float* p : d)
+        if (p) cudaFree(p);
+    }
+  } b;
+  SRS_CUDA(cudaMalloc(&b.d[0], n * sizeof(float)));
+  SRS_CUDA(cudaMalloc(&b.d[1], n * sizeof(float)));
+  SRS_CUDA(cudaMemcpy(b.d[0], in, n * sizeof(float), cudaMemcpyHostToDevice));
+  if (launch_comp_round_trip(b.d[0], b.d[1], n, packed ? 1 : 0, 0))
+    return fail(SRS_ERR_CUDA, "codec kernel launch failed");
+  SRS_CUDA(cudaMemcpy(out, b.d[1], n * sizeof(float), cudaMemcpyDeviceToHost));
+  return SRS_OK;
+}
+
 int srs_box_mesh_write(const srs_box_mesh_spec* spec, const char* base, int* rep_i, double* rep_a0) {
   if (!spec || !base) return fail(SRS_ERR_INPUT, "null argument");
   MeshGenSpec s;

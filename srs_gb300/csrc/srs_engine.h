@@ -195,6 +195,7 @@ struct MassArgs {
   double* out;            // [R][2]: cytosol, JSR
 };
 int launch_total_ca(const MassArgs& a, int R, cudaStream_t st);
+int launch_comp_round_trip(const float* in, float* out, int64_t n, int packed, cudaStream_t st);
 
 // ---- pathwise adjoint (k_adjoint.cu) ---------------------------------------
 // FP32 constants of the Jacobian beyond Consts32.
