@@ -3,11 +3,11 @@
 // The FP32 engines keep, per element and species, the rounding error c of
 // the last compensated Euler update t = u + y (Kahan: c = (t - u) - y), and
 // subtract it from the next increment.  |c| <= ulp(t) / 2.  The FP32
-// engines store c as an IEEE half of c * 2^24 (the plain engine in HBM, the
-// resident engine in shared memory, where the smaller footprint lets more
-// CTAs share an SM)
-// (round to nearest even, saturated to the largest finite half; a NaN stays
-// a NaN), 10 bytes per element for the five species instead of 20:
+// engines store c as an IEEE half of c * 2^24 (round to nearest even,
+// saturated to the largest finite half; a NaN stays a NaN): the plain engine
+// in HBM, the resident engine in shared memory, where the smaller footprint
+// lets more CTAs share an SM.  10 bytes per element for the five species
+// instead of 20:
 //   q = half(clamp(c * 2^24, +-65504)),   c' = float(q) * 2^-24.
 // Concentrations stay below 2^15 uM, so |c * 2^24| <= 2^15 and the clamp only
 // matters for a diverged state; c' keeps 11 significant bits of c (the
@@ -34,6 +34,9 @@ inline float comp_half_to_float_host(uint16_t h) {
   float v;
   if (e == 0) {
     v = (float)m * (1.0f / 16777216.0f);  // subnormal: m * 2^-24, exact
+  } else if (e == 31) {
+    const uint32_t b = 0x7F800000u | (m << 13);  // infinity, or a NaN
+    memcpy(&v, &b, 4);
   } else {
     uint32_t b = ((uint32_t)(e - 15 + 127) << 23) | (m << 13);
     memcpy(&v, &b, 4);
